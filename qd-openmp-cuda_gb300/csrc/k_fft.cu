@@ -1,0 +1,351 @@
+// Batched 2-D FFT over (R, r) of every Legendre slab, fused with the kinetic
+// phase, the kinetic-energy reduction, the 1/(n1 n2) scale, the epilogue
+// rotational phase and the rotational-energy reduction.
+//
+// Reference: cufftPlanMany 2-D Z2Z {n2, n1} batched over l_max+1 slabs
+// (wavepackets1device.cu:186-201), forward/inverse in place
+// (omegawavepacket.cu:242-269), cublasZdscal by 1/(n1 n2), the kinetic kernel
+// (evolutionCUDAaux.cu:13-31) and a per-slab ZDOTC loop for the kinetic energy
+// (omegawavepacket.cu:364-395).  Sign conventions follow cuFFT: forward
+// exp(-2 pi i jk/n), inverse exp(+2 pi i jk/n), both unnormalised.
+//
+// Algorithm: mixed-radix (4, 2, 3) Stockham autosort in shared memory, each
+// stage reading all inputs to registers, a barrier, then writing the outputs
+// in place.  Twiddles exp(-2 pi i t/n) are computed in FP64 on the host; the
+// FP32 variant rounds them.  Three passes: rows (R, contiguous) forward;
+// columns (r, stride n1) forward + kinetic phase + kinetic energy + inverse;
+// rows inverse + scale + epilogue.
+#include "qd_internal.h"
+#include "qd_device.cuh"
+
+#include <cmath>
+#include <vector>
+
+namespace qd {
+
+namespace {
+constexpr int FFT_THREADS = 256;
+constexpr int MAXV = 16;   // complex values per thread per stage
+
+template <typename R> struct CT;
+template <> struct CT<double> {
+  using T = double2;
+  static __device__ inline T make(double x, double y) { return make_double2(x, y); }
+};
+template <> struct CT<float> {
+  using T = float2;
+  static __device__ inline T make(float x, float y) { return make_float2(x, y); }
+};
+
+template <typename C> __device__ inline C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ inline C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ inline C cmulg(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+
+template <typename R, int RAD>
+__device__ inline void dft(typename CT<R>::T *v, bool inv) {
+  using C = typename CT<R>::T;
+  if (RAD == 2) {
+    const C a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  } else if (RAD == 4) {
+    const C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    const C c = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+    C id;   // forward: -i d ; inverse: +i d
+    if (!inv) { id.x = d.y; id.y = -d.x; } else { id.x = -d.y; id.y = d.x; }
+    v[0] = cadd(a, c);
+    v[2] = csub(a, c);
+    v[1] = cadd(b, id);
+    v[3] = csub(b, id);
+  } else if (RAD == 3) {
+    const R h = (R)0.86602540378443864676;   // sqrt(3)/2
+    const C t = cadd(v[1], v[2]);
+    const C x0 = v[0];
+    v[0] = cadd(x0, t);
+    C u;
+    u.x = x0.x - (R)0.5 * t.x;
+    u.y = x0.y - (R)0.5 * t.y;
+    const C s = csub(v[1], v[2]);
+    C w;   // forward: -i h s ; inverse: +i h s
+    if (!inv) { w.x = h * s.y; w.y = -h * s.x; } else { w.x = -h * s.y; w.y = h * s.x; }
+    v[1] = cadd(u, w);
+    v[2] = csub(u, w);
+  }
+}
+
+// One Stockham stage on nrows independent transforms of length N stored at
+// buf[row*rs + x*es].  COLS selects which index varies fastest across threads
+// so that shared-memory accesses stay contiguous.
+template <typename R, int RAD, bool COLS>
+__device__ inline void fft_stage(typename CT<R>::T *buf, int N, int nrows, int rs, int es, int Ns,
+                                 const typename CT<R>::T *__restrict__ tw, bool inv) {
+  using C = typename CT<R>::T;
+  constexpr int NB = (MAXV + RAD - 1) / RAD;
+  const int nbf = N / RAD;
+  const int total = nrows * nbf;
+  const int tstep = N / (Ns * RAD);
+  C v[NB][RAD];
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    const int t = threadIdx.x + FFT_THREADS * q;
+    if (t < total) {
+      const int row = COLS ? (t % nrows) : (t / nbf);
+      const int jj = COLS ? (t / nrows) : (t % nbf);
+      const int k = jj % Ns;
+#pragma unroll
+      for (int r = 0; r < RAD; r++) v[q][r] = buf[row * rs + (jj + r * nbf) * es];
+      if (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < RAD; r++) {
+          C w = tw[r * k * tstep];
+          if (inv) w.y = -w.y;
+          v[q][r] = cmulg(v[q][r], w);
+        }
+      }
+      dft<R, RAD>(v[q], inv);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    const int t = threadIdx.x + FFT_THREADS * q;
+    if (t < total) {
+      const int row = COLS ? (t % nrows) : (t / nbf);
+      const int jj = COLS ? (t / nrows) : (t % nbf);
+      const int k = jj % Ns;
+      const int dst = (jj / Ns) * Ns * RAD + k;
+#pragma unroll
+      for (int r = 0; r < RAD; r++) buf[row * rs + (dst + r * Ns) * es] = v[q][r];
+    }
+  }
+  __syncthreads();
+}
+
+struct Radices {
+  int n, nst;
+  int rad[16];
+};
+
+template <typename R, bool COLS>
+__device__ inline void fft_run(typename CT<R>::T *buf, const Radices &rd, int nrows, int rs, int es,
+                               const typename CT<R>::T *__restrict__ tw, bool inv) {
+  int Ns = 1;
+  for (int s = 0; s < rd.nst; s++) {
+    const int rad = rd.rad[s];
+    if (rad == 4) fft_stage<R, 4, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv);
+    else if (rad == 2) fft_stage<R, 2, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv);
+    else fft_stage<R, 3, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv);
+    Ns *= rad;
+  }
+}
+
+template <typename R> __device__ inline typename CT<R>::T from_d(double2 v) {
+  return CT<R>::make((R)v.x, (R)v.y);
+}
+template <typename C> __device__ inline double2 to_d(C v) { return make_double2((double)v.x, (double)v.y); }
+
+}  // namespace
+
+// ---------------------------------------------------------- rows forward
+template <typename R>
+__global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ psi, Radices rd, int nrows,
+                                                          int64_t n_rows_total, const typename CT<R>::T *__restrict__ tw,
+                                                          int inv, Grid g, double scale,
+                                                          const SlabDesc *__restrict__ slabs,
+                                                          const double2 *__restrict__ tabE,
+                                                          double *__restrict__ re_part, int re_tiles,
+                                                          const int *status) {
+  if (status && *status) return;
+  using C = typename CT<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf = reinterpret_cast<C *>(smem_raw);
+  __shared__ double red[32];
+  const int N = rd.n;
+  const int64_t row0 = (int64_t)blockIdx.x * nrows;
+  const int n = nrows * N;
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int64_t grow = row0 + e / N;
+    buf[e] = grow < n_rows_total ? from_d<R>(psi[grow * N + (e % N)]) : CT<R>::make(0, 0);
+  }
+  __syncthreads();
+  fft_run<R, false>(buf, rd, nrows, N, 1, tw, inv != 0);
+  double re = 0.0;
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int64_t grow = row0 + e / N;
+    if (grow >= n_rows_total) continue;
+    double2 v = to_d(buf[e]);
+    if (scale != 1.0) { v.x *= scale; v.y *= scale; }
+    const int i = e % N;
+    const int64_t sl = grow / g.n2;
+    const int j = (int)(grow % g.n2);
+    if (tabE) {
+      const int l = slabs[sl].l;
+      v = cmul(v, ldg2(tabE + (int64_t)l * g.npt + (int64_t)j * g.n1 + i));
+    }
+    if (re_part) {
+      const int l = slabs[sl].l;
+      const double Rr = g.left1 + i * g.dr1, rr = g.left2 + j * g.dr2;
+      const double I = 1.0 / (2 * g.m1 * Rr * Rr) + 1.0 / (2 * g.m2 * rr * rr);
+      re += (double)l * (l + 1) * I * (v.x * v.x + v.y * v.y);
+    }
+    psi[grow * N + i] = v;
+  }
+  if (re_part) {
+    re = block_sum(re, red);
+    if (threadIdx.x == 0) {
+      const int64_t sl = row0 / g.n2;
+      const int tile = (int)((row0 % g.n2) / nrows);
+      re_part[sl * re_tiles + tile] = re;
+    }
+  }
+}
+
+// ------------------------------------- columns: forward, kinetic, inverse
+template <typename R>
+__global__ void __launch_bounds__(FFT_THREADS) k_fft_cols(double2 *__restrict__ psi, Radices rd, int ncols, Grid g,
+                                                          const typename CT<R>::T *__restrict__ tw,
+                                                          const double2 *__restrict__ tab_kin,
+                                                          const double *__restrict__ T1, const double *__restrict__ T2,
+                                                          double *__restrict__ ke_part, int ke_tiles,
+                                                          const int *status) {
+  if (status && *status) return;
+  using C = typename CT<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf = reinterpret_cast<C *>(smem_raw);
+  __shared__ double red[32];
+  const int N = rd.n;                 // = n2
+  const int tiles = g.n1 / ncols;
+  const int64_t sl = blockIdx.x / tiles;
+  const int tile = blockIdx.x % tiles;
+  const int i0 = tile * ncols;
+  double2 *p = psi + sl * g.npt + i0;
+  const int n = ncols * N;
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int t = e / ncols, c = e % ncols;
+    buf[e] = from_d<R>(p[(int64_t)t * g.n1 + c]);
+  }
+  __syncthreads();
+  fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, false);
+  double ke = 0.0;
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int t = e / ncols, c = e % ncols;
+    double2 v = to_d(buf[e]);
+    v = cmul(v, ldg2(tab_kin + (int64_t)t * g.n1 + i0 + c));
+    ke += (__ldg(T1 + i0 + c) + __ldg(T2 + t)) * (v.x * v.x + v.y * v.y);
+    buf[e] = from_d<R>(v);
+  }
+  __syncthreads();
+  fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, true);
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int t = e / ncols, c = e % ncols;
+    p[(int64_t)t * g.n1 + c] = to_d(buf[e]);
+  }
+  if (ke_part) {
+    ke = block_sum(ke, red);
+    if (threadIdx.x == 0) ke_part[sl * ke_tiles + tile] = ke;
+  }
+}
+
+// ------------------------------------------------------------- host side
+bool fft_factor(int n, int *rad, int *nst) {
+  int k = 0;
+  int m = n;
+  while (m % 4 == 0) { rad[k++] = 4; m /= 4; }
+  while (m % 2 == 0) { rad[k++] = 2; m /= 2; }
+  while (m % 3 == 0) { rad[k++] = 3; m /= 3; }
+  *nst = k;
+  return m == 1 && k <= 16;
+}
+
+static int largest_divisor_at_most(int n, int cap) {
+  for (int d = std::min(n, cap); d >= 1; d--)
+    if (n % d == 0) return d;
+  return 1;
+}
+
+void fft_plan_init(FFTPlan &p, int n1, int n2) {
+  p.n1 = n1;
+  p.n2 = n2;
+  if (!fft_factor(n1, p.rad1, &p.nst1) || !fft_factor(n2, p.rad2, &p.nst2))
+    throw Error{QD_ERR_UNSUPPORTED, "FFT grid sizes must factor into 2 and 3"};
+  if (n1 > FFT_THREADS * MAXV || n2 > FFT_THREADS * MAXV)
+    throw Error{QD_ERR_UNSUPPORTED, "FFT grid size above 4096"};
+  p.rows_per_cta = largest_divisor_at_most(n2, std::max(1, FFT_THREADS * MAXV / n1));
+  p.rows_per_cta = std::min(p.rows_per_cta, largest_divisor_at_most(n2, 64));
+  p.cols_per_cta = largest_divisor_at_most(n1, std::min(32, std::max(1, FFT_THREADS * MAXV / n2)));
+  auto make = [](int n, double2 **d, float2 **f) {
+    std::vector<double2> hd(n);
+    std::vector<float2> hf(n);
+    for (int t = 0; t < n; t++) {
+      const double a = -2.0 * M_PI * (double)t / (double)n;
+      hd[t] = make_double2(std::cos(a), std::sin(a));
+      hf[t] = make_float2((float)hd[t].x, (float)hd[t].y);
+    }
+    QD_CUDA(cudaMalloc(d, n * sizeof(double2)));
+    QD_CUDA(cudaMalloc(f, n * sizeof(float2)));
+    QD_CUDA(cudaMemcpy(*d, hd.data(), n * sizeof(double2), cudaMemcpyHostToDevice));
+    QD_CUDA(cudaMemcpy(*f, hf.data(), n * sizeof(float2), cudaMemcpyHostToDevice));
+  };
+  make(n1, &p.tw1_d, &p.tw1_f);
+  make(n2, &p.tw2_d, &p.tw2_f);
+  // shared-memory opt-in, set outside any stream capture
+  QD_CUDA(cudaFuncSetAttribute(k_fft_rows<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  QD_CUDA(cudaFuncSetAttribute(k_fft_cols<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  QD_CUDA(cudaFuncSetAttribute(k_fft_rows<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  QD_CUDA(cudaFuncSetAttribute(k_fft_cols<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+}
+
+void fft_plan_free(FFTPlan &p) {
+  cudaFree(p.tw1_d);
+  cudaFree(p.tw1_f);
+  cudaFree(p.tw2_d);
+  cudaFree(p.tw2_f);
+  p.tw1_d = p.tw2_d = nullptr;
+  p.tw1_f = p.tw2_f = nullptr;
+}
+
+int fft_col_tiles(const FFTPlan &p) { return p.n1 / p.cols_per_cta; }
+int fft_row_tiles(const FFTPlan &p) { return p.n2 / p.rows_per_cta; }
+
+template <typename R>
+static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j,
+                                 const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1,
+                                 const double *T2, double *ke_part, const double2 *tabE, double *re_part,
+                                 const int *status) {
+  using C = typename CT<R>::T;
+  Radices r1{p.n1, p.nst1, {}}, r2{p.n2, p.nst2, {}};
+  for (int q = 0; q < p.nst1; q++) r1.rad[q] = p.rad1[q];
+  for (int q = 0; q < p.nst2; q++) r2.rad[q] = p.rad2[q];
+  const C *tw1 = std::is_same<R, double>::value ? (const C *)p.tw1_d : (const C *)p.tw1_f;
+  const C *tw2 = std::is_same<R, double>::value ? (const C *)p.tw2_d : (const C *)p.tw2_f;
+  const int64_t rows = (int64_t)n_slabs * g.n2;
+  const size_t sm_rows = (size_t)p.rows_per_cta * p.n1 * sizeof(C);
+  const size_t sm_cols = (size_t)p.cols_per_cta * p.n2 * sizeof(C);
+  const unsigned nrow_ctas = (unsigned)(rows / p.rows_per_cta);
+  k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 0, g, 1.0, slabs,
+                                                        nullptr, nullptr, 0, status);
+  const unsigned ncol_ctas = (unsigned)(n_slabs * (p.n1 / p.cols_per_cta));
+  k_fft_cols<R><<<ncol_ctas, FFT_THREADS, sm_cols, s>>>(psi_j, r2, p.cols_per_cta, g, tw2, tab_kin, T1, T2, ke_part,
+                                                        fft_col_tiles(p), status);
+  k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 1, g,
+                                                        1.0 / ((double)g.n1 * g.n2), slabs, tabE, re_part,
+                                                        fft_row_tiles(p), status);
+}
+
+void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, int precision, double2 *psi_j,
+                        const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1, const double *T2,
+                        double *ke_part, const double2 *tabE, const double *, const double *, double *re_part,
+                        const int *status) {
+  if (n_slabs == 0) return;
+  if (precision == QD_PRECISION_MIXED)
+    launch_fft_kinetic_t<float>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status);
+  else
+    launch_fft_kinetic_t<double>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status);
+}
+
+}  // namespace qd

@@ -1,0 +1,198 @@
+// Energy-resolved flux through the dividing surface r = r_s and the
+// reaction probability P(E).
+//
+// The reference carries the CRP inputs (FH2main.m:182-191,
+// matlabStructures.C:80-90) but computes nothing from them.  Definition used
+// here (standard time-dependent flux analysis, hbar = 1):
+//   psi(t_n) on the stencil rows = exp(-i V dt/2) psi_theta   (completes the
+//     Strang half step that the merged V(dt) of the next step would apply),
+//   A_E(R, x_k) += dt e^{i E t_n} psi(t_n; R, r_s, x_k),
+//   D_E(R, x_k) += dt e^{i E t_n} d/dr psi(t_n; R, r_s, x_k)  (centred FD stencil),
+//   P(E) = Im sum_{Omega,k,i} w_k dR conj(A_E) D_E / (2 pi mu_r |a(E)|^2),
+// with |a(E)|^2 = CRP.eta_sq.  Per step only the stencil rows are read; the
+// time-to-energy transform runs once per chunk of steps as a complex
+// [n_E x chunk] x [chunk x surface] product accumulated in FP64.
+#include "qd_internal.h"
+#include "qd_device.cuh"
+
+namespace qd {
+
+// buf layout: [slot][block][2][nth][n1]
+__global__ void k_flux_extract(Grid g, int n_grad, int n_ds, const double2 *__restrict__ psi_th,
+                               const double2 *__restrict__ hv, const double *__restrict__ fd,
+                               double2 *__restrict__ buf, int n_blocks, int slot, const int *status) {
+  if (status && *status) return;
+  const int b = blockIdx.y;
+  const int h = (n_grad - 1) / 2;
+  const int64_t ns = (int64_t)g.nth * g.n1;
+  double2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
+  const double2 *p = psi_th + (int64_t)b * g.nth * g.npt;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % g.n1), k = (int)(q / g.n1);
+    double2 A = make_double2(0.0, 0.0), D = make_double2(0.0, 0.0);
+    for (int gg = 0; gg < n_grad; gg++) {
+      const int j = n_ds - h + gg;
+      const double2 v = cmul(p[((int64_t)k * g.n2 + j) * g.n1 + i],
+                             ldg2(hv + ((int64_t)k * n_grad + gg) * g.n1 + i));
+      const double c = __ldg(fd + gg);
+      D.x = fma(c, v.x, D.x);
+      D.y = fma(c, v.y, D.y);
+      if (gg == h) A = v;
+    }
+    out[q] = A;
+    out[ns + q] = D;
+  }
+}
+
+void launch_flux_extract(cudaStream_t s, const Grid &g, const FluxConfig &f, const double2 *psi_th, int n_blocks,
+                         const double2 *half_v, const double *fd, double2 *buf, int slot, const int *status) {
+  const int64_t ns = (int64_t)g.nth * g.n1;
+  dim3 grid(grid_for(ns, 256, 64), n_blocks);
+  k_flux_extract<<<grid, 256, 0, s>>>(g, f.n_grad, f.n_ds, psi_th, half_v, fd, buf, n_blocks, slot, status);
+}
+
+// phase[n][E] = dt exp(i E (t0 + n dt))
+__global__ void k_flux_phase(const double *__restrict__ E, int nE, int count, double t0, double dt,
+                             double2 *__restrict__ phase) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nE * count) return;
+  const int n = q / nE, e = q % nE;
+  double s, c;
+  sincos(E[e] * (t0 + n * dt), &s, &c);
+  phase[q] = make_double2(dt * c, dt * s);
+}
+
+namespace {
+constexpr int FLUX_EB = 8;        // energies per thread
+constexpr int FLUX_THREADS = 128; // surface points per CTA
+constexpr int FLUX_MAXC = 64;     // maximum chunk length
+}
+
+// acc[b][c][E][k][i] += sum_n phase[n][E] buf[n][b][c][k][i]
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft(int64_t ns2, int nE, int n_blocks, int count,
+                                                           const double2 *__restrict__ buf,
+                                                           const double2 *__restrict__ phase,
+                                                           double2 *__restrict__ acc, const int *status) {
+  if (status && *status) return;
+  __shared__ double2 ph[FLUX_MAXC][FLUX_EB];
+  const int b = blockIdx.z;
+  const int e0 = blockIdx.y * FLUX_EB;
+  for (int q = threadIdx.x; q < count * FLUX_EB; q += blockDim.x) {
+    const int n = q / FLUX_EB, e = q % FLUX_EB;
+    ph[n][e] = e0 + e < nE ? phase[(int64_t)n * nE + e0 + e] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const int64_t s = (int64_t)blockIdx.x * FLUX_THREADS + threadIdx.x;   // over 2*nth*n1
+  if (s >= ns2) return;
+  double2 a[FLUX_EB];
+#pragma unroll
+  for (int e = 0; e < FLUX_EB; e++) a[e] = make_double2(0.0, 0.0);
+  for (int n = 0; n < count; n++) {
+    const double2 v = buf[((int64_t)n * n_blocks + b) * ns2 + s];
+#pragma unroll
+    for (int e = 0; e < FLUX_EB; e++) {
+      const double2 p = ph[n][e];
+      a[e].x = fma(p.x, v.x, fma(-p.y, v.y, a[e].x));
+      a[e].y = fma(p.x, v.y, fma(p.y, v.x, a[e].y));
+    }
+  }
+  const int64_t ns = ns2 / 2;
+  const int c = (int)(s / ns);
+  const int64_t kq = s % ns;
+#pragma unroll
+  for (int e = 0; e < FLUX_EB; e++) {
+    if (e0 + e >= nE) break;
+    double2 *dst = acc + (((int64_t)b * 2 + c) * nE + e0 + e) * ns + kq;
+    double2 v = *dst;
+    v.x += a[e].x;
+    v.y += a[e].y;
+    *dst = v;
+  }
+}
+
+void launch_flux_dft(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_blocks, const double2 *buf, int count,
+                     const double *energies, double t0, double dt, double2 *phase_scratch, double2 *acc,
+                     const int *status) {
+  if (count <= 0) return;
+  if (count > FLUX_MAXC) throw Error{QD_ERR_INVALID, "flux chunk above 64 steps"};
+  const int nE = f.n_energies;
+  k_flux_phase<<<(nE * count + 255) / 256, 256, 0, s>>>(energies, nE, count, t0, dt, phase_scratch);
+  const int64_t ns2 = 2LL * g.nth * g.n1;
+  dim3 grid((unsigned)((ns2 + FLUX_THREADS - 1) / FLUX_THREADS), (unsigned)((nE + FLUX_EB - 1) / FLUX_EB),
+            (unsigned)n_blocks);
+  k_flux_dft<<<grid, FLUX_THREADS, 0, s>>>(ns2, nE, n_blocks, count, buf, phase_scratch, acc, status);
+}
+
+// Same transform with the step count read from the device, so that it can sit
+// inside a captured CUDA graph; the phase table holds rows n < *count_p.
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_dev(int64_t ns2, int nE, int n_blocks, const int *count_p,
+                                                               const double2 *__restrict__ buf,
+                                                               const double2 *__restrict__ phase,
+                                                               double2 *__restrict__ acc, const int *status) {
+  if (status && *status) return;
+  const int count = min(*count_p, FLUX_MAXC);
+  if (count <= 0) return;
+  __shared__ double2 ph[FLUX_MAXC][FLUX_EB];
+  const int b = blockIdx.z;
+  const int e0 = blockIdx.y * FLUX_EB;
+  for (int q = threadIdx.x; q < count * FLUX_EB; q += blockDim.x) {
+    const int n = q / FLUX_EB, e = q % FLUX_EB;
+    ph[n][e] = e0 + e < nE ? phase[(int64_t)n * nE + e0 + e] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const int64_t s = (int64_t)blockIdx.x * FLUX_THREADS + threadIdx.x;
+  if (s >= ns2) return;
+  double2 a[FLUX_EB];
+#pragma unroll
+  for (int e = 0; e < FLUX_EB; e++) a[e] = make_double2(0.0, 0.0);
+  for (int n = 0; n < count; n++) {
+    const double2 v = buf[((int64_t)n * n_blocks + b) * ns2 + s];
+#pragma unroll
+    for (int e = 0; e < FLUX_EB; e++) {
+      const double2 p = ph[n][e];
+      a[e].x = fma(p.x, v.x, fma(-p.y, v.y, a[e].x));
+      a[e].y = fma(p.x, v.y, fma(p.y, v.x, a[e].y));
+    }
+  }
+  const int64_t ns = ns2 / 2;
+  const int c = (int)(s / ns);
+  const int64_t kq = s % ns;
+#pragma unroll
+  for (int e = 0; e < FLUX_EB; e++) {
+    if (e0 + e >= nE) break;
+    double2 *dst = acc + (((int64_t)b * 2 + c) * nE + e0 + e) * ns + kq;
+    double2 v = *dst;
+    v.x += a[e].x;
+    v.y += a[e].y;
+    *dst = v;
+  }
+}
+
+// P(E) per problem: one CTA per (E, problem)
+__global__ void k_flux_crp(Grid g, int nE, const int *__restrict__ pblock0, const double2 *__restrict__ acc,
+                           const double *__restrict__ w, const double *__restrict__ eta_sq, double *__restrict__ crp) {
+  __shared__ double red[32];
+  const int e = blockIdx.x, pr = blockIdx.y;
+  const int64_t ns = (int64_t)g.nth * g.n1;
+  double s = 0.0;
+  for (int b = pblock0[pr]; b < pblock0[pr + 1]; b++) {
+    const double2 *A = acc + (((int64_t)b * 2 + 0) * nE + e) * ns;
+    const double2 *D = acc + (((int64_t)b * 2 + 1) * nE + e) * ns;
+    for (int64_t q = threadIdx.x; q < ns; q += blockDim.x) {
+      const double2 a = A[q], d = D[q];
+      // Im(conj(a) d) = a.x d.y - a.y d.x
+      s += w[q / g.n1] * (a.x * d.y - a.y * d.x);
+    }
+  }
+  s = block_sum(s, red);
+  if (threadIdx.x == 0)
+    crp[(int64_t)pr * nE + e] = s * g.dr1 / (2.0 * M_PI * g.m2 * eta_sq[(int64_t)pr * nE + e]);
+}
+
+void launch_flux_crp(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_problems, const int *block0_of_problem,
+                     const double2 *acc, const double *w, const double *eta_sq, double *crp) {
+  dim3 grid((unsigned)f.n_energies, (unsigned)n_problems);
+  k_flux_crp<<<grid, 256, 0, s>>>(g, f.n_energies, block0_of_problem, acc, w, eta_sq, crp);
+}
+
+}  // namespace qd

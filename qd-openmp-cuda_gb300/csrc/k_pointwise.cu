@@ -1,0 +1,237 @@
+// Pointwise kernels: phase application, FP64 phase-table builders, energy
+// finalisation and the norm guard.
+//
+// The reference evaluates exp(Complex(0,-dt)*x) per element on every call
+// (evolutionCUDAaux.cu:5-54, complex.h:115).  Here each phase factor is
+// evaluated once per run, in FP64 on the device, into a table; every step then
+// multiplies by the table (one complex multiply per point instead of a sincos,
+// which matters on a part whose FP64 rate is a small fraction of its FP32 rate).
+#include "qd_internal.h"
+#include "qd_device.cuh"
+
+namespace qd {
+
+__global__ void k_theta_phase(double2 *__restrict__ psi, const double2 *__restrict__ tab, int64_t n_total,
+                              int64_t n_per_block, const int *status) {
+  if (status && *status) return;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_total; i += stride) {
+    const int64_t t = i % n_per_block;
+    psi[i] = cmul(psi[i], ldg2(tab + t));
+  }
+}
+
+void launch_theta_phase(cudaStream_t s, double2 *psi, const double2 *tab, int n_blocks, int64_t n_per_block,
+                        const int *status) {
+  const int64_t n = (int64_t)n_blocks * n_per_block;
+  k_theta_phase<<<grid_for(n, 256), 256, 0, s>>>(psi, tab, n, n_per_block, status);
+}
+
+__global__ void k_slab_phase(double2 *__restrict__ psi_j, const double2 *__restrict__ tab,
+                             const SlabDesc *__restrict__ slabs, int64_t npt, const int *status) {
+  if (status && *status) return;
+  const int sl = blockIdx.y;
+  const int l = slabs[sl].l;
+  double2 *p = psi_j + (int64_t)sl * npt;
+  const double2 *t = tab + (int64_t)l * npt;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npt; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = cmul(p[i], ldg2(t + i));
+}
+
+void launch_slab_phase(cudaStream_t s, double2 *psi_j, const double2 *tab, const SlabDesc *slabs, int n_slabs,
+                       int64_t npt, const int *status) {
+  if (n_slabs == 0) return;
+  dim3 grid((unsigned)std::min<int64_t>((npt + 255) / 256, 64), n_slabs);
+  k_slab_phase<<<grid, 256, 0, s>>>(psi_j, tab, slabs, npt, status);
+}
+
+// ------------------------------------------------------------------ tables
+__global__ void k_build_theta_table(const double *__restrict__ pot, const double *__restrict__ d1,
+                                    const double *__restrict__ d2, int n1, int n2, int64_t n, double dt,
+                                    double2 *__restrict__ tab) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % n1);
+    const int j = (int)((q / n1) % n2);
+    double s, c;
+    sincos(dt * pot[q], &s, &c);
+    double m = 1.0;
+    if (d1 && d2) m = d1[i] * d2[j];
+    tab[q] = make_double2(m * c, -m * s);
+  }
+}
+
+void launch_build_theta_table(cudaStream_t s, const Grid &g, const double *pot, const double *d1, const double *d2,
+                              double dt, double2 *tab) {
+  const int64_t n = g.npt * g.nth;
+  k_build_theta_table<<<grid_for(n, 256), 256, 0, s>>>(pot, d1, d2, g.n1, g.n2, n, dt, tab);
+}
+
+// exp(-i dt l(l+1) (1/(2 m1 R_i^2) + 1/(2 m2 r_j^2)))   (evolutionCUDAaux.cu:33-54, cudaMath.h:150-157)
+__global__ void k_build_rot_table(Grid g, double dt, double2 *__restrict__ tab) {
+  const int64_t n = g.npt * (g.l_max + 1);
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % g.n1);
+    const int j = (int)((q / g.n1) % g.n2);
+    const int l = (int)(q / g.npt);
+    const double R = g.left1 + i * g.dr1;
+    const double r = g.left2 + j * g.dr2;
+    const double I = 1.0 / (2 * g.m1 * R * R) + 1.0 / (2 * g.m2 * r * r);
+    double s, c;
+    sincos(dt * (double)l * (double)(l + 1) * I, &s, &c);
+    tab[q] = make_double2(c, -s);
+  }
+}
+
+void launch_build_rot_table(cudaStream_t s, const Grid &g, double dt, double2 *tab) {
+  k_build_rot_table<<<grid_for(g.npt * (g.l_max + 1), 256), 256, 0, s>>>(g, dt, tab);
+}
+
+__global__ void k_build_kin_table(const double *__restrict__ T1, const double *__restrict__ T2, int n1, int64_t n,
+                                  double dt, double2 *__restrict__ tab) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % n1);
+    const int j = (int)(q / n1);
+    double s, c;
+    sincos(dt * (T1[i] + T2[j]), &s, &c);
+    tab[q] = make_double2(c, -s);
+  }
+}
+
+void launch_build_kin_table(cudaStream_t s, const Grid &g, const double *T1, const double *T2, double dt,
+                            double2 *tab) {
+  k_build_kin_table<<<grid_for(g.npt, 256), 256, 0, s>>>(T1, T2, g.n1, g.npt, dt, tab);
+}
+
+// exp(-i (dt/2) V) on the flux stencil rows: [k][g][i]
+__global__ void k_build_half_v(Grid g, int n_grad, int n_ds, const double *__restrict__ pot, double dt,
+                               double2 *__restrict__ hv) {
+  const int h = (n_grad - 1) / 2;
+  const int64_t n = (int64_t)g.nth * n_grad * g.n1;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % g.n1);
+    const int gg = (int)((q / g.n1) % n_grad);
+    const int k = (int)(q / ((int64_t)g.n1 * n_grad));
+    const int j = n_ds - h + gg;
+    double s, c;
+    sincos(0.5 * dt * pot[((int64_t)k * g.n2 + j) * g.n1 + i], &s, &c);
+    hv[q] = make_double2(c, -s);
+  }
+}
+
+void launch_build_half_v(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
+                         double2 *half_v) {
+  const int64_t n = (int64_t)g.nth * f.n_grad * g.n1;
+  k_build_half_v<<<grid_for(n, 256), 256, 0, s>>>(g, f.n_grad, f.n_ds, pot, dt, half_v);
+}
+
+// ------------------------------------------------------------ energies
+// rotational energy partials: sum l(l+1) (I1_i + I2_j) |psi|^2 per (slab, tile)
+__global__ void k_rot_energy(Grid g, const double2 *__restrict__ psi_j, const SlabDesc *__restrict__ slabs,
+                             double *__restrict__ re_part, int tiles, const int *status) {
+  if (status && *status) return;
+  __shared__ double red[32];
+  const int sl = blockIdx.y;
+  const double ll = (double)slabs[sl].l * (slabs[sl].l + 1);
+  const double2 *p = psi_j + (int64_t)sl * g.npt;
+  double acc = 0.0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < g.npt; q += (int64_t)tiles * blockDim.x) {
+    const int i = (int)(q % g.n1), j = (int)(q / g.n1);
+    const double R = g.left1 + i * g.dr1, r = g.left2 + j * g.dr2;
+    const double I = 1.0 / (2 * g.m1 * R * R) + 1.0 / (2 * g.m2 * r * r);
+    const double2 v = p[q];
+    acc += ll * I * (v.x * v.x + v.y * v.y);
+  }
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) re_part[(int64_t)sl * tiles + blockIdx.x] = acc;
+}
+
+void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, const SlabDesc *slabs, int n_slabs,
+                       const double *, const double *, double *re_part, int tiles, const int *status) {
+  if (n_slabs == 0) return;
+  k_rot_energy<<<dim3(tiles, n_slabs), 256, 0, s>>>(g, psi_j, slabs, re_part, tiles, status);
+}
+
+// One CTA per problem: per block, sum the partial arrays in a fixed order,
+// scale, write energies[b][6] and the step record; then the norm guard of
+// print_energies (cudaOpenMP2.cu:425-445).  Coupling-energy partials are laid
+// out [group][ce_n][tiles]; a block collects them from every group (one per l)
+// of its problem that contains its Omega.
+__global__ void k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__restrict__ blocks,
+                                  const int *__restrict__ pblock0, const CoriolisGroup *__restrict__ groups,
+                                  const int *__restrict__ pgroup0, int ce_n, double *__restrict__ energies,
+                                  double *__restrict__ rec, const int *__restrict__ d_step, int rec_base,
+                                  int rec_cap, int n_blocks, double norm_tol, int *status, int *status_step) {
+  if (*status) return;
+  __shared__ double red[32];
+  const int pr = blockIdx.x;
+  const int b0 = pblock0[pr], b1 = pblock0[pr + 1];
+  const double dV = g.dr1 * g.dr2;
+  const int step = *d_step;
+  double total_module = 0.0;
+  for (int b = b0; b < b1; b++) {
+    const BlockDesc bd = blocks[b];
+    double e[6];
+    for (int q = 0; q < 6; q++) e[q] = energies[b * 6 + q];
+    if (ep.have_mod) {
+      double m = 0.0, pe = 0.0;
+      for (int t = threadIdx.x; t < ep.mod_pe_tiles; t += blockDim.x) {
+        m += ep.mod_pe[((int64_t)b * ep.mod_pe_tiles + t) * 2 + 0];
+        pe += ep.mod_pe[((int64_t)b * ep.mod_pe_tiles + t) * 2 + 1];
+      }
+      m = block_sum(m, red);
+      pe = block_sum(pe, red);
+      e[E_MODULE] = m * dV;
+      e[E_POTENTIAL] = pe * dV;
+    }
+    if (ep.have_ke) {
+      double k = 0.0;
+      const int64_t n = (int64_t)bd.nl * ep.ke_tiles;
+      for (int64_t t = threadIdx.x; t < n; t += blockDim.x) k += ep.ke[(int64_t)bd.slab0 * ep.ke_tiles + t];
+      k = block_sum(k, red);
+      e[E_KINETIC] = k * dV / ((double)g.n1 * g.n2);
+    }
+    if (ep.have_re) {
+      double r = 0.0;
+      const int64_t n = (int64_t)bd.nl * ep.re_tiles;
+      for (int64_t t = threadIdx.x; t < n; t += blockDim.x) r += ep.re[(int64_t)bd.slab0 * ep.re_tiles + t];
+      r = block_sum(r, red);
+      e[E_ROTATIONAL] = r * dV;
+    }
+    if (ep.have_ce) {
+      double c = 0.0;
+      if (groups) {
+        for (int gi = pgroup0[pr]; gi < pgroup0[pr + 1]; gi++) {
+          const CoriolisGroup gr = groups[gi];
+          const int o = bd.omega - gr.omega_lo;
+          if (o < 0 || o >= gr.n) continue;
+          for (int t = threadIdx.x; t < ep.ce_tiles; t += blockDim.x)
+            c += ep.ce[((int64_t)gi * ce_n + o) * ep.ce_tiles + t];
+        }
+      }
+      c = block_sum(c, red);
+      e[E_CORIOLIS] = c * dV;
+    }
+    e[E_TOTAL] = e[E_POTENTIAL] + e[E_KINETIC] + e[E_ROTATIONAL] + e[E_CORIOLIS];
+    total_module += e[E_MODULE];
+    if (threadIdx.x == 0) {
+      for (int q = 0; q < 6; q++) energies[b * 6 + q] = e[q];
+      const int slot = step - rec_base;
+      if (rec && slot >= 0 && slot < rec_cap)
+        for (int q = 0; q < 6; q++) rec[((int64_t)slot * n_blocks + b) * 6 + q] = e[q];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && ep.have_mod && total_module > 1.0 + norm_tol) {
+    if (atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
+  }
+}
+
+void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &ep, const BlockDesc *blocks,
+                             const int *pblock0, int n_problems, const CoriolisGroup *groups, const int *pgroup0,
+                             int ce_n, double *energies, double *rec, const int *d_step, int rec_base, int rec_cap,
+                             double norm_tol, int *status, int *status_step, int n_blocks) {
+  k_energy_finalize<<<n_problems, 256, 0, st>>>(g, ep, blocks, pblock0, groups, pgroup0, ce_n, energies, rec, d_step,
+                                               rec_base, rec_cap, n_blocks, norm_tol, status, status_step);
+}
+
+}  // namespace qd

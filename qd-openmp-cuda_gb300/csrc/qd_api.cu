@@ -1,0 +1,1074 @@
+// C ABI and host engine of the GB300 split-operator propagator.
+//
+// Reference entry: mexFunction (cudaOpenMPEvolution.C:15-79) -> CudaOpenMPQMMD
+// (cudaOpenMP2.cu:23-127) -> test_multiple_cards (cudaOpenMP2.cu:328-390).
+// The multi-GPU orchestration (OpenMP threads per device, P2P Coriolis
+// exchange) is replaced by one session on one device holding every Omega block
+// of every problem resident in HBM; each stage is one launch over all blocks,
+// and steps are replayed from CUDA graphs.
+#include "qd_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace qd {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+// ------------------------------------------------------- Coriolis matrices
+// Tridiagonal Omega matrix of setup_coriolis_matrix (CoriolisMatrix.C:63-99):
+// diagonal J(J+1) - 2 Omega^2, off-diagonal -lambda(J,Omega) lambda(l,Omega)
+// sqrt(1 + delta_{Omega,0}), lambda(J,Omega) = sqrt(J(J+1) - Omega(Omega+1))
+// for J >= Omega (CoriolisMatrix.C:23-33).
+static double lam(int J, int omega) {
+  return J >= omega ? std::sqrt(J * (J + 1.0) - omega * (omega + 1.0)) : 0.0;
+}
+
+// Cyclic Jacobi diagonalisation of a small symmetric matrix (row-major a[n*n]).
+// Returns eigenvalues ascending in e and eigenvectors as columns of v
+// (v[p*n + a] = component p of vector a), the layout dstev writes.
+static void jacobi_eigen(int n, std::vector<double> a, std::vector<double> &e, std::vector<double> &v) {
+  v.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) v[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0, diag = 0.0;
+    for (int p = 0; p < n; p++)
+      for (int q = 0; q < n; q++) (p == q ? diag : off) += a[(size_t)p * n + q] * a[(size_t)p * n + q];
+    if (off <= 1e-32 * std::max(diag, 1e-300)) break;
+    for (int p = 0; p < n - 1; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double apq = a[(size_t)p * n + q];
+        if (std::fabs(apq) < 1e-300) continue;
+        const double app = a[(size_t)p * n + p], aqq = a[(size_t)q * n + q];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; k++) {   // A <- A J (columns p, q)
+          const double akp = a[(size_t)k * n + p], akq = a[(size_t)k * n + q];
+          a[(size_t)k * n + p] = c * akp - s * akq;
+          a[(size_t)k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; k++) {   // A <- J^T A (rows p, q)
+          const double apk = a[(size_t)p * n + k], aqk = a[(size_t)q * n + k];
+          a[(size_t)p * n + k] = c * apk - s * aqk;
+          a[(size_t)q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; k++) {   // V <- V J
+          const double vkp = v[(size_t)k * n + p], vkq = v[(size_t)k * n + q];
+          v[(size_t)k * n + p] = c * vkp - s * vkq;
+          v[(size_t)k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  e.resize(n);
+  for (int i = 0; i < n; i++) e[i] = a[(size_t)i * n + i];
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; i++) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return e[x] < e[y]; });
+  std::vector<double> e2(n), v2((size_t)n * n);
+  for (int k = 0; k < n; k++) {
+    e2[k] = e[idx[k]];
+    for (int p = 0; p < n; p++) v2[(size_t)p * n + k] = v[(size_t)p * n + idx[k]];
+  }
+  e.swap(e2);
+  v.swap(v2);
+}
+
+// ------------------------------------------------------------- validation
+struct ProblemHost {
+  qd_fh2data *d;
+  int J, parity, l_max, n_omegas, omega_min, omega_cap;
+  bool coupled;
+  std::vector<int> omegas;
+};
+
+static void validate_problem(qd_fh2data *d, ProblemHost &ph) {
+  QD_REQUIRE(d != nullptr, "FH2Data != NULL");
+  QD_REQUIRE(d->r1.n > 0 && d->r2.n > 0 && d->theta.n > 0, "grid sizes > 0");
+  QD_REQUIRE(d->r1.dr > 0 && d->r2.dr > 0, "r1.dr > 0 && r2.dr > 0");
+  QD_REQUIRE(d->r1.mass > 0 && d->r2.mass > 0, "masses > 0");
+  QD_REQUIRE(d->r1.left > 0 && d->r2.left > 0, "radial grids start above 0 (1/R^2 terms)");
+  QD_REQUIRE(d->theta.x && d->theta.w, "theta.x && theta.w");
+  QD_REQUIRE(d->pot, "pot");
+  QD_REQUIRE(d->time.total_steps >= 0, "time.total_steps >= 0");
+  QD_REQUIRE(std::isfinite(d->time.time_step), "time.time_step finite");
+  QD_REQUIRE(d->time.steps >= 0, "time.steps >= 0");
+  if (d->r1.n % 2 || d->r2.n % 2)
+    throw Error{QD_ERR_UNSUPPORTED, "r1.n and r2.n must be even (FFT kinetic table, cudaMath.h:117-130)"};
+  const qd_omega_states &om = d->OmegaStates;
+  QD_REQUIRE(om.J >= 0, "OmegaStates.J >= 0");
+  if (om.J == 0) QD_REQUIRE(om.parity == 0, "p == 0 when J == 0 (CoriolisMatrix.C:52)");
+  QD_REQUIRE(om.l_max >= 0, "l_max >= 0");
+  QD_REQUIRE(om.n_omegas >= 1 && om.omegas, "omegas");
+  QD_REQUIRE(om.n_omegas_max >= om.n_omegas, "n_omegas_max >= omegas.size() (matlabStructures.C:128)");
+  QD_REQUIRE(d->theta.n >= om.l_max + 1, "theta.n >= l_max + 1 (Gauss-Legendre exactness)");
+  QD_REQUIRE(om.associated_legendres && om.wave_packets, "associated_legendres && wave_packets");
+  const int omega_min = om.J == 0 ? 0 : ((om.J + om.parity) % 2 == 0 ? 0 : 1);
+  QD_REQUIRE(om.omegas[0] == omega_min, "omegas[0] == (J+p)%2 (OmegaList.m)");
+  for (int i = 1; i < om.n_omegas; i++) QD_REQUIRE(om.omegas[i] == om.omegas[i - 1] + 1, "consecutive omegas");
+  const int omega_last = om.omegas[om.n_omegas - 1];
+  QD_REQUIRE(omega_last <= std::min(om.J, om.l_max), "omega <= min(J, l_max)");
+  QD_REQUIRE(om.n_cols >= om.l_max - omega_min + 1, "associated_legendres columns >= l_max - omega_min + 1");
+  const qd_crp &c = d->CRP;
+  if (c.calculate_CRP) {
+    QD_REQUIRE(c.energies && c.eta_sq && c.CRP, "CRP.energies && CRP.eta_sq && CRP.CRP");
+    QD_REQUIRE(c.n_energies > 0, "CRP.n_energies > 0");
+    QD_REQUIRE(c.n_gradient_points >= 3 && c.n_gradient_points % 2 == 1, "CRP.n_gradient_points odd >= 3");
+    const int h = (c.n_gradient_points - 1) / 2;
+    QD_REQUIRE(c.n_dividing_surface - h >= 0 && c.n_dividing_surface + h < d->r2.n,
+               "flux stencil inside the r2 grid");
+    for (int e = 0; e < c.n_energies; e++) QD_REQUIRE(c.eta_sq[e] > 0, "CRP.eta_sq > 0");
+  }
+  if (d->options.wave_to_matlab)
+    QD_REQUIRE(d->options.steps_to_copy_psi_from_device_to_host > 0, "steps_to_copy_psi_from_device_to_host > 0");
+  QD_REQUIRE(d->options.precision == QD_PRECISION_FP64 || d->options.precision == QD_PRECISION_MIXED,
+             "options.precision in {0, 1}");
+  ph.d = d;
+  ph.J = om.J;
+  ph.parity = om.parity;
+  ph.l_max = om.l_max;
+  ph.n_omegas = om.n_omegas;
+  ph.omega_min = omega_min;
+  ph.omegas.assign(om.omegas, om.omegas + om.n_omegas);
+  ph.omega_cap = omega_last;
+  ph.coupled = om.J > 0;
+}
+
+static void validate_batch(qd_fh2data *const *pr, int n, std::vector<ProblemHost> &out) {
+  QD_REQUIRE(pr != nullptr && n >= 1, "n_problems >= 1");
+  out.resize(n);
+  for (int i = 0; i < n; i++) validate_problem(pr[i], out[i]);
+  const qd_fh2data *a = pr[0];
+  for (int i = 1; i < n; i++) {
+    const qd_fh2data *b = pr[i];
+    QD_REQUIRE(a->r1.n == b->r1.n && a->r2.n == b->r2.n && a->theta.n == b->theta.n, "batch: same grids");
+    QD_REQUIRE(a->r1.left == b->r1.left && a->r1.dr == b->r1.dr && a->r1.mass == b->r1.mass, "batch: same r1");
+    QD_REQUIRE(a->r2.left == b->r2.left && a->r2.dr == b->r2.dr && a->r2.mass == b->r2.mass, "batch: same r2");
+    QD_REQUIRE(a->OmegaStates.l_max == b->OmegaStates.l_max, "batch: same l_max");
+    QD_REQUIRE(a->time.time_step == b->time.time_step && a->time.steps == b->time.steps &&
+                   a->time.total_steps == b->time.total_steps,
+               "batch: same time");
+    QD_REQUIRE(a->options.precision == b->options.precision, "batch: same precision");
+    QD_REQUIRE(a->CRP.calculate_CRP == b->CRP.calculate_CRP, "batch: same CRP switch");
+    const size_t npot = (size_t)a->r1.n * a->r2.n * a->theta.n;
+    QD_REQUIRE(a->pot == b->pot || std::memcmp(a->pot, b->pot, npot * sizeof(double)) == 0, "batch: same pot");
+    QD_REQUIRE((a->dump1.dump == nullptr) == (b->dump1.dump == nullptr) &&
+                   (a->dump2.dump == nullptr) == (b->dump2.dump == nullptr),
+               "batch: same masks");
+    if (a->CRP.calculate_CRP) {
+      QD_REQUIRE(a->CRP.n_energies == b->CRP.n_energies && a->CRP.n_dividing_surface == b->CRP.n_dividing_surface &&
+                     a->CRP.n_gradient_points == b->CRP.n_gradient_points,
+                 "batch: same CRP shape");
+      QD_REQUIRE(std::memcmp(a->CRP.energies, b->CRP.energies, a->CRP.n_energies * sizeof(double)) == 0,
+                 "batch: same CRP energies");
+    }
+  }
+}
+
+// first-derivative weights of the centred n-point stencil (Fornberg 1988)
+static std::vector<double> fd_weights(int n) {
+  const int h = (n - 1) / 2;
+  std::vector<double> x(n);
+  for (int i = 0; i < n; i++) x[i] = i - h;
+  std::vector<std::vector<double>> c(n, std::vector<double>(2, 0.0));
+  double c1 = 1.0, c4 = x[0];
+  c[0][0] = 1.0;
+  for (int i = 1; i < n; i++) {
+    const int mn = std::min(i, 1);
+    double c2 = 1.0;
+    const double c5 = c4;
+    c4 = x[i];
+    for (int j = 0; j < i; j++) {
+      const double c3 = x[i] - x[j];
+      c2 *= c3;
+      if (j == i - 1) {
+        for (int k = mn; k > 0; k--) c[i][k] = c1 * (k * c[i - 1][k - 1] - c5 * c[i - 1][k]) / c2;
+        c[i][0] = -c1 * c5 * c[i - 1][0] / c2;
+      }
+      for (int k = mn; k > 0; k--) c[j][k] = (c4 * c[j][k] - k * c[j][k - 1]) / c3;
+      c[j][0] = c4 * c[j][0] / c3;
+    }
+    c1 = c2;
+  }
+  std::vector<double> w(n);
+  for (int i = 0; i < n; i++) w[i] = c[i][1];
+  return w;
+}
+
+template <typename T> static T *dalloc(size_t n) {
+  T *p = nullptr;
+  if (n == 0) return nullptr;
+  QD_CUDA(cudaMalloc(&p, n * sizeof(T)));
+  return p;
+}
+template <typename T> static T *dupload(const T *h, size_t n, cudaStream_t s) {
+  T *p = dalloc<T>(n);
+  if (n) QD_CUDA(cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+  return p;
+}
+
+__global__ void k_step_end(int *step, const int *status, int *flux_count, double *flux_t0, double dt,
+                           int flux_on);
+__global__ void k_flux_begin(const int *step, int *flux_count, double *flux_t0, double dt, int *slot_out);
+
+}  // namespace qd
+
+using namespace qd;
+
+// ------------------------------------------------------------------ session
+struct qd_session {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Grid g{};
+  int precision = 0;
+  double dt = 0.0;
+  double norm_tol = 1e-10;
+  int n_problems = 0, n_blocks = 0, n_slabs = 0, max_nl = 0;
+  bool any_coupled = false, has_mask = false;
+  std::vector<ProblemHost> probs;
+  std::vector<BlockDesc> h_blocks;
+  std::vector<SlabDesc> h_slabs;
+  std::vector<int> h_pblock0;
+  BlockDesc *d_blocks = nullptr;
+  SlabDesc *d_slabs = nullptr;
+  int *d_pblock0 = nullptr;
+  // coupled / uncoupled slab lists (epilogue tables differ)
+  double2 *psi_th = nullptr, *psi_j = nullptr;
+  double *pot = nullptr, *w = nullptr, *T1 = nullptr, *T2 = nullptr, *I1 = nullptr, *I2 = nullptr;
+  double *d1 = nullptr, *d2 = nullptr;
+  double2 *tab_v = nullptr, *tab_v0 = nullptr, *tab_rot2 = nullptr, *tab_rot4 = nullptr, *tab_kin = nullptr;
+  double *Bf = nullptr, *Bb = nullptr;
+  // Coriolis
+  std::vector<CoriolisGroup> h_groups;
+  CoriolisGroup *d_groups = nullptr;
+  int n_groups = 0, max_group_n = 1;
+  double *cor_V = nullptr, *cor_e = nullptr, *cor_H = nullptr;
+  double2 *cor_ph = nullptr;
+  std::vector<int> h_pgroup0;
+  int *d_pgroup0 = nullptr;
+  // energies
+  double *part_modpe = nullptr, *part_ke = nullptr, *part_re = nullptr, *part_ce = nullptr;
+  int t_modpe = 0, t_ke = 0, t_re = 0, t_ce = 0;
+  double *energies = nullptr;     // [n_blocks][6]
+  double *rec = nullptr;          // [rec_cap][n_blocks][6]
+  int rec_cap = 0, rec_base = 0;
+  int *status = nullptr, *status_step = nullptr, *d_step = nullptr;
+  // flux
+  FluxConfig flux{};
+  double2 *flux_buf = nullptr, *flux_acc = nullptr, *flux_phase = nullptr, *half_v = nullptr;
+  double *fd = nullptr, *flux_E = nullptr, *flux_eta = nullptr, *crp = nullptr, *flux_t0 = nullptr;
+  int *flux_count = nullptr, *flux_slot = nullptr;
+  int flux_pending = 0;
+  FFTPlan fft{};
+  int steps = 0;   // host mirror of time.steps
+  int launches_per_step = 0;
+  cudaGraphExec_t graph_chunk = nullptr;
+  int graph_steps = 0;
+
+  ~qd_session();
+};
+
+namespace qd {
+
+__global__ void k_step_end(int *step, const int *status, int *, double *, double, int) {
+  if (*status) return;
+  *step += 1;
+}
+
+// sets the flux slot for this step; records t0 when the chunk starts
+__global__ void k_flux_begin(const int *step, int *flux_count, double *flux_t0, double dt, int *slot_out) {
+  const int c = *flux_count;
+  if (c == 0) *flux_t0 = (*step + 1) * dt;
+  *slot_out = c;
+  *flux_count = c + 1;
+}
+
+// flux extract with a device-side slot
+__global__ void k_flux_extract_dev(Grid g, int n_grad, int n_ds, const double2 *__restrict__ psi_th,
+                                   const double2 *__restrict__ hv, const double *__restrict__ fd,
+                                   double2 *__restrict__ buf, int n_blocks, const int *slot_p, const int *status) {
+  if (status && *status) return;
+  const int slot = *slot_p;
+  const int b = blockIdx.y;
+  const int h = (n_grad - 1) / 2;
+  const int64_t ns = (int64_t)g.nth * g.n1;
+  double2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
+  const double2 *p = psi_th + (int64_t)b * g.nth * g.npt;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % g.n1), k = (int)(q / g.n1);
+    double2 A = make_double2(0.0, 0.0), D = make_double2(0.0, 0.0);
+    for (int gg = 0; gg < n_grad; gg++) {
+      const int j = n_ds - h + gg;
+      const double2 a = p[((int64_t)k * g.n2 + j) * g.n1 + i];
+      const double2 m = hv[((int64_t)k * n_grad + gg) * g.n1 + i];
+      const double2 v = make_double2(a.x * m.x - a.y * m.y, a.x * m.y + a.y * m.x);
+      const double c = fd[gg];
+      D.x = fma(c, v.x, D.x);
+      D.y = fma(c, v.y, D.y);
+      if (gg == h) A = v;
+    }
+    out[q] = A;
+    out[ns + q] = D;
+  }
+}
+
+// phase[n][E] = dt exp(i E (t0 + n dt)) for n < count (device count and t0)
+__global__ void k_flux_phase_dev(const double *__restrict__ E, int nE, int cap, const int *count_p,
+                                 const double *t0_p, double dt, double2 *__restrict__ phase) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nE * cap) return;
+  const int n = q / nE, e = q % nE;
+  if (n >= *count_p) return;
+  double s, c;
+  sincos(E[e] * (*t0_p + n * dt), &s, &c);
+  phase[q] = make_double2(dt * c, dt * s);
+}
+
+__global__ void k_flux_reset(int *count) { *count = 0; }
+
+}  // namespace qd
+
+qd_session::~qd_session() {
+  if (graph_chunk) cudaGraphExecDestroy(graph_chunk);
+  void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
+                  tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, d_pgroup0,
+                  part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
+                  flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  fft_plan_free(fft);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+namespace qd {
+
+// flux DFT reading count/t0 from the device (graph friendly)
+__global__ void k_flux_dft_dev(int64_t ns2, int nE, int n_blocks, const int *count_p,
+                               const double2 *__restrict__ buf, const double2 *__restrict__ phase,
+                               double2 *__restrict__ acc, const int *status);
+
+static void enqueue_flux_dft(qd_session *s) {
+  const int nE = s->flux.n_energies;
+  const int cap = s->flux.chunk;
+  k_flux_phase_dev<<<(nE * cap + 255) / 256, 256, 0, s->stream>>>(s->flux_E, nE, cap, s->flux_count, s->flux_t0,
+                                                                   s->dt, s->flux_phase);
+  const int64_t ns2 = 2LL * s->g.nth * s->g.n1;
+  dim3 grid((unsigned)((ns2 + 127) / 128), (unsigned)((nE + 7) / 8), (unsigned)s->n_blocks);
+  k_flux_dft_dev<<<grid, 128, 0, s->stream>>>(ns2, nE, s->n_blocks, s->flux_count, s->flux_buf, s->flux_phase,
+                                               s->flux_acc, s->status);
+  k_flux_reset<<<1, 1, 0, s->stream>>>(s->flux_count);
+}
+
+static EnergyParts energy_parts(qd_session *s, bool mod, bool ke, bool re, bool ce) {
+  EnergyParts ep{};
+  ep.mod_pe = s->part_modpe;
+  ep.mod_pe_tiles = s->t_modpe;
+  ep.ke = s->part_ke;
+  ep.ke_tiles = s->t_ke;
+  ep.re = s->part_re;
+  ep.re_tiles = s->t_re;
+  ep.ce = s->part_ce;
+  ep.ce_tiles = s->t_ce;
+  ep.have_mod = mod;
+  ep.have_ke = ke;
+  ep.have_re = re;
+  ep.have_ce = ce;
+  return ep;
+}
+
+// One full time step, sequence of test_multiple_cards (cudaOpenMP2.cu:338-386).
+static void enqueue_step(qd_session *s, bool first) {
+  cudaStream_t st = s->stream;
+  const Grid &g = s->g;
+  const double2 *tabA = first ? s->tab_v0 : s->tab_v;
+  // dump_wavepacket + evolution_with_potential(-dt/2 at step 0) + potential(dt) -> prologue,
+  // forward_legendre_transform, rotational(dt/4) [x2 fused when uncoupled] -> epilogue
+  launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, tabA,
+                          s->any_coupled ? s->tab_rot4 : s->tab_rot2, s->status);
+  if (s->any_coupled) {
+    // evolution_with_coriolis(dt/2) + rotational(dt/4)
+    launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
+                    s->cor_H, nullptr, s->t_ce, s->tab_rot4, s->status);
+  }
+  // forward FFT, kinetic(dt), kinetic energy, backward FFT + scale, rotational(dt/4)
+  launch_fft_kinetic(st, g, s->fft, s->precision, s->psi_j, s->d_slabs, s->n_slabs, s->tab_kin, s->T1, s->T2,
+                     s->part_ke, s->any_coupled ? s->tab_rot4 : s->tab_rot2, s->I1, s->I2,
+                     s->any_coupled ? nullptr : s->part_re, s->status);
+  if (s->any_coupled) {
+    // evolution_with_coriolis(dt/2, energy) + rotational(dt/4), then the rotational energy
+    launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
+                    s->cor_H, s->part_ce, s->t_ce, s->tab_rot4, s->status);
+    launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->I1, s->I2, s->part_re, s->t_re, s->status);
+  }
+  // backward_legendre_transform + potential energy + module
+  launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
+                          s->part_modpe, s->t_modpe, s->status);
+  EnergyParts ep = energy_parts(s, true, true, true, s->any_coupled);
+  launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
+                          s->max_group_n, s->energies, s->rec, s->d_step, s->rec_base, s->rec_cap, s->norm_tol,
+                          s->status, s->status_step, s->n_blocks);
+  if (s->flux.enabled) {
+    k_flux_begin<<<1, 1, 0, st>>>(s->d_step, s->flux_count, s->flux_t0, s->dt, s->flux_slot);
+    const int64_t ns = (int64_t)g.nth * g.n1;
+    dim3 grid((unsigned)std::min<int64_t>((ns + 255) / 256, 64), (unsigned)s->n_blocks);
+    k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
+                                             s->flux_buf, s->n_blocks, s->flux_slot, s->status);
+  }
+  k_step_end<<<1, 1, 0, st>>>(s->d_step, s->status, nullptr, nullptr, 0.0, 0);
+}
+
+static int count_launches_per_step(qd_session *s) {
+  int n = 1 + 3 + 1 + 1 + 1;   // fwd, fft x3, bwd, finalize, step_end
+  if (s->any_coupled) n += 3;  // coriolis x2, rot energy
+  if (s->flux.enabled) n += 2;
+  return n;
+}
+
+}  // namespace qd
+
+// ------------------------------------------------------------ create
+static void session_build(qd_session *s, qd_fh2data *const *problems, int n_problems) {
+  validate_batch(problems, n_problems, s->probs);
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    throw Error{QD_ERR_NO_DEVICE, "no CUDA device"};
+  QD_CUDA(cudaGetDevice(&s->device));
+  QD_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  cudaStream_t st = s->stream;
+  const qd_fh2data *d0 = problems[0];
+  Grid &g = s->g;
+  g.n1 = d0->r1.n;
+  g.n2 = d0->r2.n;
+  g.nth = d0->theta.n;
+  g.l_max = d0->OmegaStates.l_max;
+  g.npt = (int64_t)g.n1 * g.n2;
+  g.dr1 = d0->r1.dr;
+  g.dr2 = d0->r2.dr;
+  g.m1 = d0->r1.mass;
+  g.m2 = d0->r2.mass;
+  g.left1 = d0->r1.left;
+  g.left2 = d0->r2.left;
+  s->precision = d0->options.precision;
+  s->dt = d0->time.time_step;
+  s->steps = d0->time.steps;
+  s->norm_tol = s->precision == QD_PRECISION_MIXED ? 1e-4 : 1e-10;
+  s->n_problems = n_problems;
+  fft_plan_init(s->fft, g.n1, g.n2);
+
+  // blocks and slabs
+  int slab = 0;
+  int64_t bmat = 0;
+  s->h_pblock0.push_back(0);
+  for (int p = 0; p < n_problems; p++) {
+    ProblemHost &ph = s->probs[p];
+    if (ph.coupled) s->any_coupled = true;
+    for (int o : ph.omegas) {
+      BlockDesc bd{};
+      bd.problem = p;
+      bd.omega = o;
+      bd.nl = g.l_max - o + 1;
+      bd.slab0 = slab;
+      bd.bmat0 = bmat;
+      for (int l = o; l <= g.l_max; l++) s->h_slabs.push_back(SlabDesc{(int32_t)s->h_blocks.size(), l});
+      slab += bd.nl;
+      bmat += (int64_t)bd.nl * g.nth;
+      s->max_nl = std::max(s->max_nl, bd.nl);
+      s->h_blocks.push_back(bd);
+    }
+    s->h_pblock0.push_back((int)s->h_blocks.size());
+  }
+  s->n_blocks = (int)s->h_blocks.size();
+  s->n_slabs = slab;
+  s->d_blocks = dupload(s->h_blocks.data(), s->h_blocks.size(), st);
+  s->d_slabs = dupload(s->h_slabs.data(), s->h_slabs.size(), st);
+  s->d_pblock0 = dupload(s->h_pblock0.data(), s->h_pblock0.size(), st);
+
+  // wave packets
+  const int64_t nth_pt = g.npt * g.nth;
+  s->psi_th = dalloc<double2>((size_t)s->n_blocks * nth_pt);
+  s->psi_j = dalloc<double2>((size_t)s->n_slabs * g.npt);
+  for (int p = 0; p < n_problems; p++)
+    QD_CUDA(cudaMemcpyAsync(s->psi_th + (int64_t)s->h_pblock0[p] * nth_pt, problems[p]->OmegaStates.wave_packets,
+                            (size_t)s->probs[p].n_omegas * nth_pt * sizeof(double2), cudaMemcpyHostToDevice, st));
+
+  // grid tables
+  std::vector<double> T1(g.n1), T2(g.n2);
+  auto kin = [](int n, double dr, double mass, std::vector<double> &T) {
+    const double two_pi_xl = 2 * M_PI / (n * dr);   // cudaMath.h:117-130
+    for (int i = 0; i < n; i++) {
+      const double k = two_pi_xl * (i <= n / 2 ? i : i - n);
+      T[i] = k * k / (mass + mass);
+    }
+  };
+  kin(g.n1, g.dr1, g.m1, T1);
+  kin(g.n2, g.dr2, g.m2, T2);
+  s->T1 = dupload(T1.data(), T1.size(), st);
+  s->T2 = dupload(T2.data(), T2.size(), st);
+  s->pot = dupload(d0->pot, (size_t)nth_pt, st);
+  s->w = dupload(d0->theta.w, (size_t)g.nth, st);
+  s->has_mask = d0->dump1.dump && d0->dump2.dump;   // MatlabData::dump_wavepacket (matlabData.h:27)
+  if (s->has_mask) {
+    s->d1 = dupload(d0->dump1.dump, (size_t)g.n1, st);
+    s->d2 = dupload(d0->dump2.dump, (size_t)g.n2, st);
+  }
+  s->tab_v = dalloc<double2>((size_t)nth_pt);
+  s->tab_v0 = dalloc<double2>((size_t)nth_pt);
+  launch_build_theta_table(st, g, s->pot, s->d1, s->d2, s->dt, s->tab_v);
+  launch_build_theta_table(st, g, s->pot, s->d1, s->d2, 0.5 * s->dt, s->tab_v0);
+  const int64_t nrot = g.npt * (g.l_max + 1);
+  bool any_uncoupled = false;
+  for (auto &ph : s->probs) any_uncoupled |= !ph.coupled;
+  if (s->any_coupled) {
+    s->tab_rot4 = dalloc<double2>((size_t)nrot);
+    launch_build_rot_table(st, g, 0.25 * s->dt, s->tab_rot4);
+  } else {
+    s->tab_rot2 = dalloc<double2>((size_t)nrot);
+    launch_build_rot_table(st, g, 0.5 * s->dt, s->tab_rot2);
+  }
+  s->tab_kin = dalloc<double2>((size_t)g.npt);
+  launch_build_kin_table(st, g, s->T1, s->T2, s->dt, s->tab_kin);
+
+  // Legendre matrices: forward B = w_k P (k, n) as [k][n]; backward P as [n][k]
+  std::vector<double> Bf((size_t)bmat), Bb((size_t)bmat);
+  for (int b = 0; b < s->n_blocks; b++) {
+    const BlockDesc &bd = s->h_blocks[b];
+    const ProblemHost &ph = s->probs[bd.problem];
+    const qd_omega_states &om = ph.d->OmegaStates;
+    const int bi = b - s->h_pblock0[bd.problem];
+    for (int n = 0; n < bd.nl; n++)
+      for (int k = 0; k < g.nth; k++) {
+        const double P = om.associated_legendres[((int64_t)bi * om.n_cols + n) * g.nth + k];
+        Bf[bd.bmat0 + (int64_t)k * bd.nl + n] = ph.d->theta.w[k] * P;
+        Bb[bd.bmat0 + (int64_t)n * g.nth + k] = P;
+      }
+  }
+  s->Bf = dupload(Bf.data(), Bf.size(), st);
+  s->Bb = dupload(Bb.data(), Bb.size(), st);
+
+  // Coriolis groups (cudaOpenMP2.cu:158-209): one per (problem, l >= omega_min)
+  if (s->any_coupled) {
+    std::vector<double> V, E, H;
+    s->h_pgroup0.push_back(0);
+    int64_t ph0 = 0;
+    for (int p = 0; p < n_problems; p++) {
+      const ProblemHost &ph = s->probs[p];
+      {
+        // J = 0 problems of a coupled batch get 1x1 zero matrices: identity
+        // coupling, but their second rotational quarter step still applies
+        for (int l = ph.omega_min; l <= g.l_max; l++) {
+          const int omax = std::min(std::min(ph.J, l), ph.omega_cap);
+          const int n = omax - ph.omega_min + 1;
+          if (n < 1) continue;
+          std::vector<double> a((size_t)n * n, 0.0);
+          for (int k = 0; k < n; k++) {
+            const int om = k + ph.omega_min;
+            a[(size_t)k * n + k] = ph.J * (ph.J + 1.0) - 2.0 * om * om;
+            if (k + 1 < n) {
+              const double off = -lam(ph.J, om) * lam(l, om) * std::sqrt(1.0 + (om == 0 ? 1.0 : 0.0));
+              a[(size_t)k * n + k + 1] = off;
+              a[(size_t)(k + 1) * n + k] = off;
+            }
+          }
+          std::vector<double> e, v;
+          jacobi_eigen(n, a, e, v);
+          CoriolisGroup gr{};
+          gr.l = l;
+          gr.n = n;
+          gr.block_lo = s->h_pblock0[p];
+          gr.omega_lo = ph.omega_min;
+          gr.v0 = (int64_t)V.size();
+          gr.e0 = (int64_t)E.size();
+          gr.h0 = (int64_t)H.size();
+          gr.ph0 = ph0;
+          ph0 += (int64_t)n * g.n1;
+          V.insert(V.end(), v.begin(), v.end());
+          E.insert(E.end(), e.begin(), e.end());
+          H.insert(H.end(), a.begin(), a.end());
+          s->h_groups.push_back(gr);
+          s->max_group_n = std::max(s->max_group_n, n);
+        }
+      }
+      s->h_pgroup0.push_back((int)s->h_groups.size());
+    }
+    s->n_groups = (int)s->h_groups.size();
+    s->d_groups = dupload(s->h_groups.data(), s->h_groups.size(), st);
+    s->d_pgroup0 = dupload(s->h_pgroup0.data(), s->h_pgroup0.size(), st);
+    s->cor_V = dupload(V.data(), V.size(), st);
+    s->cor_e = dupload(E.data(), E.size(), st);
+    s->cor_H = dupload(H.data(), H.size(), st);
+    s->cor_ph = dalloc<double2>((size_t)ph0);
+    launch_build_coriolis_phase(st, g, s->d_groups, s->n_groups, s->max_group_n, s->cor_e, 0.5 * s->dt, s->cor_ph);
+  }
+
+  // energies and partials
+  s->t_modpe = legendre_bwd_part_tiles(g);
+  s->t_ke = fft_col_tiles(s->fft);
+  s->t_re = s->any_coupled ? 16 : fft_row_tiles(s->fft);
+  s->t_ce = coriolis_tiles(g);
+  s->part_modpe = dalloc<double>((size_t)s->n_blocks * s->t_modpe * 2);
+  s->part_ke = dalloc<double>((size_t)s->n_slabs * s->t_ke);
+  s->part_re = dalloc<double>((size_t)s->n_slabs * s->t_re);
+  if (s->any_coupled) s->part_ce = dalloc<double>((size_t)std::max(1, s->n_groups) * s->max_group_n * s->t_ce);
+  s->energies = dalloc<double>((size_t)s->n_blocks * 6);
+  QD_CUDA(cudaMemsetAsync(s->energies, 0, (size_t)s->n_blocks * 6 * sizeof(double), st));
+  s->status = dalloc<int>(1);
+  s->status_step = dalloc<int>(1);
+  s->d_step = dalloc<int>(1);
+  QD_CUDA(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+  QD_CUDA(cudaMemsetAsync(s->status_step, 0, sizeof(int), st));
+  QD_CUDA(cudaMemcpyAsync(s->d_step, &s->steps, sizeof(int), cudaMemcpyHostToDevice, st));
+
+  // flux
+  const qd_crp &c = d0->CRP;
+  s->flux.enabled = c.calculate_CRP != 0;
+  if (s->flux.enabled) {
+    s->flux.n_energies = c.n_energies;
+    s->flux.n_grad = c.n_gradient_points;
+    s->flux.n_ds = c.n_dividing_surface;
+    s->flux.chunk = 32;
+    const int64_t ns = (int64_t)g.nth * g.n1;
+    s->flux_buf = dalloc<double2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
+    s->flux_acc = dalloc<double2>((size_t)s->n_blocks * 2 * c.n_energies * ns);
+    s->flux_phase = dalloc<double2>((size_t)s->flux.chunk * c.n_energies);
+    s->half_v = dalloc<double2>((size_t)g.nth * c.n_gradient_points * g.n1);
+    launch_build_half_v(st, g, s->flux, s->pot, s->dt, s->half_v);
+    std::vector<double> fdw = fd_weights(c.n_gradient_points);
+    for (double &x : fdw) x /= g.dr2;
+    s->fd = dupload(fdw.data(), fdw.size(), st);
+    s->flux_E = dupload(c.energies, (size_t)c.n_energies, st);
+    std::vector<double> eta((size_t)n_problems * c.n_energies);
+    for (int p = 0; p < n_problems; p++)
+      std::memcpy(&eta[(size_t)p * c.n_energies], problems[p]->CRP.eta_sq, c.n_energies * sizeof(double));
+    s->flux_eta = dupload(eta.data(), eta.size(), st);
+    s->crp = dalloc<double>((size_t)n_problems * c.n_energies);
+    s->flux_t0 = dalloc<double>(1);
+    s->flux_count = dalloc<int>(1);
+    s->flux_slot = dalloc<int>(1);
+    QD_CUDA(cudaMemsetAsync(s->flux_count, 0, sizeof(int), st));
+    for (int p = 0; p < n_problems; p++) {
+      double2 *dst = s->flux_acc + (int64_t)s->h_pblock0[p] * 2 * c.n_energies * ns;
+      const size_t bytes = (size_t)s->probs[p].n_omegas * 2 * c.n_energies * ns * sizeof(double2);
+      if (problems[p]->CRP.accumulators)
+        QD_CUDA(cudaMemcpyAsync(dst, problems[p]->CRP.accumulators, bytes, cudaMemcpyHostToDevice, st));
+      else
+        QD_CUDA(cudaMemsetAsync(dst, 0, bytes, st));
+    }
+  }
+  s->launches_per_step = count_launches_per_step(s);
+  QD_CUDA(cudaStreamSynchronize(st));
+  QD_CUDA(cudaGetLastError());
+}
+
+// -------------------------------------------------------------- running
+static void check_status(qd_session *s) {
+  QD_CUDA(cudaStreamSynchronize(s->stream));
+  QD_CUDA(cudaGetLastError());
+  int st = 0, stp = 0;
+  QD_CUDA(cudaMemcpy(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st) {
+    QD_CUDA(cudaMemcpy(&stp, s->status_step, sizeof(int), cudaMemcpyDeviceToHost));
+    throw Error{st, "Total module error: norm above 1 at step " + std::to_string(stp) +
+                        " (print_energies, cudaOpenMP2.cu:437-440)"};
+  }
+}
+
+static void flush_flux(qd_session *s) {
+  if (s->flux.enabled && s->flux_pending > 0) {
+    enqueue_flux_dft(s);
+    s->flux_pending = 0;
+  }
+}
+
+static void build_chunk_graph(qd_session *s, int steps) {
+  if (s->graph_chunk) {
+    cudaGraphExecDestroy(s->graph_chunk);
+    s->graph_chunk = nullptr;
+  }
+  cudaGraph_t graph;
+  QD_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    for (int i = 0; i < steps; i++) enqueue_step(s, false);
+    if (s->flux.enabled) enqueue_flux_dft(s);
+  } catch (...) {
+    cudaStreamEndCapture(s->stream, &graph);
+    throw;
+  }
+  QD_CUDA(cudaStreamEndCapture(s->stream, &graph));
+  QD_CUDA(cudaGraphInstantiate(&s->graph_chunk, graph, 0));
+  cudaGraphDestroy(graph);
+  s->graph_steps = steps;
+}
+
+// Enqueue n steps without host synchronisation.
+static void run_steps(qd_session *s, int n) {
+  const int chunk = s->flux.enabled ? s->flux.chunk : 32;
+  while (n > 0) {
+    if (s->steps == 0) {
+      // first step: V(-dt/2) folded into the prologue table (cudaOpenMP2.cu:344)
+      enqueue_step(s, true);
+      s->steps++;
+      n--;
+      if (s->flux.enabled && ++s->flux_pending == s->flux.chunk) flush_flux(s);
+      continue;
+    }
+    if (n >= chunk && s->flux_pending == 0) {
+      if (!s->graph_chunk || s->graph_steps != chunk) build_chunk_graph(s, chunk);
+      QD_CUDA(cudaGraphLaunch(s->graph_chunk, s->stream));
+      s->steps += chunk;
+      n -= chunk;
+      continue;
+    }
+    enqueue_step(s, false);
+    s->steps++;
+    n--;
+    if (s->flux.enabled && ++s->flux_pending == s->flux.chunk) flush_flux(s);
+  }
+}
+
+static void download_psi(qd_session *s, qd_fh2data *const *problems, int n) {
+  const int64_t nth_pt = s->g.npt * s->g.nth;
+  for (int p = 0; p < n; p++)
+    QD_CUDA(cudaMemcpyAsync(problems[p]->OmegaStates.wave_packets, s->psi_th + (int64_t)s->h_pblock0[p] * nth_pt,
+                            (size_t)s->probs[p].n_omegas * nth_pt * sizeof(double2), cudaMemcpyDeviceToHost,
+                            s->stream));
+  QD_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+static void download_crp(qd_session *s, qd_fh2data *const *problems, int n) {
+  if (!s->flux.enabled) return;
+  flush_flux(s);
+  launch_flux_crp(s->stream, s->g, s->flux, s->n_problems, s->d_pblock0, s->flux_acc, s->w, s->flux_eta, s->crp);
+  const int nE = s->flux.n_energies;
+  const int64_t ns = (int64_t)s->g.nth * s->g.n1;
+  for (int p = 0; p < n; p++) {
+    QD_CUDA(cudaMemcpyAsync(problems[p]->CRP.CRP, s->crp + (int64_t)p * nE, nE * sizeof(double),
+                            cudaMemcpyDeviceToHost, s->stream));
+    if (problems[p]->CRP.accumulators)
+      QD_CUDA(cudaMemcpyAsync(problems[p]->CRP.accumulators, s->flux_acc + (int64_t)s->h_pblock0[p] * 2 * nE * ns,
+                              (size_t)s->probs[p].n_omegas * 2 * nE * ns * sizeof(double2), cudaMemcpyDeviceToHost,
+                              s->stream));
+  }
+  QD_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+static void print_energies(qd_session *s, const std::vector<double> &e) {
+  double total_module = 0.0, total_energy = 0.0;
+  for (int b = 0; b < s->n_blocks; b++) {
+    std::printf(" %d %.12f %.12f %.12f %.12f %.12f %.12f\n", s->h_blocks[b].omega, e[b * 6 + 0], e[b * 6 + 1],
+                e[b * 6 + 2], e[b * 6 + 3], e[b * 6 + 4], e[b * 6 + 5]);
+    total_module += e[b * 6 + 0];
+    total_energy += e[b * 6 + 5];
+  }
+  std::printf(" Total: %.12f %.12f\n", total_module, total_energy);
+}
+
+// The evolution loop of test_multiple_cards with callbacks and outputs.
+static void evolve(qd_fh2data *const *problems, int n, qd_callback cb, void *user) {
+  std::unique_ptr<qd_session> s(new qd_session());
+  session_build(s.get(), problems, n);
+  const qd_fh2data *d0 = problems[0];
+  const int total = d0->time.total_steps;
+  const qd_options &op = d0->options;
+  const bool want_rec = op.energies != nullptr;
+  if (want_rec && total > 0) {
+    s->rec_cap = total;
+    s->rec_base = s->steps;
+    s->rec = dalloc<double>((size_t)total * s->n_blocks * 6);
+  }
+  const int every = op.wave_to_matlab ? op.steps_to_copy_psi_from_device_to_host : 0;
+  int done = 0;
+  while (done < total) {
+    // run until the next host-side event: callback step, print, or end
+    int seg = total - done;
+    if (op.print_energies) seg = 1;
+    if (every > 0) {
+      // callback fires after the step whose pre-increment counter is a multiple of `every`
+      const int k = s->steps;   // counter value at the start of the next step
+      const int next = ((k + every - 1) / every) * every;   // first counter >= k divisible by every
+      seg = std::min(seg, next - k + 1);
+    }
+    const int before = s->steps;
+    run_steps(s.get(), seg);
+    done += seg;
+    check_status(s.get());
+    if (op.print_energies) {
+      std::vector<double> e((size_t)s->n_blocks * 6);
+      QD_CUDA(cudaMemcpy(e.data(), s->energies, e.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      std::printf("\n Step: %d\n", s->steps - 1);
+      print_energies(s.get(), e);
+    }
+    const int last = s->steps - 1;   // counter value of the last completed step
+    if (every > 0 && last >= before && last % every == 0) {
+      download_psi(s.get(), problems, n);
+      for (int p = 0; p < n; p++) problems[p]->time.steps = last;
+      if (cb) {
+        for (int p = 0; p < n; p++)
+          if (cb(problems[p], user) != 0) throw Error{QD_ERR_CALLBACK, "wave_to_matlab callback returned an error"};
+      }
+    }
+  }
+  check_status(s.get());
+  download_psi(s.get(), problems, n);
+  download_crp(s.get(), problems, n);
+  for (int p = 0; p < n; p++) problems[p]->time.steps = s->steps;
+  if (want_rec && total > 0) {
+    std::vector<double> r((size_t)total * s->n_blocks * 6);
+    QD_CUDA(cudaMemcpy(r.data(), s->rec, r.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int p = 0; p < n; p++) {
+      double *out = problems[p]->options.energies;
+      if (!out) continue;
+      const int nb = s->probs[p].n_omegas, b0 = s->h_pblock0[p];
+      for (int t = 0; t < total; t++)
+        std::memcpy(out + ((size_t)t * nb) * 6, &r[((size_t)t * s->n_blocks + b0) * 6], (size_t)nb * 6 * sizeof(double));
+    }
+  }
+}
+
+// ---------------------------------------------------------------- C ABI
+#define QD_GUARD(...)                                    \
+  try {                                                  \
+    qd::set_error("");                                   \
+    __VA_ARGS__;                                         \
+    return QD_OK;                                        \
+  } catch (const qd::Error &e) {                         \
+    qd::set_error(e.msg);                                \
+    return e.status;                                     \
+  } catch (const std::bad_alloc &) {                     \
+    qd::set_error("host allocation failed");             \
+    return QD_ERR_NOMEM;                                 \
+  } catch (const std::exception &e) {                    \
+    qd::set_error(e.what());                             \
+    return QD_ERR_INVALID;                               \
+  }
+
+extern "C" {
+
+int qd_version(void) { return QD_VERSION; }
+
+const char *qd_last_error(void) { return qd::g_last_error.c_str(); }
+
+int qd_evolve(qd_fh2data *data, qd_callback cb, void *user) {
+  QD_GUARD({
+    qd_fh2data *p[1] = {data};
+    evolve(p, 1, cb, user);
+  })
+}
+
+int qd_evolve_batch(qd_fh2data *const *problems, int32_t n_problems, qd_callback cb, void *user) {
+  QD_GUARD(evolve(problems, n_problems, cb, user))
+}
+
+int qd_session_create(qd_fh2data *const *problems, int32_t n_problems, qd_session **out) {
+  QD_GUARD({
+    QD_REQUIRE(out != nullptr, "out != NULL");
+    *out = nullptr;
+    std::unique_ptr<qd_session> s(new qd_session());
+    session_build(s.get(), problems, n_problems);
+    *out = s.release();
+  })
+}
+
+int qd_session_destroy(qd_session *s) {
+  QD_GUARD(delete s)
+}
+
+int qd_session_run(qd_session *s, int32_t n_steps) {
+  QD_GUARD({
+    QD_REQUIRE(s && n_steps >= 0, "session && n_steps >= 0");
+    run_steps(s, n_steps);
+    QD_CUDA(cudaGetLastError());
+  })
+}
+
+int qd_session_synchronize(qd_session *s) {
+  QD_GUARD({
+    QD_REQUIRE(s, "session");
+    check_status(s);
+  })
+}
+
+int qd_session_download(qd_session *s, qd_fh2data *const *problems, int32_t n_problems) {
+  QD_GUARD({
+    QD_REQUIRE(s && problems && n_problems == s->n_problems, "session download: same problem count");
+    check_status(s);
+    download_psi(s, problems, n_problems);
+    download_crp(s, problems, n_problems);
+    for (int p = 0; p < n_problems; p++) problems[p]->time.steps = s->steps;
+  })
+}
+
+int qd_session_upload(qd_session *s, qd_fh2data *const *problems, int32_t n_problems) {
+  QD_GUARD({
+    QD_REQUIRE(s && problems && n_problems == s->n_problems, "session upload: same problem count");
+    const int64_t nth_pt = s->g.npt * s->g.nth;
+    for (int p = 0; p < n_problems; p++)
+      QD_CUDA(cudaMemcpyAsync(s->psi_th + (int64_t)s->h_pblock0[p] * nth_pt, problems[p]->OmegaStates.wave_packets,
+                              (size_t)s->probs[p].n_omegas * nth_pt * sizeof(double2), cudaMemcpyHostToDevice,
+                              s->stream));
+  })
+}
+
+void *qd_session_stream(qd_session *s) { return s ? (void *)s->stream : nullptr; }
+
+int qd_session_info(qd_session *s, int32_t *n_blocks, int32_t *launches_per_step) {
+  QD_GUARD({
+    QD_REQUIRE(s, "session");
+    if (n_blocks) *n_blocks = s->n_blocks;
+    if (launches_per_step) *launches_per_step = s->launches_per_step;
+  })
+}
+
+int qd_session_apply(qd_session *s, int32_t stage, double dt) {
+  QD_GUARD({
+    QD_REQUIRE(s, "session");
+    cudaStream_t st = s->stream;
+    const Grid &g = s->g;
+    double2 *tab = nullptr;
+    auto scratch_tab = [&](int64_t n) {
+      double2 *t = dalloc<double2>((size_t)n);
+      return t;
+    };
+    switch (stage) {
+      case QD_STAGE_DUMP: {
+        if (!s->has_mask) break;
+        tab = scratch_tab(g.npt * g.nth);
+        std::vector<double> zero((size_t)g.npt * g.nth, 0.0);
+        double *z = dupload(zero.data(), zero.size(), st);
+        launch_build_theta_table(st, g, z, s->d1, s->d2, 0.0, tab);
+        launch_theta_phase(st, s->psi_th, tab, s->n_blocks, g.npt * g.nth, s->status);
+        QD_CUDA(cudaStreamSynchronize(st));
+        cudaFree(z);
+        break;
+      }
+      case QD_STAGE_POTENTIAL:
+        tab = scratch_tab(g.npt * g.nth);
+        launch_build_theta_table(st, g, s->pot, nullptr, nullptr, dt, tab);
+        launch_theta_phase(st, s->psi_th, tab, s->n_blocks, g.npt * g.nth, s->status);
+        break;
+      case QD_STAGE_FORWARD_LEGENDRE:
+        launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, nullptr,
+                                nullptr, s->status);
+        break;
+      case QD_STAGE_BACKWARD_LEGENDRE:
+        launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
+                                s->part_modpe, s->t_modpe, s->status);
+        break;
+      case QD_STAGE_ROTATIONAL:
+        tab = scratch_tab(g.npt * (g.l_max + 1));
+        launch_build_rot_table(st, g, dt, tab);
+        launch_slab_phase(st, s->psi_j, tab, s->d_slabs, s->n_slabs, g.npt, s->status);
+        break;
+      case QD_STAGE_CORIOLIS:
+      case QD_STAGE_CORIOLIS_ENERGY: {
+        if (!s->any_coupled) break;
+        double2 *ph = dalloc<double2>((size_t)s->h_groups.back().ph0 + (size_t)s->h_groups.back().n * g.n1);
+        launch_build_coriolis_phase(st, g, s->d_groups, s->n_groups, s->max_group_n, s->cor_e, dt, ph);
+        const bool en = stage == QD_STAGE_CORIOLIS_ENERGY;
+        launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, ph,
+                        s->cor_H, en ? s->part_ce : nullptr, s->t_ce, nullptr, s->status);
+        if (en) {
+          EnergyParts ep = energy_parts(s, false, false, false, true);
+          launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
+                                  s->max_group_n, s->energies, nullptr, s->d_step, 0, 0, 1e300, s->status,
+                                  s->status_step, s->n_blocks);
+        }
+        QD_CUDA(cudaStreamSynchronize(st));
+        cudaFree(ph);
+        break;
+      }
+      case QD_STAGE_FFT_KINETIC: {
+        tab = scratch_tab(g.npt);
+        launch_build_kin_table(st, g, s->T1, s->T2, dt, tab);
+        launch_fft_kinetic(st, g, s->fft, s->precision, s->psi_j, s->d_slabs, s->n_slabs, tab, s->T1, s->T2,
+                           s->part_ke, nullptr, s->I1, s->I2, nullptr, s->status);
+        EnergyParts ep = energy_parts(s, false, true, false, false);
+        launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
+                                s->max_group_n, s->energies, nullptr, s->d_step, 0, 0, 1e300, s->status,
+                                s->status_step, s->n_blocks);
+        break;
+      }
+      case QD_STAGE_ENERGIES: {
+        const int t_re_saved = s->t_re;
+        launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->I1, s->I2, s->part_re, s->t_re, s->status);
+        // module and potential energy come from a backward contraction into psi_theta
+        EnergyParts ep = energy_parts(s, true, false, true, false);
+        ep.re_tiles = t_re_saved;
+        launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
+                                s->max_group_n, s->energies, nullptr, s->d_step, 0, 0, 1e300, s->status,
+                                s->status_step, s->n_blocks);
+        break;
+      }
+      case QD_STAGE_FLUX: {
+        QD_REQUIRE(s->flux.enabled, "CRP.calculate_CRP");
+        k_flux_begin<<<1, 1, 0, st>>>(s->d_step, s->flux_count, s->flux_t0, s->dt, s->flux_slot);
+        const int64_t ns = (int64_t)g.nth * g.n1;
+        dim3 grid((unsigned)std::min<int64_t>((ns + 255) / 256, 64), (unsigned)s->n_blocks);
+        k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
+                                                 s->flux_buf, s->n_blocks, s->flux_slot, s->status);
+        k_step_end<<<1, 1, 0, st>>>(s->d_step, s->status, nullptr, nullptr, 0.0, 0);
+        s->steps++;
+        if (++s->flux_pending == s->flux.chunk) flush_flux(s);
+        break;
+      }
+      default:
+        throw Error{QD_ERR_INVALID, "unknown stage"};
+    }
+    QD_CUDA(cudaStreamSynchronize(st));
+    if (tab) cudaFree(tab);
+    QD_CUDA(cudaGetLastError());
+  })
+}
+
+int qd_session_get_psi(qd_session *s, int32_t which, int32_t block, double *host_out, size_t n_doubles) {
+  QD_GUARD({
+    QD_REQUIRE(s && host_out && block >= 0 && block < s->n_blocks, "session, block");
+    const BlockDesc &bd = s->h_blocks[block];
+    const double2 *src;
+    size_t n;
+    if (which == 0) {
+      n = (size_t)s->g.npt * s->g.nth;
+      src = s->psi_th + (int64_t)block * n;
+    } else {
+      n = (size_t)s->g.npt * bd.nl;
+      src = s->psi_j + (int64_t)bd.slab0 * s->g.npt;
+    }
+    QD_REQUIRE(n_doubles == 2 * n, "buffer size");
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    QD_CUDA(cudaMemcpy(host_out, src, n * sizeof(double2), cudaMemcpyDeviceToHost));
+  })
+}
+
+int qd_session_set_psi(qd_session *s, int32_t which, int32_t block, const double *host_in, size_t n_doubles) {
+  QD_GUARD({
+    QD_REQUIRE(s && host_in && block >= 0 && block < s->n_blocks, "session, block");
+    const BlockDesc &bd = s->h_blocks[block];
+    double2 *dst;
+    size_t n;
+    if (which == 0) {
+      n = (size_t)s->g.npt * s->g.nth;
+      dst = s->psi_th + (int64_t)block * n;
+    } else {
+      n = (size_t)s->g.npt * bd.nl;
+      dst = s->psi_j + (int64_t)bd.slab0 * s->g.npt;
+    }
+    QD_REQUIRE(n_doubles == 2 * n, "buffer size");
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    QD_CUDA(cudaMemcpy(dst, host_in, n * sizeof(double2), cudaMemcpyHostToDevice));
+  })
+}
+
+int qd_session_get_energies(qd_session *s, double *host_out, size_t n_doubles) {
+  QD_GUARD({
+    QD_REQUIRE(s && host_out && n_doubles == (size_t)s->n_blocks * 6, "session, buffer size");
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    QD_CUDA(cudaMemcpy(host_out, s->energies, n_doubles * sizeof(double), cudaMemcpyDeviceToHost));
+  })
+}
+
+}  // extern "C"

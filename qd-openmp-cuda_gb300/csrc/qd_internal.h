@@ -1,0 +1,177 @@
+// Internal declarations shared by the host engine and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include "../../include/qd.h"
+
+namespace qd {
+
+// ------------------------------------------------------------------ errors
+void set_error(const std::string &msg);
+struct Error {
+  int status;
+  std::string msg;
+};
+
+#define QD_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      throw ::qd::Error{e_ == cudaErrorMemoryAllocation ? QD_ERR_NOMEM : QD_ERR_CUDA,   \
+                        std::string(#call) + ": " + cudaGetErrorString(e_)};            \
+  } while (0)
+
+#define QD_REQUIRE(cond, msg)                                                           \
+  do {                                                                                  \
+    if (!(cond)) throw ::qd::Error{QD_ERR_INVALID, std::string("insist failed: ") + (msg)}; \
+  } while (0)
+
+// ------------------------------------------------------------- device data
+// One Omega block (one helicity of one total-J problem).
+struct BlockDesc {
+  int32_t problem;
+  int32_t omega;
+  int32_t nl;      // l_max - omega + 1 Legendre slabs
+  int32_t slab0;   // global index of its first Legendre slab
+  int64_t bmat0;   // offset (doubles) of its Legendre matrices in the B pools
+};
+
+// Legendre-space slab: one (block, l) pair, n1*n2 complex values.
+struct SlabDesc {
+  int32_t block;
+  int32_t l;
+};
+
+// One Coriolis coupling group: a fixed l of one problem, coupling the
+// blocks with omega in [omega_lo, omega_hi].
+struct CoriolisGroup {
+  int32_t l;
+  int32_t n;          // omega_hi - omega_lo + 1
+  int32_t block_lo;   // block index of omega_lo
+  int32_t omega_lo;
+  int64_t v0;         // offset (double) of the eigenvectors V[n][n] (V[p*n+a] = component p of vector a)
+  int64_t e0;         // offset (double) of the eigenvalues e[n]
+  int64_t ph0;        // offset (double2) of exp(-i dt e_a/(2 m1 R_i^2)) as ph[a][n1]
+  int64_t h0;         // offset (double) of the matrix H[n][n] (coupling energy)
+};
+
+struct FluxConfig {
+  int enabled;
+  int n_energies;
+  int n_grad;
+  int n_ds;
+  int chunk;           // steps buffered between time-to-energy transforms
+};
+
+enum { E_MODULE = 0, E_POTENTIAL = 1, E_KINETIC = 2, E_ROTATIONAL = 3, E_CORIOLIS = 4, E_TOTAL = 5 };
+
+// ------------------------------------------------------------ kernel API
+// All launches take the session stream.  Pointers are device pointers.
+struct Grid {
+  int n1, n2, nth, l_max;
+  int64_t npt;          // n1*n2
+  double dr1, dr2, m1, m2, left1, left2;
+};
+
+// theta-space phase: psi[b][k][j][i] *= tab[k][j][i] for every block
+void launch_theta_phase(cudaStream_t s, double2 *psi, const double2 *tab, int n_blocks,
+                        int64_t n_per_block, const int *status);
+
+// j-space phase: slab s (l = slabs[s].l) *= tab[l][j][i]
+void launch_slab_phase(cudaStream_t s, double2 *psi_j, const double2 *tab, const SlabDesc *slabs,
+                       int n_slabs, int64_t npt, const int *status);
+
+// FP64 Legendre contractions (SIMT DFMA).
+// forward: psi_j(slab0_b+n) = sum_k wP_b[k][n] (tabA[k] * psi_th[b][k]);  tabA may be null;
+//          epilogue multiplies by tabE[l] (may be null)
+void launch_legendre_fwd_f64(cudaStream_t s, const Grid &g, const double2 *psi_th, double2 *psi_j,
+                             const double *Bfwd, const BlockDesc *blocks, int n_blocks, int max_nl,
+                             const double2 *tabA, const double2 *tabE, const int *status);
+// backward: psi_th[b][k] = sum_n P_b[n][k] (tabA[l] * psi_j(slab0_b+n)); tabA may be null.
+//           partial sums of module and potential energy per CTA -> part[b][tile][2]
+void launch_legendre_bwd_f64(cudaStream_t s, const Grid &g, const double2 *psi_j, double2 *psi_th,
+                             const double *Bbwd, const BlockDesc *blocks, int n_blocks,
+                             const double2 *tabA, const double *w, const double *pot,
+                             double *part, int n_part_tiles, const int *status);
+int legendre_bwd_part_tiles(const Grid &g);
+
+// 2-D FFT over (R, r) of every Legendre slab with the kinetic phase between
+// the passes.  precision: 0 = FP64 butterflies, 1 = FP32 butterflies.
+struct FFTPlan {
+  int n1, n2;
+  int rad1[16], nst1;
+  int rad2[16], nst2;
+  double2 *tw1_d;  float2 *tw1_f;   // exp(-2 pi i t / n1), t < n1
+  double2 *tw2_d;  float2 *tw2_f;
+  int rows_per_cta;
+  int cols_per_cta;
+};
+bool fft_factor(int n, int *rad, int *nst);
+void fft_plan_init(FFTPlan &p, int n1, int n2);
+void fft_plan_free(FFTPlan &p);
+// forward rows -> cols (fwd, kinetic, KE partials, inv) -> rows inverse with
+// scale 1/(n1 n2) and the epilogue phase tabE (may be null) and rotational
+// energy partials (when re_part is non-null).
+void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, int precision, double2 *psi_j,
+                        const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1,
+                        const double *T2, double *ke_part, const double2 *tabE, const double *I1,
+                        const double *I2, double *re_part, const int *status);
+int fft_col_tiles(const FFTPlan &p);
+int fft_row_tiles(const FFTPlan &p);
+
+// rotational energy partials only (for stage-by-stage use)
+void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, const SlabDesc *slabs,
+                       int n_slabs, const double *I1, const double *I2, double *re_part, int tiles,
+                       const int *status);
+
+// Coriolis: in-place psi_l^Omega <- sum_Omega1 U_l[Omega][Omega1](R) psi_l^Omega1 per group,
+// optional coupling-energy partials per block (computed on the input psi),
+// optional epilogue phase tabE[l] (may be null).
+void launch_coriolis(cudaStream_t s, const Grid &g, double2 *psi_j, const BlockDesc *blocks,
+                     const CoriolisGroup *groups, int n_groups, int max_n, const double *V,
+                     const double2 *ph, const double *H, double *ce_part, int ce_tiles,
+                     const double2 *tabE, const int *status);
+void launch_build_coriolis_phase(cudaStream_t s, const Grid &g, const CoriolisGroup *groups, int n_groups,
+                                 int max_n, const double *e, double dt, double2 *ph);
+int coriolis_tiles(const Grid &g);
+
+// Energy finalisation: sums partial arrays per block in a fixed order,
+// writes energies[b][6] (and rec if non-null), applies the norm guard.
+struct EnergyParts {
+  const double *mod_pe;  int mod_pe_tiles;    // [b][tiles][2]
+  const double *ke;      int ke_tiles;        // [slab][tiles]
+  const double *re;      int re_tiles;        // [slab][tiles]
+  const double *ce;      int ce_tiles;        // [b][tiles]
+  int have_ke, have_re, have_ce, have_mod;
+};
+void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &ep, const BlockDesc *blocks,
+                             const int *pblock0, int n_problems, const CoriolisGroup *groups, const int *pgroup0,
+                             int ce_n, double *energies, double *rec, const int *d_step, int rec_base, int rec_cap,
+                             double norm_tol, int *status, int *status_step, int n_blocks);
+
+// flux: extract surface values (A, dA/dr) into buf[slot], then DFT chunks
+void launch_flux_extract(cudaStream_t s, const Grid &g, const FluxConfig &f, const double2 *psi_th,
+                         int n_blocks, const double2 *half_v, const double *fd, double2 *buf, int slot,
+                         const int *status);
+void launch_flux_dft(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_blocks, const double2 *buf,
+                     int count, const double *energies, double t0, double dt, double2 *phase_scratch,
+                     double2 *acc, const int *status);
+void launch_flux_crp(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_problems,
+                     const int *block0_of_problem, const double2 *acc, const double *w, const double *eta_sq,
+                     double *crp);
+
+// table builders (FP64 on the device)
+void launch_build_theta_table(cudaStream_t s, const Grid &g, const double *pot, const double *d1,
+                              const double *d2, double dt, double2 *tab);
+void launch_build_rot_table(cudaStream_t s, const Grid &g, double dt, double2 *tab);
+void launch_build_kin_table(cudaStream_t s, const Grid &g, const double *T1, const double *T2, double dt,
+                            double2 *tab);
+void launch_build_half_v(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
+                         double2 *half_v);
+
+}  // namespace qd

@@ -1,0 +1,207 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle.
+
+Tolerances: FP64 form, element-wise relative L2 error of psi <= 1e-12 after a
+few steps and <= 1e-10 after 500 steps; energies to 1e-11 relative;
+P(E) to 1e-9 of max|P|.  Mixed form: psi <= 1e-5 relative, P(E) <= 1e-4.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300))
+
+
+def make(qd, **kw):
+    steps = kw.pop("steps", 4)
+    cfg = qd.inputs.small_config(steps=steps, **kw)
+    return cfg, qd.inputs.build_fh2data(cfg), qd.inputs.build_fh2data(cfg)
+
+
+CASES = [
+    dict(J=0, n1=16, n2=8, n_theta=6, l_max=5),
+    dict(J=2, parity=0, n1=16, n2=8, n_theta=8, l_max=6),
+    dict(J=3, parity=1, n1=24, n2=12, n_theta=8, l_max=7),
+    dict(J=4, parity=1, n1=32, n2=16, n_theta=10, l_max=8, n_energies=12),
+]
+
+
+@pytest.fixture(scope="module")
+def gpu(lib):
+    return lib
+
+
+def _random_state(o, rng):
+    for b in range(len(o.psi)):
+        o.psi[b] = (rng.standard_normal(o.psi[b].shape) + 1j * rng.standard_normal(o.psi[b].shape)) * 1e-2
+
+
+@pytest.mark.parametrize("case", CASES[:3])
+def test_stages_match_oracle(qd, oracle, gpu, case):
+    """Each reference stage (omegawavepacket.h:79-126) on the same random state."""
+    cfg, d, dref = make(qd, **case)
+    o = oracle.Oracle(dref)
+    rng = np.random.default_rng(7)
+    _random_state(o, rng)
+    dt = cfg.dt
+    with qd.Session(d) as s:
+        for b in range(len(o.psi)):
+            s.set_psi("theta", b, o.psi[b])
+        checks = [
+            ("dump", 0.0, o.dump_wavepacket, "theta"),
+            ("potential", dt, lambda: o.evolution_with_potential(dt), "theta"),
+            ("forward_legendre", 0.0, o.forward_legendre_transform, "j"),
+            ("rotational", dt / 4, lambda: o.evolution_with_rotational(dt / 4), "j"),
+            ("coriolis", dt / 2, lambda: o.evolution_with_coriolis(dt / 2), "j"),
+            ("fft_kinetic", dt, lambda: (o.forward_fft(), o.evolution_with_kinetic(dt), o.backward_fft()), "j"),
+            ("coriolis_energy", dt / 2, lambda: o.evolution_with_coriolis(dt / 2, calculate_energy=True), "j"),
+            ("backward_legendre", 0.0, o.backward_legendre_transform, "theta"),
+        ]
+        for stage, sdt, fn, space in checks:
+            if stage == "fft_kinetic":
+                ke_ref = None
+                o.forward_fft(); o.evolution_with_kinetic(dt); ke_ref = o.kinetic_energy(); o.backward_fft()
+            else:
+                fn()
+            s.apply(stage, sdt)
+            for b in range(len(o.psi)):
+                got = s.get_psi(space, b)
+                ref = o.psi[b] if space == "theta" else o.lpsi[b]
+                assert rel(got, ref) < 1e-13, (stage, b, rel(got, ref))
+            if stage == "fft_kinetic":
+                np.testing.assert_allclose(s.energies()[:, 2], ke_ref, rtol=1e-12, atol=1e-18)
+            if stage == "coriolis_energy":
+                np.testing.assert_allclose(s.energies()[:, 4], o.energies["coriolis"], rtol=1e-10, atol=1e-16)
+        s.apply("energies")
+        e = s.energies()
+        np.testing.assert_allclose(e[:, 0], o.module(), rtol=1e-12)
+        np.testing.assert_allclose(e[:, 1], o.potential_energy(), rtol=1e-11, atol=1e-16)
+        np.testing.assert_allclose(e[:, 3], o.rotational_energy(), rtol=1e-11, atol=1e-16)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_evolve_matches_oracle(qd, oracle, gpu, case):
+    """Full steps of test_multiple_cards (cudaOpenMP2.cu:338-386) via qd_evolve."""
+    cfg, d, dref = make(qd, steps=6, **case)
+    nb = len(d["OmegaStates"]["omegas"])
+    d["options"]["energies"] = np.zeros((cfg.total_steps, nb, 6))
+    o = oracle.Oracle(dref)
+    rec = o.run(cfg.total_steps)
+    qd.cudaOpenMPEvolution(d)
+    assert int(d["time"]["steps"]) == cfg.total_steps
+    assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-12
+    np.testing.assert_allclose(d["options"]["energies"][:, :, :4], rec[:, :, :4], rtol=1e-10, atol=1e-15)
+    np.testing.assert_allclose(d["options"]["energies"][:, :, 4], rec[:, :, 4], rtol=1e-8, atol=1e-14)
+    crp = o.crp()
+    assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-9 * max(1e-30, np.abs(crp).max())
+
+
+def test_fp64_500_steps_reference_grid(qd, oracle, gpu):
+    """64x32x24, J=0, dt=10, 500 steps: relative |dpsi| <= 1e-10 and |dP| <= 1e-8 (relative to max P)."""
+    cfg = qd.inputs.CONFIGS["fh2_j0_64x32x24"]
+    d = qd.inputs.build_fh2data(cfg)
+    o = oracle.Oracle(qd.inputs.build_fh2data(cfg))
+    o.run(cfg.total_steps)
+    qd.cudaOpenMPEvolution(d)
+    assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-10
+    crp = o.crp()
+    assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-8 * np.abs(crp).max()
+
+
+def test_batch_equals_separate_problems(qd, oracle, gpu):
+    """Uneven Omega counts (J = 0, 1, 2, 3) stepped in one batch."""
+    cfgs = [qd.inputs.small_config(J=J, parity=0, n1=16, n2=8, n_theta=8, l_max=6, steps=5, n_energies=8)
+            for J in (0, 1, 2, 3)]
+    ds = [qd.inputs.build_fh2data(c) for c in cfgs]
+    qd.evolve_batch(ds)
+    for c, d in zip(cfgs, ds):
+        o = oracle.Oracle(qd.inputs.build_fh2data(c))
+        o.run(c.total_steps)
+        assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-12
+        crp = o.crp()
+        assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-9 * np.abs(crp).max()
+
+
+def test_callback_sees_copied_wave_packets(qd, oracle, gpu):
+    """wave_to_matlab fires when steps % N == 0, after the D2H copy (cudaOpenMP2.cu:380-384)."""
+    cfg, d, dref = make(qd, J=0, n1=16, n2=8, n_theta=6, l_max=5, steps=7)
+    d["options"]["wave_to_matlab"] = "FH2Matlab.m"
+    d["options"]["steps_to_copy_psi_from_device_to_host"] = 3
+    o = oracle.Oracle(dref)
+    seen = []
+
+    def cb(data):
+        seen.append((int(data["time"]["steps"]), data["OmegaStates"]["wave_packets"].copy()))
+        return 0
+
+    qd.cudaOpenMPEvolution(d, callback=cb)
+    assert [s for s, _ in seen] == [0, 3, 6]
+    for st, psi in seen:
+        while o.steps <= st:
+            o.step()
+        assert rel(psi, o.wave_packets()) < 1e-12
+
+
+def test_callback_error_aborts(qd, gpu):
+    cfg, d, _ = make(qd, J=0, steps=4)
+    d["options"]["wave_to_matlab"] = "FH2Matlab.m"
+    d["options"]["steps_to_copy_psi_from_device_to_host"] = 2
+    with pytest.raises(qd.QDError) as e:
+        qd.cudaOpenMPEvolution(d, callback=lambda data: 1)
+    assert e.value.status == 5
+
+
+def test_norm_guard(qd, gpu):
+    """insist(total_module <= 1) (cudaOpenMP2.cu:437-440) becomes QD_ERR_NORM."""
+    cfg, d, _ = make(qd, J=0, steps=3)
+    d["OmegaStates"]["wave_packets"] *= 1.5
+    with pytest.raises(qd.QDError) as e:
+        qd.cudaOpenMPEvolution(d)
+    assert e.value.status == 4
+    assert "step 0" in str(e.value)
+
+
+def test_resume_in_two_calls(qd, gpu):
+    """time.steps is in/out: two calls of N steps equal one call of 2N (V(-dt/2) only at steps == 0)."""
+    cfg, d1, _ = make(qd, J=2, parity=0, n1=16, n2=8, n_theta=8, l_max=6, steps=8, n_energies=8)
+    d2 = qd.inputs.build_fh2data(cfg)
+    qd.cudaOpenMPEvolution(d1)
+    nb = len(d2["OmegaStates"]["omegas"])
+    acc = np.zeros((nb, 2, 8, cfg.n_theta, cfg.n1), np.complex128)
+    d2["CRP"]["accumulators"] = acc
+    d2["time"]["total_steps"] = 4
+    qd.cudaOpenMPEvolution(d2)
+    assert int(d2["time"]["steps"]) == 4
+    qd.cudaOpenMPEvolution(d2)
+    assert int(d2["time"]["steps"]) == 8
+    assert rel(d2["OmegaStates"]["wave_packets"], d1["OmegaStates"]["wave_packets"]) < 1e-13
+    np.testing.assert_allclose(d2["CRP"]["CRP"], d1["CRP"]["CRP"], rtol=1e-11, atol=1e-14)
+
+
+def test_norm_conserved_at_production_grid(qd, gpu):
+    """256x128x96, l_max=95, no mask: the module stays 1 (unitary factors) over 20 steps."""
+    cfg = qd.inputs.CONFIGS["fh2_j0_256x128x96"]
+    d = qd.inputs.build_fh2data(cfg)
+    d["dump1"] = None
+    d["dump2"] = None
+    d["time"]["total_steps"] = 20
+    d["CRP"]["calculate_CRP"] = 0
+    d["options"]["energies"] = np.zeros((20, 1, 6))
+    qd.cudaOpenMPEvolution(d)
+    mod = d["options"]["energies"][:, 0, 0]
+    np.testing.assert_allclose(mod, 1.0, atol=1e-12)
+    tot = d["options"]["energies"][:, 0, 5]
+    assert np.ptp(tot) < 1e-4 * abs(tot.mean())
+
+
+def test_mixed_precision_close_to_fp64(qd, oracle, gpu):
+    cfg, d, dref = make(qd, J=2, parity=0, n1=32, n2=16, n_theta=8, l_max=6, steps=20, n_energies=8)
+    d["options"]["precision"] = 1
+    o = oracle.Oracle(dref)
+    o.run(cfg.total_steps)
+    qd.cudaOpenMPEvolution(d)
+    assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-5
+    crp = o.crp()
+    assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-4 * max(1.0, np.abs(crp).max())
