@@ -1,0 +1,338 @@
+"""Benchmark: split-operator Omega-block steps/s on the 256x128x96 J=0 F+H2 workload.
+
+Contract (one JSON line on rank 0):
+  value      = Omega-block steps/s of the mixed-precision form, device-resident
+               state, CUDA events on the session stream around exactly K steps
+  e2e        = the same metric through the public call cudaOpenMPEvolution
+               (qd_evolve) with pinned host buffers, host<->device copies and
+               device set-up inside the timed region (the reference's own timing
+               hook: tic/toc around the MEX call, FH2main.m:212-215)
+  fp64       = the plain FP64 form on the same GPU, and the mixed/FP64 ratio
+  roofline   = dominant kernel of the mixed form, per-launch CUDA-event time
+  cpu_baseline = the FP64 numpy oracle on the host cores (bounded sample)
+
+Multi-GPU: Omega blocks of one J are coupled every half step, different total
+J are independent, so N GPUs run N independent replicas (weak scaling, no
+data-path collective); the barrier and max-over-ranks timing use torch.distributed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+import __graft_entry__ as entry  # noqa: E402
+
+WORKLOAD = "fh2_j0_256x128x96"
+METRIC = "split-op steps/s per Omega-block (256x128x96 c128); mixed-vs-FP64 at dP<=1e-4"
+UNIT = "Omega-block steps/s"
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def algorithmic(kernel: str, d: dict, flux_chunk: int = 32):
+    """Algorithmic flops or bytes of one launch of ``kernel`` on FH2Data ``d``:
+    returns (bound, amount, unit_of_rate)."""
+    n1, n2, nth = int(d["r1"]["n"]), int(d["r2"]["n"]), int(d["theta"]["n"])
+    lmax = int(d["OmegaStates"]["l_max"])
+    npt = n1 * n2
+    nls = [lmax - int(o) + 1 for o in np.ravel(d["OmegaStates"]["omegas"])]
+    nb = len(nls)
+    snl = sum(nls)
+    prec = int(d["options"].get("precision", 0))
+    if kernel in ("legendre_forward", "legendre_backward"):
+        flops = sum(4.0 * npt * nth * nl for nl in nls)
+        if prec == 0:
+            return "fp64", flops, "TFLOP/s"
+        return "tensor", flops, "TFLOP/s"
+    if kernel == "fft_rows_forward" or kernel == "fft_cols_kinetic":
+        return "hbm", 32.0 * npt * snl, "GB/s"
+    if kernel == "fft_rows_inverse":
+        return "hbm", 48.0 * npt * snl, "GB/s"
+    if kernel == "flux_dft":
+        ne = int(d["CRP"]["n_energies"])
+        return "fp64", 8.0 * ne * 2 * nth * n1 * flux_chunk * nb, "TFLOP/s"
+    return "hbm", 0.0, "GB/s"
+
+
+def peaks():
+    p = {}
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        p = json.loads(f.read_text())
+    return {"hbm_gbs": p.get("hbm_gbs", 6800.0), "bf16_tflops": p.get("bf16_tflops", 1900.0),
+            "source": "measured" if f.exists() else "fallback"}
+
+
+def read_traffic():
+    """Per-launch DRAM bytes from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "dram_traffic.txt"
+    out = {}
+    if f.exists():
+        for line in f.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+def run_form(qd, precision: int, steps: int, warmup: int, sampler=None):
+    import torch
+
+    cfg = qd.inputs.CONFIGS[WORKLOAD]
+    d = qd.inputs.build_fh2data(cfg)
+    d["options"]["precision"] = precision
+    with qd.Session(d) as s:
+        stream = torch.cuda.ExternalStream(s.stream())
+        s.run(warmup)
+        s.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        if torch.distributed.is_initialized():
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.start()
+        e0.record(stream)
+        s.run(steps)
+        e1.record(stream)
+        e1.synchronize()
+        s.synchronize()
+        if sampler:
+            clocks = sampler.stop()
+        else:
+            clocks = None
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if torch.distributed.is_initialized():
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        prof = s.profile(64)
+        psi = s.get_psi("theta", 0)
+        return {"ms": ms, "n_blocks": s.n_blocks, "launches_per_step": s.launches_per_step, "profile": prof,
+                "clocks": clocks, "psi": psi, "d": d}
+
+
+def e2e(qd, precision: int, steps: int):
+    """K steps through cudaOpenMPEvolution with pinned host buffers."""
+    import torch
+
+    cfg = qd.inputs.CONFIGS[WORKLOAD]
+    d = qd.inputs.build_fh2data(cfg)
+    d["options"]["precision"] = precision
+    d["time"]["total_steps"] = steps
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype={np.dtype(np.float64): torch.float64,
+                                        np.dtype(np.complex128): torch.complex128}[a.dtype], pin_memory=True)
+        out = t.numpy()
+        out[...] = a
+        return out, t
+
+    keep = []
+    wp, t1 = pinned(d["OmegaStates"]["wave_packets"])
+    pot, t2 = pinned(d["pot"])
+    keep += [t1, t2]
+    d["OmegaStates"]["wave_packets"] = wp
+    d["pot"] = pot
+    h2d = wp.nbytes + pot.nbytes + d["OmegaStates"]["associated_legendres"].nbytes
+    d2h = wp.nbytes + d["CRP"]["CRP"].nbytes
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    qd.cudaOpenMPEvolution(d)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    nb = len(np.ravel(d["OmegaStates"]["omegas"]))
+    return {"value": steps * nb / sec, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
+            "d2h_bytes_per_step": d2h / steps, "seconds": sec, "steps": steps,
+            "note": "one qd_evolve call of K steps: H2D of psi/pot/Legendre matrices, table build, "
+                    "K steps, D2H of psi and P(E); bytes are per step over the call"}
+
+
+def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 1):
+    cfg = qd.inputs.CONFIGS[WORKLOAD]
+    d = qd.inputs.build_fh2data(cfg)
+    o = oracle.Oracle(d)
+    for _ in range(warm):
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(n_steps):
+        o.step()
+    sec = time.perf_counter() - t0
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return {"value": n_steps * len(o.omegas) / sec, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n_steps} FP64 oracle steps (numpy/scipy, pocketfft + OpenBLAS) of the "
+                      f"{WORKLOAD} workload after {warm} warm-up step"}
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    qd = entry.load_package()
+    oracle = entry.load_oracle()
+    n = max(1, min(args.steps, 10))
+    cb = cpu_baseline(qd, oracle, n_steps=n, warm=min(args.warmup, 1))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (c128)",
+            "data": "synthetic (LEPS F+H2, seeded/deterministic)",
+            "config": {"workload": WORKLOAD, "grid": [256, 128, 96], "l_max": 95, "J": 0, "dt": 10.0,
+                       "n_energies": 400, "parallelism": "replicas"},
+            "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": cb["sample"]},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference cannot run here (MATLAB MEX, CUDA samples, MKL, sm_37/52); its CPU "
+                    "restatement (FP64 oracle) runs on the host cores"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        return
+    args.warmup = max(args.warmup, 3)
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    qd = entry.load_package()
+    qd.load_library()
+    gpu_index = local
+    if os.environ.get("CUDA_VISIBLE_DEVICES"):
+        vis = os.environ["CUDA_VISIBLE_DEVICES"].split(",")
+        if local < len(vis) and vis[local].strip().isdigit():
+            gpu_index = int(vis[local])
+    fp64_peak, fp32_peak = qd.fma_peaks()
+    mixed = run_form(qd, 1, args.steps, args.warmup, ClockSampler(gpu_index))
+    fp64 = run_form(qd, 0, args.steps, args.warmup)
+    nb = mixed["n_blocks"]
+    value = world * args.steps * nb / (mixed["ms"] / 1e3)
+    fp64_value = world * args.steps * nb / (fp64["ms"] / 1e3)
+    # same number of steps from the same state: accuracy of the mixed form
+    steps_done = args.warmup + args.steps + 64
+    dpsi = float(np.linalg.norm(mixed["psi"] - fp64["psi"]) / np.linalg.norm(fp64["psi"]))
+    # roofline of the dominant kernel of the headline (mixed) form
+    pk = peaks()
+    prof = mixed["profile"]
+    dom = max(prof, key=lambda k: prof[k]["ms"] * prof[k]["per_step"])
+    bound, amount, unit = algorithmic(dom, mixed["d"])
+    t = prof[dom]["ms"] * 1e-3
+    if bound == "hbm":
+        achieved, peak, psrc = amount / t / 1e9, pk["hbm_gbs"], f"{pk['source']} hbm_gbs"
+    elif bound == "tensor":
+        achieved, peak, psrc = amount / t / 1e12, pk["bf16_tflops"] / 6.0, f"{pk['source']} bf16_tflops / 6 (3-term split)"
+    else:
+        achieved, peak, psrc = amount / t / 1e12, fp64_peak, "measured FP64 FMA loop (qd_device_fma_peaks)"
+    traffic = read_traffic().get(dom)
+    kernels = {k: {"ms": round(v["ms"], 5), "per_step": v["per_step"],
+                   "share": round(v["ms"] * v["per_step"] / sum(x["ms"] * x["per_step"] for x in prof.values()), 4)}
+               for k, v in prof.items()}
+    fp64_prof = fp64["profile"]
+    fdom = max(fp64_prof, key=lambda k: fp64_prof[k]["ms"] * fp64_prof[k]["per_step"])
+    fb, fa, fu = algorithmic(fdom, fp64["d"])
+    fach = fa / (fp64_prof[fdom]["ms"] * 1e-3) / (1e12 if fu == "TFLOP/s" else 1e9)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 storage; bf16x3-split Legendre GEMM / fp32 FFT; fp64 phases, norms, flux",
+        "data": "synthetic (LEPS F+H2, deterministic inputs built on the host)",
+        "config": {"workload": WORKLOAD, "grid": [256, 128, 96], "l_max": 95, "J": 0, "omega_blocks": nb,
+                   "dt": 10.0, "n_energies": 400, "flux": True, "parallelism": f"replicas x{world}",
+                   "l2": "working set ~0.9 GB per replica (> 129 MB L2), no flush needed"},
+        "fp64": {"value": fp64_value, "ms_per_step": fp64["ms"] / args.steps,
+                 "dominant_kernel": fdom, "dominant_achieved": fach, "dominant_unit": fu,
+                 "fp64_fma_peak_tflops": fp64_peak},
+        "mixed_over_fp64": value / fp64_value,
+        "mixed_rel_dpsi_vs_fp64": dpsi, "accuracy_steps": steps_done,
+        "roofline": {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "peak_source": psrc,
+                     "unit": unit, "frac": achieved / peak, "traffic": traffic,
+                     "algorithmic_per_launch": amount},
+        "kernels": kernels,
+        "gpu_launches": mixed["launches_per_step"] * args.steps + 3 * (args.steps // 32),
+        "clocks": mixed["clocks"],
+        "measured_fma_tflops": {"fp64": fp64_peak, "fp32": fp32_peak},
+    }
+    if rank == 0:
+        line["e2e"] = e2e(qd, 1, args.steps)
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(qd, entry.load_oracle())
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

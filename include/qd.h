@@ -209,6 +209,20 @@ int qd_session_set_psi(qd_session *s, int32_t which, int32_t block, const double
 /* energies of the last completed step or stage: [n_blocks][6] */
 int qd_session_get_energies(qd_session *s, double *host_out, size_t n_doubles);
 
+/* ------------------------------------------------------------ diagnostics */
+
+/* Runs n_steps regular time steps eagerly with a CUDA event after every
+   kernel launch on the session stream and reports, per kernel name, the mean
+   duration of one launch (ms) and the launches per step.  names receives the
+   kernel names separated by '\n'. */
+int qd_session_profile(qd_session *s, int32_t n_steps, char *names, size_t names_cap, double *avg_ms,
+                       int32_t *launches_per_step, int32_t max_kernels, int32_t *n_kernels);
+
+/* Measured FP64 fused-multiply-add throughput of the current device
+   (TFLOP/s, 2 flops per FMA) from a register-resident DFMA loop, and the
+   same for FP32 FMA. */
+int qd_device_fma_peaks(double *fp64_tflops, double *fp32_tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,8 +26,13 @@ from __future__ import annotations
 import math
 from typing import List, Optional
 
+import os
+
 import numpy as np
+import scipy.fft
 import scipy.linalg
+
+_WORKERS = os.cpu_count() or 1
 
 
 def _fd_weights(n_points: int) -> np.ndarray:
@@ -200,12 +205,12 @@ class Oracle:
     def forward_fft(self):
         """cufft Z2Z forward over dims {n2, n1} (wavepackets1device.cu:186-201)."""
         for b in range(len(self.lpsi)):
-            self.lpsi[b] = np.fft.fft2(self.lpsi[b], axes=(1, 2))
+            self.lpsi[b] = scipy.fft.fft2(self.lpsi[b], axes=(1, 2), workers=_WORKERS)
 
     def backward_fft(self):
         """cufft Z2Z inverse + ZDSCAL 1/(n1 n2) (omegawavepacket.cu:250-269)."""
         for b in range(len(self.lpsi)):
-            self.lpsi[b] = np.fft.ifft2(self.lpsi[b], axes=(1, 2))
+            self.lpsi[b] = scipy.fft.ifft2(self.lpsi[b], axes=(1, 2), workers=_WORKERS)
 
     def evolution_with_kinetic(self, dt):
         """``_evolution_with_kinetic_`` (evolutionCUDAaux.cu:13-31)."""

@@ -94,7 +94,7 @@ _lib = None
 EXPORTED = ("qd_evolve", "qd_evolve_batch", "qd_last_error", "qd_version", "qd_session_create",
             "qd_session_destroy", "qd_session_run", "qd_session_synchronize", "qd_session_download",
             "qd_session_upload", "qd_session_stream", "qd_session_info", "qd_session_apply", "qd_session_get_psi",
-            "qd_session_set_psi", "qd_session_get_energies")
+            "qd_session_set_psi", "qd_session_get_energies", "qd_session_profile", "qd_device_fma_peaks")
 
 
 def library_path() -> Path:
@@ -128,6 +128,9 @@ def load_library():
     lib.qd_session_get_psi.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(C.c_double), C.c_size_t]
     lib.qd_session_set_psi.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(C.c_double), C.c_size_t]
     lib.qd_session_get_energies.argtypes = [C.c_void_p, P(C.c_double), C.c_size_t]
+    lib.qd_session_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double),
+                                       P(C.c_int32), C.c_int32, P(C.c_int32)]
+    lib.qd_device_fma_peaks.argtypes = [P(C.c_double), P(C.c_double)]
     _lib = lib
     return lib
 
@@ -344,10 +347,28 @@ class Session:
         _check(self.lib.qd_session_set_psi(self.h, 0 if which == "theta" else 1, block,
                                            C.cast(v.ctypes.data, C.POINTER(C.c_double)), v.size * 2))
 
+    def profile(self, n_steps: int) -> dict:
+        """Mean per-launch duration (ms) and launches per step of every kernel over n_steps."""
+        names = C.create_string_buffer(4096)
+        avg = (C.c_double * 64)()
+        cnt = (C.c_int32 * 64)()
+        nk = C.c_int32()
+        _check(self.lib.qd_session_profile(self.h, int(n_steps), names, 4096, avg, cnt, 64, C.byref(nk)))
+        keys = names.value.decode().split("\n")
+        return {k: {"ms": avg[i], "per_step": cnt[i]} for i, k in enumerate(keys[: nk.value])}
+
     def energies(self) -> np.ndarray:
         out = np.empty((self.n_blocks, 6))
         _check(self.lib.qd_session_get_energies(self.h, _dptr(out), out.size))
         return out
+
+
+def fma_peaks() -> tuple:
+    """Measured (FP64, FP32) FMA throughput of the current device in TFLOP/s."""
+    lib = load_library()
+    a, b = C.c_double(), C.c_double()
+    _check(lib.qd_device_fma_peaks(C.byref(a), C.byref(b)))
+    return a.value, b.value
 
 
 def build(force: bool = False) -> Path:

@@ -1,0 +1,46 @@
+// Diagnostics: a register-resident FMA loop to measure the device's FP64 and
+// FP32 FMA throughput (the denominators of the FP64 roofline fractions).
+#include "qd_internal.h"
+
+namespace qd {
+
+template <typename T>
+__global__ void k_fma_loop(T *out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; i++) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  const T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == (T)-12345.0) out[threadIdx.x] = s;   // keeps the loop live
+}
+
+template <typename T>
+static double measure(int iters) {
+  int dev = 0, sms = 0;
+  QD_CUDA(cudaGetDevice(&dev));
+  QD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  T *out = nullptr;
+  QD_CUDA(cudaMalloc(&out, 1024 * sizeof(T)));
+  cudaEvent_t e0, e1;
+  QD_CUDA(cudaEventCreate(&e0));
+  QD_CUDA(cudaEventCreate(&e1));
+  const int blocks = sms * 8, threads = 256;
+  k_fma_loop<T><<<blocks, threads>>>(out, iters / 10, (T)0.999999, (T)1e-7);   // warm-up
+  QD_CUDA(cudaEventRecord(e0));
+  k_fma_loop<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+  QD_CUDA(cudaEventRecord(e1));
+  QD_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  QD_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+  return flops / (ms * 1e-3) / 1e12;
+}
+
+double measure_fp64_tflops() { return measure<double>(20000); }
+double measure_fp32_tflops() { return measure<float>(400000); }
+
+}  // namespace qd

@@ -329,12 +329,15 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
   const unsigned nrow_ctas = (unsigned)(rows / p.rows_per_cta);
   k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 0, g, 1.0, slabs,
                                                         nullptr, nullptr, 0, status);
+  prof_mark(s, "fft_rows_forward");
   const unsigned ncol_ctas = (unsigned)(n_slabs * (p.n1 / p.cols_per_cta));
   k_fft_cols<R><<<ncol_ctas, FFT_THREADS, sm_cols, s>>>(psi_j, r2, p.cols_per_cta, g, tw2, tab_kin, T1, T2, ke_part,
                                                         fft_col_tiles(p), status);
+  prof_mark(s, "fft_cols_kinetic");
   k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 1, g,
                                                         1.0 / ((double)g.n1 * g.n2), slabs, tabE, re_part,
                                                         fft_row_tiles(p), status);
+  prof_mark(s, "fft_rows_inverse");
 }
 
 void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, int precision, double2 *psi_j,

@@ -126,11 +126,12 @@ void launch_flux_dft(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_b
 // Same transform with the step count read from the device, so that it can sit
 // inside a captured CUDA graph; the phase table holds rows n < *count_p.
 __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_dev(int64_t ns2, int nE, int n_blocks, const int *count_p,
+                                                               int cap,
                                                                const double2 *__restrict__ buf,
                                                                const double2 *__restrict__ phase,
                                                                double2 *__restrict__ acc, const int *status) {
   if (status && *status) return;
-  const int count = min(*count_p, FLUX_MAXC);
+  const int count = min(min(*count_p, cap), FLUX_MAXC);
   if (count <= 0) return;
   __shared__ double2 ph[FLUX_MAXC][FLUX_EB];
   const int b = blockIdx.z;

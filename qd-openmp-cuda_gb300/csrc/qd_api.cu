@@ -21,6 +21,22 @@ namespace qd {
 static thread_local std::string g_last_error;
 void set_error(const std::string &msg) { g_last_error = msg; }
 
+struct Profiler {
+  cudaEvent_t start = nullptr;
+  std::vector<cudaEvent_t> ev;
+  std::vector<std::string> names;
+};
+static thread_local Profiler *g_prof = nullptr;
+
+void prof_mark(cudaStream_t s, const char *name) {
+  if (!g_prof) return;
+  cudaEvent_t e;
+  QD_CUDA(cudaEventCreate(&e));
+  QD_CUDA(cudaEventRecord(e, s));
+  g_prof->ev.push_back(e);
+  g_prof->names.push_back(name);
+}
+
 // ------------------------------------------------------- Coriolis matrices
 // Tridiagonal Omega matrix of setup_coriolis_matrix (CoriolisMatrix.C:63-99):
 // diagonal J(J+1) - 2 Omega^2, off-diagonal -lambda(J,Omega) lambda(l,Omega)
@@ -215,7 +231,8 @@ template <typename T> static T *dupload(const T *h, size_t n, cudaStream_t s) {
 
 __global__ void k_step_end(int *step, const int *status, int *flux_count, double *flux_t0, double dt,
                            int flux_on);
-__global__ void k_flux_begin(const int *step, int *flux_count, double *flux_t0, double dt, int *slot_out);
+__global__ void k_flux_begin(const int *step, int *flux_count, double *flux_t0, double dt, int *slot_out, int cap,
+                             int *status);
 
 }  // namespace qd
 
@@ -281,9 +298,17 @@ __global__ void k_step_end(int *step, const int *status, int *, double *, double
   *step += 1;
 }
 
-// sets the flux slot for this step; records t0 when the chunk starts
-__global__ void k_flux_begin(const int *step, int *flux_count, double *flux_t0, double dt, int *slot_out) {
+// sets the flux slot for this step; records t0 when the chunk starts.  A full
+// buffer (which the host scheduling never produces) stops the run with an
+// error status instead of writing past the buffer.
+__global__ void k_flux_begin(const int *step, int *flux_count, double *flux_t0, double dt, int *slot_out, int cap,
+                             int *status) {
   const int c = *flux_count;
+  if (c >= cap) {
+    atomicCAS(status, 0, QD_ERR_INVALID);
+    *slot_out = 0;
+    return;
+  }
   if (c == 0) *flux_t0 = (*step + 1) * dt;
   *slot_out = c;
   *flux_count = c + 1;
@@ -349,7 +374,7 @@ qd_session::~qd_session() {
 namespace qd {
 
 // flux DFT reading count/t0 from the device (graph friendly)
-__global__ void k_flux_dft_dev(int64_t ns2, int nE, int n_blocks, const int *count_p,
+__global__ void k_flux_dft_dev(int64_t ns2, int nE, int n_blocks, const int *count_p, int cap,
                                const double2 *__restrict__ buf, const double2 *__restrict__ phase,
                                double2 *__restrict__ acc, const int *status);
 
@@ -358,11 +383,14 @@ static void enqueue_flux_dft(qd_session *s) {
   const int cap = s->flux.chunk;
   k_flux_phase_dev<<<(nE * cap + 255) / 256, 256, 0, s->stream>>>(s->flux_E, nE, cap, s->flux_count, s->flux_t0,
                                                                    s->dt, s->flux_phase);
+  prof_mark(s->stream, "flux_phase");
   const int64_t ns2 = 2LL * s->g.nth * s->g.n1;
   dim3 grid((unsigned)((ns2 + 127) / 128), (unsigned)((nE + 7) / 8), (unsigned)s->n_blocks);
-  k_flux_dft_dev<<<grid, 128, 0, s->stream>>>(ns2, nE, s->n_blocks, s->flux_count, s->flux_buf, s->flux_phase,
+  k_flux_dft_dev<<<grid, 128, 0, s->stream>>>(ns2, nE, s->n_blocks, s->flux_count, cap, s->flux_buf, s->flux_phase,
                                                s->flux_acc, s->status);
+  prof_mark(s->stream, "flux_dft");
   k_flux_reset<<<1, 1, 0, s->stream>>>(s->flux_count);
+  prof_mark(s->stream, "flux_reset");
 }
 
 static EnergyParts energy_parts(qd_session *s, bool mod, bool ke, bool re, bool ce) {
@@ -391,10 +419,12 @@ static void enqueue_step(qd_session *s, bool first) {
   // forward_legendre_transform, rotational(dt/4) [x2 fused when uncoupled] -> epilogue
   launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, tabA,
                           s->any_coupled ? s->tab_rot4 : s->tab_rot2, s->status);
+  prof_mark(st, "legendre_forward");
   if (s->any_coupled) {
     // evolution_with_coriolis(dt/2) + rotational(dt/4)
     launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
                     s->cor_H, nullptr, s->t_ce, s->tab_rot4, s->status);
+    prof_mark(st, "coriolis");
   }
   // forward FFT, kinetic(dt), kinetic energy, backward FFT + scale, rotational(dt/4)
   launch_fft_kinetic(st, g, s->fft, s->precision, s->psi_j, s->d_slabs, s->n_slabs, s->tab_kin, s->T1, s->T2,
@@ -404,23 +434,30 @@ static void enqueue_step(qd_session *s, bool first) {
     // evolution_with_coriolis(dt/2, energy) + rotational(dt/4), then the rotational energy
     launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
                     s->cor_H, s->part_ce, s->t_ce, s->tab_rot4, s->status);
+    prof_mark(st, "coriolis_energy");
     launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->I1, s->I2, s->part_re, s->t_re, s->status);
+    prof_mark(st, "rotational_energy");
   }
   // backward_legendre_transform + potential energy + module
   launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
                           s->part_modpe, s->t_modpe, s->status);
+  prof_mark(st, "legendre_backward");
   EnergyParts ep = energy_parts(s, true, true, true, s->any_coupled);
   launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                           s->max_group_n, s->energies, s->rec, s->d_step, s->rec_base, s->rec_cap, s->norm_tol,
                           s->status, s->status_step, s->n_blocks);
+  prof_mark(st, "energy_finalize");
   if (s->flux.enabled) {
-    k_flux_begin<<<1, 1, 0, st>>>(s->d_step, s->flux_count, s->flux_t0, s->dt, s->flux_slot);
+    k_flux_begin<<<1, 1, 0, st>>>(s->d_step, s->flux_count, s->flux_t0, s->dt, s->flux_slot, s->flux.chunk,
+                                  s->status);
     const int64_t ns = (int64_t)g.nth * g.n1;
     dim3 grid((unsigned)std::min<int64_t>((ns + 255) / 256, 64), (unsigned)s->n_blocks);
     k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
                                              s->flux_buf, s->n_blocks, s->flux_slot, s->status);
+    prof_mark(st, "flux_extract");
   }
   k_step_end<<<1, 1, 0, st>>>(s->d_step, s->status, nullptr, nullptr, 0.0, 0);
+  prof_mark(st, "step_end");
 }
 
 static int count_launches_per_step(qd_session *s) {
@@ -1006,7 +1043,8 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       }
       case QD_STAGE_FLUX: {
         QD_REQUIRE(s->flux.enabled, "CRP.calculate_CRP");
-        k_flux_begin<<<1, 1, 0, st>>>(s->d_step, s->flux_count, s->flux_t0, s->dt, s->flux_slot);
+        k_flux_begin<<<1, 1, 0, st>>>(s->d_step, s->flux_count, s->flux_t0, s->dt, s->flux_slot, s->flux.chunk,
+                                  s->status);
         const int64_t ns = (int64_t)g.nth * g.n1;
         dim3 grid((unsigned)std::min<int64_t>((ns + 255) / 256, 64), (unsigned)s->n_blocks);
         k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
@@ -1060,6 +1098,72 @@ int qd_session_set_psi(qd_session *s, int32_t which, int32_t block, const double
     QD_REQUIRE(n_doubles == 2 * n, "buffer size");
     QD_CUDA(cudaStreamSynchronize(s->stream));
     QD_CUDA(cudaMemcpy(dst, host_in, n * sizeof(double2), cudaMemcpyHostToDevice));
+  })
+}
+
+int qd_session_profile(qd_session *s, int32_t n_steps, char *names, size_t names_cap, double *avg_ms,
+                       int32_t *launches_per_step, int32_t max_kernels, int32_t *n_kernels) {
+  Profiler prof;
+  struct Reset {
+    Profiler *p;
+    ~Reset() {
+      g_prof = nullptr;
+      if (p->start) cudaEventDestroy(p->start);
+      for (cudaEvent_t e : p->ev) cudaEventDestroy(e);
+    }
+  } reset{&prof};
+  QD_GUARD({
+    QD_REQUIRE(s && n_steps > 0 && names && avg_ms && launches_per_step && n_kernels, "profile arguments");
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    flush_flux(s);
+    QD_CUDA(cudaEventCreate(&prof.start));
+    QD_CUDA(cudaEventRecord(prof.start, s->stream));
+    g_prof = &prof;
+    for (int i = 0; i < n_steps; i++) {
+      enqueue_step(s, false);
+      s->steps++;
+      if (s->flux.enabled && ++s->flux_pending == s->flux.chunk) flush_flux(s);
+    }
+    g_prof = nullptr;
+    check_status(s);
+    std::vector<std::string> order;
+    std::vector<double> tot;
+    std::vector<int> cnt;
+    cudaEvent_t prev = prof.start;
+    for (size_t i = 0; i < prof.ev.size(); i++) {
+      float ms = 0;
+      QD_CUDA(cudaEventElapsedTime(&ms, prev, prof.ev[i]));
+      prev = prof.ev[i];
+      size_t k = 0;
+      while (k < order.size() && order[k] != prof.names[i]) k++;
+      if (k == order.size()) {
+        order.push_back(prof.names[i]);
+        tot.push_back(0.0);
+        cnt.push_back(0);
+      }
+      tot[k] += ms;
+      cnt[k] += 1;
+    }
+    QD_REQUIRE((int)order.size() <= max_kernels, "max_kernels too small");
+    std::string joined;
+    for (size_t k = 0; k < order.size(); k++) {
+      avg_ms[k] = tot[k] / cnt[k];
+      launches_per_step[k] = cnt[k] / n_steps;
+      joined += order[k];
+      if (k + 1 < order.size()) joined += "\n";
+    }
+    QD_REQUIRE(joined.size() + 1 <= names_cap, "names buffer too small");
+    std::memcpy(names, joined.c_str(), joined.size() + 1);
+    *n_kernels = (int32_t)order.size();
+  })
+}
+
+int qd_device_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
+  QD_GUARD({
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw Error{QD_ERR_NO_DEVICE, "no CUDA device"};
+    if (fp64_tflops) *fp64_tflops = measure_fp64_tflops();
+    if (fp32_tflops) *fp32_tflops = measure_fp32_tflops();
   })
 }
 

