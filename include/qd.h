@@ -213,10 +213,10 @@ int qd_session_get_energies(qd_session *s, double *host_out, size_t n_doubles);
 
 /* Runs n_steps regular time steps eagerly with a CUDA event after every
    kernel launch on the session stream and reports, per kernel name, the mean
-   duration of one launch (ms) and the launches per step.  names receives the
-   kernel names separated by '\n'. */
+   duration of one launch (ms) and its number of launches over the n_steps.
+   names receives the kernel names separated by '\n'. */
 int qd_session_profile(qd_session *s, int32_t n_steps, char *names, size_t names_cap, double *avg_ms,
-                       int32_t *launches_per_step, int32_t max_kernels, int32_t *n_kernels);
+                       int32_t *launches, int32_t max_kernels, int32_t *n_kernels);
 
 /* Measured FP64 fused-multiply-add throughput of the current device
    (TFLOP/s, 2 flops per FMA) from a register-resident DFMA loop, and the

@@ -355,7 +355,7 @@ class Session:
         nk = C.c_int32()
         _check(self.lib.qd_session_profile(self.h, int(n_steps), names, 4096, avg, cnt, 64, C.byref(nk)))
         keys = names.value.decode().split("\n")
-        return {k: {"ms": avg[i], "per_step": cnt[i]} for i, k in enumerate(keys[: nk.value])}
+        return {k: {"ms": avg[i], "per_step": cnt[i] / n_steps} for i, k in enumerate(keys[: nk.value])}
 
     def energies(self) -> np.ndarray:
         out = np.empty((self.n_blocks, 6))

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, double2 *__res
                                                           const double *__restrict__ Vp, const double2 *__restrict__ php,
                                                           const double *__restrict__ Hp, double *__restrict__ ce_part,
                                                           int ce_tiles, int ce_n, const double2 *__restrict__ tabE,
-                                                          const int *status) {
+                                                          const int *status, const double2 *__restrict__ tabP) {
   if (status && *status) return;
   __shared__ double Vs[MAXN * MAXN];
   __shared__ double Hd[MAXN], Ho[MAXN];
@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, double2 *__res
       const BlockDesc bd = blocks[gr.block_lo + o];
       addr[o] = (int64_t)(bd.slab0 + (gr.l - bd.omega)) * g.npt + pt;
       x[o] = active ? psi_j[addr[o]] : make_double2(0.0, 0.0);
+      if (tabP && active) x[o] = cmul(x[o], ldg2(tabP + (int64_t)gr.l * g.npt + pt));
     }
   }
   if (ce_part) {
@@ -128,12 +129,13 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, double2 *__res
 
 void launch_coriolis(cudaStream_t s, const Grid &g, double2 *psi_j, const BlockDesc *blocks,
                      const CoriolisGroup *groups, int n_groups, int max_n, const double *V, const double2 *ph,
-                     const double *H, double *ce_part, int ce_tiles, const double2 *tabE, const int *status) {
+                     const double *H, double *ce_part, int ce_tiles, const double2 *tabE, const int *status,
+                     const double2 *tabP) {
   if (n_groups == 0) return;
   dim3 grid((unsigned)coriolis_tiles(g), (unsigned)n_groups);
 #define QD_COR(M)                                                                                        \
   k_coriolis<M><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, V, ph, H, ce_part, ce_tiles, max_n, \
-                                             tabE, status)
+                                             tabE, status, tabP)
   if (max_n <= 2) QD_COR(2);
   else if (max_n <= 4) QD_COR(4);
   else if (max_n <= 8) QD_COR(8);

@@ -144,6 +144,17 @@ __device__ inline void fft_run(typename CT<R>::T *buf, const Radices &rd, int nr
   }
 }
 
+// rotation by 2*alpha from (t, s) = (-tan(alpha/2), sin(alpha)): two
+// three-shear rotations, each of determinant exactly 1 in any rounding
+__device__ inline void lift2(float &x, float &y, float2 ts) {
+  x = fmaf(ts.x, y, x);
+  y = fmaf(ts.y, x, y);
+  x = fmaf(ts.x, y, x);
+  x = fmaf(ts.x, y, x);
+  y = fmaf(ts.y, x, y);
+  x = fmaf(ts.x, y, x);
+}
+
 template <typename R> __device__ inline typename CT<R>::T from_d(double2 v) {
   return CT<R>::make((R)v.x, (R)v.y);
 }
@@ -159,7 +170,8 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ 
                                                           const SlabDesc *__restrict__ slabs,
                                                           const double2 *__restrict__ tabE,
                                                           double *__restrict__ re_part, int re_tiles,
-                                                          const int *status) {
+                                                          const int *status, const float2 *__restrict__ liftR,
+                                                          const float2 *__restrict__ liftr, float fscale) {
   if (status && *status) return;
   using C = typename CT<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -168,21 +180,60 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ 
   const int N = rd.n;
   const int64_t row0 = (int64_t)blockIdx.x * nrows;
   const int n = nrows * N;
+  // FP32 path: the rotational phase as separable three-shear rotations,
+  // before the forward transform or after the inverse one
+  const bool lift = std::is_same<R, float>::value && liftR != nullptr;
   for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
     const int64_t grow = row0 + e / N;
-    buf[e] = grow < n_rows_total ? from_d<R>(psi[grow * N + (e % N)]) : CT<R>::make(0, 0);
+    C v = grow < n_rows_total ? from_d<R>(psi[grow * N + (e % N)]) : CT<R>::make(0, 0);
+    if (lift && !inv && grow < n_rows_total) {
+      const int l = slabs[grow / g.n2].l, i = e % N, j = (int)(grow % g.n2);
+      float x = (float)v.x, y = (float)v.y;
+      lift2(x, y, __ldg(liftR + (int64_t)l * g.n1 + i));
+      lift2(x, y, __ldg(liftr + (int64_t)l * g.n2 + j));
+      v.x = x;
+      v.y = y;
+    }
+    buf[e] = v;
   }
   __syncthreads();
   fft_run<R, false>(buf, rd, nrows, N, 1, tw, inv != 0);
   double re = 0.0;
+  float ref = 0.0f;
   for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
     const int64_t grow = row0 + e / N;
     if (grow >= n_rows_total) continue;
-    double2 v = to_d(buf[e]);
-    if (scale != 1.0) { v.x *= scale; v.y *= scale; }
     const int i = e % N;
     const int64_t sl = grow / g.n2;
     const int j = (int)(grow % g.n2);
+    if (std::is_same<R, float>::value && inv) {
+      float x = (float)buf[e].x, y = (float)buf[e].y;
+      double2 v;
+      if (fscale != 0.0f) {   // exact FP32 scale (power of two)
+        x *= fscale;
+        y *= fscale;
+      }
+      const int l = slabs[sl].l;
+      if (lift) {
+        lift2(x, y, __ldg(liftR + (int64_t)l * g.n1 + i));
+        lift2(x, y, __ldg(liftr + (int64_t)l * g.n2 + j));
+      }
+      if (fscale != 0.0f) {
+        v = make_double2((double)x, (double)y);
+      } else {
+        v = make_double2((double)x * scale, (double)y * scale);
+      }
+      if (re_part) {
+        const float Rr = (float)(g.left1 + i * g.dr1), rr = (float)(g.left2 + j * g.dr2);
+        const float I = 1.0f / (2.0f * (float)g.m1 * Rr * Rr) + 1.0f / (2.0f * (float)g.m2 * rr * rr);
+        const float s2 = fscale != 0.0f ? 1.0f : (float)(scale * scale);
+        ref = fmaf((float)l * (float)(l + 1) * I * s2, x * x + y * y, ref);
+      }
+      psi[grow * N + i] = v;
+      continue;
+    }
+    double2 v = to_d(buf[e]);
+    if (scale != 1.0) { v.x *= scale; v.y *= scale; }
     if (tabE) {
       const int l = slabs[sl].l;
       v = cmul(v, ldg2(tabE + (int64_t)l * g.npt + (int64_t)j * g.n1 + i));
@@ -196,7 +247,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ 
     psi[grow * N + i] = v;
   }
   if (re_part) {
-    re = block_sum(re, red);
+    re = block_sum(re + (double)ref, red);
     if (threadIdx.x == 0) {
       const int64_t sl = row0 / g.n2;
       const int tile = (int)((row0 % g.n2) / nrows);
@@ -212,7 +263,9 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_cols(double2 *__restrict__ 
                                                           const double2 *__restrict__ tab_kin,
                                                           const double *__restrict__ T1, const double *__restrict__ T2,
                                                           double *__restrict__ ke_part, int ke_tiles,
-                                                          const int *status) {
+                                                          const int *status, const float2 *__restrict__ kinR,
+                                                          const float2 *__restrict__ kinr, const float *__restrict__ T1f,
+                                                          const float *__restrict__ T2f) {
   if (status && *status) return;
   using C = typename CT<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -232,13 +285,24 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_cols(double2 *__restrict__ 
   __syncthreads();
   fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, false);
   double ke = 0.0;
+  float kef = 0.0f;
   for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
     const int t = e / ncols, c = e % ncols;
+    if (std::is_same<R, float>::value && kinR) {
+      float x = (float)buf[e].x, y = (float)buf[e].y;
+      lift2(x, y, __ldg(kinR + i0 + c));
+      lift2(x, y, __ldg(kinr + t));
+      kef = fmaf(__ldg(T1f + i0 + c) + __ldg(T2f + t), x * x + y * y, kef);
+      buf[e].x = x;
+      buf[e].y = y;
+      continue;
+    }
     double2 v = to_d(buf[e]);
     v = cmul(v, ldg2(tab_kin + (int64_t)t * g.n1 + i0 + c));
     ke += (__ldg(T1 + i0 + c) + __ldg(T2 + t)) * (v.x * v.x + v.y * v.y);
     buf[e] = from_d<R>(v);
   }
+  ke += (double)kef;
   __syncthreads();
   fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, true);
   for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
@@ -316,7 +380,7 @@ template <typename R>
 static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j,
                                  const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1,
                                  const double *T2, double *ke_part, const double2 *tabE, double *re_part,
-                                 const int *status) {
+                                 const int *status, const FFTLift *lf) {
   using C = typename CT<R>::T;
   Radices r1{p.n1, p.nst1, {}}, r2{p.n2, p.nst2, {}};
   for (int q = 0; q < p.nst1; q++) r1.rad[q] = p.rad1[q];
@@ -327,28 +391,35 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
   const size_t sm_rows = (size_t)p.rows_per_cta * p.n1 * sizeof(C);
   const size_t sm_cols = (size_t)p.cols_per_cta * p.n2 * sizeof(C);
   const unsigned nrow_ctas = (unsigned)(rows / p.rows_per_cta);
+  const double scale = 1.0 / ((double)g.n1 * g.n2);
+  const bool pow2 = ((g.n1 * g.n2) & (g.n1 * g.n2 - 1)) == 0;
+  const float fscale = pow2 ? (float)scale : 0.0f;
   k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 0, g, 1.0, slabs,
-                                                        nullptr, nullptr, 0, status);
+                                                        nullptr, nullptr, 0, status, lf ? lf->proR : nullptr,
+                                                        lf ? lf->pror : nullptr, 0.0f);
   prof_mark(s, "fft_rows_forward");
   const unsigned ncol_ctas = (unsigned)(n_slabs * (p.n1 / p.cols_per_cta));
   k_fft_cols<R><<<ncol_ctas, FFT_THREADS, sm_cols, s>>>(psi_j, r2, p.cols_per_cta, g, tw2, tab_kin, T1, T2, ke_part,
-                                                        fft_col_tiles(p), status);
+                                                        fft_col_tiles(p), status, lf ? lf->kinR : nullptr,
+                                                        lf ? lf->kinr : nullptr, lf ? lf->T1f : nullptr,
+                                                        lf ? lf->T2f : nullptr);
   prof_mark(s, "fft_cols_kinetic");
-  k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 1, g,
-                                                        1.0 / ((double)g.n1 * g.n2), slabs, tabE, re_part,
-                                                        fft_row_tiles(p), status);
+  k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 1, g, scale, slabs,
+                                                        tabE, re_part, fft_row_tiles(p), status,
+                                                        lf ? lf->epiR : nullptr, lf ? lf->epir : nullptr, fscale);
   prof_mark(s, "fft_rows_inverse");
 }
 
 void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, int precision, double2 *psi_j,
                         const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1, const double *T2,
                         double *ke_part, const double2 *tabE, const double *, const double *, double *re_part,
-                        const int *status) {
+                        const int *status, const FFTLift *lift) {
   if (n_slabs == 0) return;
   if (precision == QD_PRECISION_MIXED)
-    launch_fft_kinetic_t<float>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status);
+    launch_fft_kinetic_t<float>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status, lift);
   else
-    launch_fft_kinetic_t<double>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status);
+    launch_fft_kinetic_t<double>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status,
+                                 nullptr);
 }
 
 }  // namespace qd

@@ -124,6 +124,81 @@ void launch_build_half_v(cudaStream_t s, const Grid &g, const FluxConfig &f, con
   k_build_half_v<<<grid_for(n, 256), 256, 0, s>>>(g, f.n_grad, f.n_ds, pot, dt, half_v);
 }
 
+// ------------------------------------------------------- lifting tables
+// Multiplication by exp(i a) is a rotation by a.  For the FP32 path it is
+// applied as two rotations by a/2, each the three shears x += t y, y += s x,
+// x += t y with t = -tan(a/4), s = sin(a/2) (|a/2| <= pi/2 after reducing a
+// to (-pi, pi], so |t| <= 1).  Each shear has determinant exactly 1 whatever
+// the rounding of t and s, so a factor applied every step cannot make the
+// norm grow or decay systematically (a rounded e^{ia} in FP32 has
+// |e^{ia}| = 1 +- 6e-8, which compounds over 10^4 steps).
+__device__ inline float2 lift_coeffs(double a) {
+  const double r = remainder(a, 2.0 * M_PI);
+  const double h = 0.5 * r;
+  return make_float2((float)(-tan(0.5 * h)), (float)sin(h));
+}
+
+__global__ void k_build_lift_theta(const double *__restrict__ pot, int64_t n, double dt, float2 *__restrict__ out) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    out[q] = lift_coeffs(-dt * pot[q]);
+}
+
+void launch_build_lift_theta(cudaStream_t s, const Grid &g, const double *pot, double dt, float2 *out) {
+  const int64_t n = g.npt * g.nth;
+  k_build_lift_theta<<<grid_for(n, 256), 256, 0, s>>>(pot, n, dt, out);
+}
+
+__global__ void k_build_lift_rot(int n, int l_max, double left, double dr, double mass, double dt,
+                                 float2 *__restrict__ out) {
+  const int64_t tot = (int64_t)(l_max + 1) * n;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % n), l = (int)(q / n);
+    const double x = left + i * dr;
+    out[q] = lift_coeffs(-dt * (double)l * (double)(l + 1) / (2.0 * mass * x * x));
+  }
+}
+
+void launch_build_lift_rot(cudaStream_t s, int n, int l_max, double left, double dr, double mass, double dt,
+                           float2 *out) {
+  k_build_lift_rot<<<grid_for((int64_t)(l_max + 1) * n, 256), 256, 0, s>>>(n, l_max, left, dr, mass, dt, out);
+}
+
+__global__ void k_build_lift_kin(int n, const double *__restrict__ T, double dt, float2 *__restrict__ out) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) out[q] = lift_coeffs(-dt * T[q]);
+}
+
+void launch_build_lift_kin(cudaStream_t s, int n, const double *T, double dt, float2 *out) {
+  k_build_lift_kin<<<(n + 255) / 256, 256, 0, s>>>(n, T, dt, out);
+}
+
+__global__ void k_build_float_tables(Grid g, const double *__restrict__ w, const double *__restrict__ pot,
+                                     const double *__restrict__ d1, const double *__restrict__ d2,
+                                     const double *__restrict__ T1, const double *__restrict__ T2, float *wf,
+                                     float *wvf, float *d1f, float *d2f, float *T1f, float *T2f) {
+  const int64_t n = g.npt * g.nth;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(q / g.npt);
+    wvf[q] = (float)(w[k] * pot[q]);
+    if (q < g.nth) wf[q] = (float)w[q];
+    if (q < g.n1) {
+      T1f[q] = (float)T1[q];
+      if (d1f) d1f[q] = (float)d1[q];
+    }
+    if (q < g.n2) {
+      T2f[q] = (float)T2[q];
+      if (d2f) d2f[q] = (float)d2[q];
+    }
+  }
+}
+
+void launch_build_float_tables(cudaStream_t s, const Grid &g, const double *w, const double *pot, const double *d1,
+                               const double *d2, const double *T1, const double *T2, float *wf, float *wvf,
+                               float *d1f, float *d2f, float *T1f, float *T2f) {
+  const int64_t n = g.npt * g.nth;
+  k_build_float_tables<<<grid_for(n, 256), 256, 0, s>>>(g, w, pot, d1, d2, T1, T2, wf, wvf, d1f, d2f, T1f, T2f);
+}
+
 // ------------------------------------------------------------ energies
 // rotational energy partials: sum l(l+1) (I1_i + I2_j) |psi|^2 per (slab, tile)
 __global__ void k_rot_energy(Grid g, const double2 *__restrict__ psi_j, const SlabDesc *__restrict__ slabs,

@@ -283,6 +283,12 @@ struct qd_session {
   int *flux_count = nullptr, *flux_slot = nullptr;
   int flux_pending = 0;
   FFTPlan fft{};
+  // mixed form: tensor-core Legendre images and FP32 three-shear tables
+  uint16_t *img_f = nullptr, *img_b = nullptr;
+  int64_t *imgoff_f = nullptr, *imgoff_b = nullptr;
+  size_t smem_f = 0, smem_b = 0;
+  float2 *vph = nullptr, *vph0 = nullptr, *lrotR = nullptr, *lrotr = nullptr, *lkinR = nullptr, *lkinr = nullptr;
+  float *wf = nullptr, *wvf = nullptr, *d1f = nullptr, *d2f = nullptr, *T1f = nullptr, *T2f = nullptr;
   int steps = 0;   // host mirror of time.steps
   int launches_per_step = 0;
   cudaGraphExec_t graph_chunk = nullptr;
@@ -364,7 +370,9 @@ qd_session::~qd_session() {
   void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
                   tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, d_pgroup0,
                   part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
-                  flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot};
+                  flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
+                  img_f, img_b, imgoff_f, imgoff_b, vph, vph0, lrotR, lrotr, lkinR, lkinr, wf, wvf, d1f, d2f,
+                  T1f, T2f};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   fft_plan_free(fft);
@@ -410,8 +418,51 @@ static EnergyParts energy_parts(qd_session *s, bool mod, bool ke, bool re, bool 
   return ep;
 }
 
+static void enqueue_tail(qd_session *s);
+
+// Mixed form of the same step: tensor-core Legendre contractions, FP32 FFT and
+// FP32 three-shear phases; Coriolis, energies and flux in FP64.
+static void enqueue_step_mixed(qd_session *s, bool first) {
+  cudaStream_t st = s->stream;
+  const Grid &g = s->g;
+  launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_j, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f,
+                         first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status);
+  prof_mark(st, "legendre_forward");
+  if (s->any_coupled) {
+    launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
+                    s->cor_H, nullptr, s->t_ce, s->tab_rot4, s->status, s->tab_rot4);
+    prof_mark(st, "coriolis");
+  }
+  FFTLift lf{};
+  lf.proR = s->any_coupled ? nullptr : s->lrotR;
+  lf.pror = s->any_coupled ? nullptr : s->lrotr;
+  lf.epiR = s->lrotR;
+  lf.epir = s->lrotr;
+  lf.kinR = s->lkinR;
+  lf.kinr = s->lkinr;
+  lf.T1f = s->T1f;
+  lf.T2f = s->T2f;
+  launch_fft_kinetic(st, g, s->fft, QD_PRECISION_MIXED, s->psi_j, s->d_slabs, s->n_slabs, nullptr, s->T1, s->T2,
+                     s->part_ke, nullptr, s->I1, s->I2, s->any_coupled ? nullptr : s->part_re, s->status, &lf);
+  if (s->any_coupled) {
+    launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
+                    s->cor_H, s->part_ce, s->t_ce, s->tab_rot4, s->status);
+    prof_mark(st, "coriolis_energy");
+    launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->I1, s->I2, s->part_re, s->t_re, s->status);
+    prof_mark(st, "rotational_energy");
+  }
+  launch_legendre_tc_bwd(st, g, s->psi_j, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf, s->wvf,
+                         s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status);
+  prof_mark(st, "legendre_backward");
+  enqueue_tail(s);
+}
+
 // One full time step, sequence of test_multiple_cards (cudaOpenMP2.cu:338-386).
 static void enqueue_step(qd_session *s, bool first) {
+  if (s->precision == QD_PRECISION_MIXED) {
+    enqueue_step_mixed(s, first);
+    return;
+  }
   cudaStream_t st = s->stream;
   const Grid &g = s->g;
   const double2 *tabA = first ? s->tab_v0 : s->tab_v;
@@ -442,6 +493,13 @@ static void enqueue_step(qd_session *s, bool first) {
   launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
                           s->part_modpe, s->t_modpe, s->status);
   prof_mark(st, "legendre_backward");
+  enqueue_tail(s);
+}
+
+// energies, norm guard, flux surface values, step counter
+static void enqueue_tail(qd_session *s) {
+  cudaStream_t st = s->stream;
+  const Grid &g = s->g;
   EnergyParts ep = energy_parts(s, true, true, true, s->any_coupled);
   launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                           s->max_group_n, s->energies, s->rec, s->d_step, s->rec_base, s->rec_cap, s->norm_tol,
@@ -554,22 +612,49 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     s->d1 = dupload(d0->dump1.dump, (size_t)g.n1, st);
     s->d2 = dupload(d0->dump2.dump, (size_t)g.n2, st);
   }
-  s->tab_v = dalloc<double2>((size_t)nth_pt);
-  s->tab_v0 = dalloc<double2>((size_t)nth_pt);
-  launch_build_theta_table(st, g, s->pot, s->d1, s->d2, s->dt, s->tab_v);
-  launch_build_theta_table(st, g, s->pot, s->d1, s->d2, 0.5 * s->dt, s->tab_v0);
+  const bool fp64 = s->precision == QD_PRECISION_FP64;
+  if (fp64) {
+    s->tab_v = dalloc<double2>((size_t)nth_pt);
+    s->tab_v0 = dalloc<double2>((size_t)nth_pt);
+    launch_build_theta_table(st, g, s->pot, s->d1, s->d2, s->dt, s->tab_v);
+    launch_build_theta_table(st, g, s->pot, s->d1, s->d2, 0.5 * s->dt, s->tab_v0);
+  }
   const int64_t nrot = g.npt * (g.l_max + 1);
-  bool any_uncoupled = false;
-  for (auto &ph : s->probs) any_uncoupled |= !ph.coupled;
   if (s->any_coupled) {
     s->tab_rot4 = dalloc<double2>((size_t)nrot);
     launch_build_rot_table(st, g, 0.25 * s->dt, s->tab_rot4);
-  } else {
+  } else if (fp64) {
     s->tab_rot2 = dalloc<double2>((size_t)nrot);
     launch_build_rot_table(st, g, 0.5 * s->dt, s->tab_rot2);
   }
   s->tab_kin = dalloc<double2>((size_t)g.npt);
   launch_build_kin_table(st, g, s->T1, s->T2, s->dt, s->tab_kin);
+  // FP32 tables (the mixed form; also used by mixed-precision stage calls)
+  s->wf = dalloc<float>((size_t)g.nth);
+  s->wvf = dalloc<float>((size_t)nth_pt);
+  s->T1f = dalloc<float>((size_t)g.n1);
+  s->T2f = dalloc<float>((size_t)g.n2);
+  if (s->has_mask) {
+    s->d1f = dalloc<float>((size_t)g.n1);
+    s->d2f = dalloc<float>((size_t)g.n2);
+  }
+  launch_build_float_tables(st, g, s->w, s->pot, s->d1, s->d2, s->T1, s->T2, s->wf, s->wvf, s->d1f, s->d2f, s->T1f,
+                            s->T2f);
+  if (!fp64) {
+    s->vph = dalloc<float2>((size_t)nth_pt);
+    s->vph0 = dalloc<float2>((size_t)nth_pt);
+    launch_build_lift_theta(st, g, s->pot, s->dt, s->vph);
+    launch_build_lift_theta(st, g, s->pot, 0.5 * s->dt, s->vph0);
+    const double drot = (s->any_coupled ? 0.25 : 0.5) * s->dt;
+    s->lrotR = dalloc<float2>((size_t)(g.l_max + 1) * g.n1);
+    s->lrotr = dalloc<float2>((size_t)(g.l_max + 1) * g.n2);
+    launch_build_lift_rot(st, g.n1, g.l_max, g.left1, g.dr1, g.m1, drot, s->lrotR);
+    launch_build_lift_rot(st, g.n2, g.l_max, g.left2, g.dr2, g.m2, drot, s->lrotr);
+    s->lkinR = dalloc<float2>((size_t)g.n1);
+    s->lkinr = dalloc<float2>((size_t)g.n2);
+    launch_build_lift_kin(st, g.n1, s->T1, s->dt, s->lkinR);
+    launch_build_lift_kin(st, g.n2, s->T2, s->dt, s->lkinr);
+  }
 
   // Legendre matrices: forward B = w_k P (k, n) as [k][n]; backward P as [n][k]
   std::vector<double> Bf((size_t)bmat), Bb((size_t)bmat);
@@ -587,6 +672,33 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   }
   s->Bf = dupload(Bf.data(), Bf.size(), st);
   s->Bb = dupload(Bb.data(), Bb.size(), st);
+  {
+    // tensor-core images (BF16x3 split, shared-memory layout) of both directions
+    auto r16 = [](int x) { return (x + 15) & ~15; };
+    std::vector<int64_t> of, ob;
+    int64_t tf = 0, tb = 0;
+    for (const BlockDesc &bd : s->h_blocks) {
+      of.push_back(tf);
+      tf += 3LL * r16(bd.nl) * r16(g.nth) * 2;
+      s->smem_f = std::max(s->smem_f, tc_smem_bytes(r16(g.nth), r16(bd.nl)));
+      ob.push_back(tb);
+      tb += 3LL * r16(g.nth) * r16(bd.nl) * 2;
+      s->smem_b = std::max(s->smem_b, tc_smem_bytes(r16(bd.nl), r16(g.nth)));
+    }
+    const size_t limit = 200 * 1024;
+    if (s->smem_f > limit || s->smem_b > limit) {
+      if (s->precision == QD_PRECISION_MIXED)
+        throw Error{QD_ERR_UNSUPPORTED, "mixed form: n_theta and l_max+1 above the tensor-core tile limit"};
+    } else {
+      tc_set_smem_limit(std::max(s->smem_f, s->smem_b));
+      s->imgoff_f = dupload(of.data(), of.size(), st);
+      s->imgoff_b = dupload(ob.data(), ob.size(), st);
+      s->img_f = dalloc<uint16_t>((size_t)tf / 2);
+      s->img_b = dalloc<uint16_t>((size_t)tb / 2);
+      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bf, g.nth, true, s->imgoff_f, s->img_f);
+      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bb, g.nth, false, s->imgoff_b, s->img_b);
+    }
+  }
 
   // Coriolis groups (cudaOpenMP2.cu:158-209): one per (problem, l >= omega_min)
   if (s->any_coupled) {
@@ -644,7 +756,7 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   }
 
   // energies and partials
-  s->t_modpe = legendre_bwd_part_tiles(g);
+  s->t_modpe = s->precision == QD_PRECISION_MIXED ? legendre_tc_part_tiles(g) : legendre_bwd_part_tiles(g);
   s->t_ke = fft_col_tiles(s->fft);
   s->t_re = s->any_coupled ? 16 : fft_row_tiles(s->fft);
   s->t_ce = coriolis_tiles(g);
@@ -989,12 +1101,20 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         launch_theta_phase(st, s->psi_th, tab, s->n_blocks, g.npt * g.nth, s->status);
         break;
       case QD_STAGE_FORWARD_LEGENDRE:
-        launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, nullptr,
-                                nullptr, s->status);
+        if (s->precision == QD_PRECISION_MIXED)
+          launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_j, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f, nullptr,
+                                 nullptr, nullptr, s->smem_f, s->status, s->status);
+        else
+          launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, nullptr,
+                                  nullptr, s->status);
         break;
       case QD_STAGE_BACKWARD_LEGENDRE:
-        launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
-                                s->part_modpe, s->t_modpe, s->status);
+        if (s->precision == QD_PRECISION_MIXED)
+          launch_legendre_tc_bwd(st, g, s->psi_j, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf,
+                                 s->wvf, s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status);
+        else
+          launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
+                                  s->part_modpe, s->t_modpe, s->status);
         break;
       case QD_STAGE_ROTATIONAL:
         tab = scratch_tab(g.npt * (g.l_max + 1));
@@ -1022,8 +1142,23 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       case QD_STAGE_FFT_KINETIC: {
         tab = scratch_tab(g.npt);
         launch_build_kin_table(st, g, s->T1, s->T2, dt, tab);
+        FFTLift lf{};
+        float2 *kR = nullptr, *kr = nullptr;
+        if (s->precision == QD_PRECISION_MIXED) {
+          kR = dalloc<float2>((size_t)g.n1);
+          kr = dalloc<float2>((size_t)g.n2);
+          launch_build_lift_kin(st, g.n1, s->T1, dt, kR);
+          launch_build_lift_kin(st, g.n2, s->T2, dt, kr);
+          lf.kinR = kR;
+          lf.kinr = kr;
+          lf.T1f = s->T1f;
+          lf.T2f = s->T2f;
+        }
         launch_fft_kinetic(st, g, s->fft, s->precision, s->psi_j, s->d_slabs, s->n_slabs, tab, s->T1, s->T2,
-                           s->part_ke, nullptr, s->I1, s->I2, nullptr, s->status);
+                           s->part_ke, nullptr, s->I1, s->I2, nullptr, s->status, &lf);
+        QD_CUDA(cudaStreamSynchronize(st));
+        if (kR) cudaFree(kR);
+        if (kr) cudaFree(kr);
         EnergyParts ep = energy_parts(s, false, true, false, false);
         launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                                 s->max_group_n, s->energies, nullptr, s->d_step, 0, 0, 1e300, s->status,
@@ -1148,7 +1283,7 @@ int qd_session_profile(qd_session *s, int32_t n_steps, char *names, size_t names
     std::string joined;
     for (size_t k = 0; k < order.size(); k++) {
       avg_ms[k] = tot[k] / cnt[k];
-      launches_per_step[k] = cnt[k] / n_steps;
+      launches_per_step[k] = cnt[k];
       joined += order[k];
       if (k + 1 < order.size()) joined += "\n";
     }

@@ -118,6 +118,14 @@ struct FFTPlan {
   int rows_per_cta;
   int cols_per_cta;
 };
+// FP32 three-shear phase tables of the mixed form (float2 (t, s) per entry,
+// see lift tables below); null entries are skipped.
+struct FFTLift {
+  const float2 *proR, *pror;   // [l][n1], [l][n2]: rotational phase before the forward transform
+  const float2 *epiR, *epir;   // after the inverse transform
+  const float2 *kinR, *kinr;   // [n1], [n2]: kinetic phase
+  const float *T1f, *T2f;      // kinetic energy tables in FP32
+};
 bool fft_factor(int n, int *rad, int *nst);
 void fft_plan_init(FFTPlan &p, int n1, int n2);
 void fft_plan_free(FFTPlan &p);
@@ -127,7 +135,7 @@ void fft_plan_free(FFTPlan &p);
 void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, int precision, double2 *psi_j,
                         const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1,
                         const double *T2, double *ke_part, const double2 *tabE, const double *I1,
-                        const double *I2, double *re_part, const int *status);
+                        const double *I2, double *re_part, const int *status, const FFTLift *lift = nullptr);
 int fft_col_tiles(const FFTPlan &p);
 int fft_row_tiles(const FFTPlan &p);
 
@@ -142,7 +150,7 @@ void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, cons
 void launch_coriolis(cudaStream_t s, const Grid &g, double2 *psi_j, const BlockDesc *blocks,
                      const CoriolisGroup *groups, int n_groups, int max_n, const double *V,
                      const double2 *ph, const double *H, double *ce_part, int ce_tiles,
-                     const double2 *tabE, const int *status);
+                     const double2 *tabE, const int *status, const double2 *tabP = nullptr);
 void launch_build_coriolis_phase(cudaStream_t s, const Grid &g, const CoriolisGroup *groups, int n_groups,
                                  int max_n, const double *e, double dt, double2 *ph);
 int coriolis_tiles(const Grid &g);
@@ -178,6 +186,36 @@ void launch_build_theta_table(cudaStream_t s, const Grid &g, const double *pot, 
 void launch_build_rot_table(cudaStream_t s, const Grid &g, double dt, double2 *tab);
 void launch_build_kin_table(cudaStream_t s, const Grid &g, const double *T1, const double *T2, double dt,
                             double2 *tab);
+// Lifting tables: entry = (-tan(a/4), sin(a/2)) of the rotation angle a =
+// -scale * f (reduced to (-pi, pi]), applied as two half-angle three-shear
+// rotations.
+//   theta:  f = V[k][p] (with scale dt)                      -> [nth][npt]
+//   rot:    f = l(l+1)/(2 m R^2) per coordinate              -> [l_max+1][n]
+//   kin:    f = T[i]                                          -> [n]
+void launch_build_lift_theta(cudaStream_t s, const Grid &g, const double *pot, double dt, float2 *out);
+void launch_build_lift_rot(cudaStream_t s, int n, int l_max, double left, double dr, double mass, double dt,
+                           float2 *out);
+void launch_build_lift_kin(cudaStream_t s, int n, const double *T, double dt, float2 *out);
+void launch_build_float_tables(cudaStream_t s, const Grid &g, const double *w, const double *pot, const double *d1,
+                               const double *d2, const double *T1, const double *T2, float *wf, float *wvf,
+                               float *d1f, float *d2f, float *T1f, float *T2f);
+
+// tcgen05 BF16x3 Legendre contraction
+struct TcArgs;
+size_t tc_smem_bytes(int Kp, int Np);
+void tc_set_smem_limit(size_t bytes);
+void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,
+                            bool fwd, const int64_t *img_off, uint16_t *img);
+void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, double2 *psi_j,
+                            const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
+                            const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
+                            int *status_w);
+void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j, double2 *psi_th,
+                            const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
+                            const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
+                            const int *status, int *status_w);
+int legendre_tc_part_tiles(const Grid &g);
+
 void launch_build_half_v(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
                          double2 *half_v);
 

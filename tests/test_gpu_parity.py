@@ -209,3 +209,53 @@ def test_mixed_precision_close_to_fp64(qd, oracle, gpu):
     phys = np.abs(crp) <= 2.0
     assert phys.sum() >= 4
     assert np.max(np.abs(d["CRP"]["CRP"] - crp)[phys]) <= 1e-4
+
+
+@pytest.mark.parametrize("case", [dict(J=0, n1=16, n2=8, n_theta=6, l_max=5),
+                                  dict(J=2, parity=0, n1=32, n2=16, n_theta=24, l_max=23),
+                                  dict(J=3, parity=1, n1=24, n2=12, n_theta=40, l_max=37)])
+def test_mixed_stages_match_oracle(qd, oracle, gpu, case):
+    """tcgen05 BF16x3 Legendre contractions and the FP32 FFT: FP32-level agreement (rel <= 3e-6)."""
+    cfg, d, dref = make(qd, **case)
+    d["options"]["precision"] = 1
+    o = oracle.Oracle(dref)
+    rng = np.random.default_rng(11)
+    _random_state(o, rng)
+    with qd.Session(d) as s:
+        for b in range(len(o.psi)):
+            s.set_psi("theta", b, o.psi[b])
+        o.forward_legendre_transform()
+        s.apply("forward_legendre")
+        for b in range(len(o.psi)):
+            assert rel(s.get_psi("j", b), o.lpsi[b]) < 3e-6
+            s.set_psi("j", b, o.lpsi[b])   # restart the next stage from the exact state
+        o.forward_fft(); o.evolution_with_kinetic(cfg.dt); ke = o.kinetic_energy(); o.backward_fft()
+        s.apply("fft_kinetic", cfg.dt)
+        for b in range(len(o.psi)):
+            assert rel(s.get_psi("j", b), o.lpsi[b]) < 3e-6
+            s.set_psi("j", b, o.lpsi[b])
+        np.testing.assert_allclose(s.energies()[:, 2], ke, rtol=1e-5)
+        o.backward_legendre_transform()
+        s.apply("backward_legendre")
+        s.apply("energies")
+        for b in range(len(o.psi)):
+            assert rel(s.get_psi("theta", b), o.psi[b]) < 3e-6
+        np.testing.assert_allclose(s.energies()[:, 0], o.module(), rtol=1e-5)
+        np.testing.assert_allclose(s.energies()[:, 1], o.potential_energy(), rtol=1e-5, atol=1e-12)
+
+
+def test_mixed_production_grid_tracks_fp64(qd, gpu):
+    """256x128x96: 40 steps of the mixed form stay within 1e-5 of the FP64 form; norm drift <= 1e-6."""
+    cfg = qd.inputs.CONFIGS["fh2_j0_256x128x96"]
+    out = {}
+    for prec in (0, 1):
+        d = qd.inputs.build_fh2data(cfg)
+        d["time"]["total_steps"] = 40
+        d["options"]["precision"] = prec
+        d["options"]["energies"] = np.zeros((40, 1, 6))
+        qd.cudaOpenMPEvolution(d)
+        out[prec] = d
+    a, b = out[1]["OmegaStates"]["wave_packets"], out[0]["OmegaStates"]["wave_packets"]
+    assert rel(a, b) < 1e-5
+    ma, mb = out[1]["options"]["energies"][:, 0, 0], out[0]["options"]["energies"][:, 0, 0]
+    assert np.max(np.abs(ma - mb)) < 1e-6
