@@ -227,6 +227,45 @@ def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 1):
                       f"{WORKLOAD} workload after {warm} warm-up step"}
 
 
+def accuracy(qd, total: int, checkpoints=(10, 40, 160, 640, 2560, 10240, 20000)):
+    """Mixed vs FP64 form on the production workload: relative |dpsi|_2, norm
+    drift and P(E) after ``total`` steps (both forms on this GPU)."""
+    cfg = qd.inputs.CONFIGS[WORKLOAD]
+    ds, ss = {}, {}
+    for prec in (0, 1):
+        d = qd.inputs.build_fh2data(cfg)
+        d["options"]["precision"] = prec
+        ds[prec] = d
+        ss[prec] = qd.Session(d)
+    rows = []
+    done = 0
+    t0 = time.perf_counter()
+    for cp in sorted(set([c for c in checkpoints if c <= total] + [total])):
+        for prec in (0, 1):
+            ss[prec].run(cp - done)
+            ss[prec].synchronize()
+        done = cp
+        a, b = ss[1].get_psi("theta", 0), ss[0].get_psi("theta", 0)
+        ea, eb = ss[1].energies()[0], ss[0].energies()[0]
+        rows.append({"step": cp, "rel_dpsi": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                     "module_fp64": float(eb[0]), "module_mixed": float(ea[0]),
+                     "dmodule": float(ea[0] - eb[0]), "dE_total": float(ea[5] - eb[5])})
+        print(json.dumps(rows[-1]), flush=True)
+    for prec in (0, 1):
+        ss[prec].download()
+        ss[prec].close()
+    Pm, Pf = ds[1]["CRP"]["CRP"], ds[0]["CRP"]["CRP"]
+    ecoll = ds[0]["CRP"]["energies"] - ds[0]["CRP"]["eDiatomic"]
+    eta = ds[0]["CRP"]["eta_sq"]
+    win = eta >= 1e-4 * eta.max()     # energies the initial packet actually carries
+    return {"workload": WORKLOAD, "steps": total, "checkpoints": rows,
+            "p_window_ecoll": [float(ecoll[win].min()), float(ecoll[win].max())],
+            "max_abs_dP_window": float(np.max(np.abs(Pm - Pf)[win])),
+            "max_abs_dP": float(np.max(np.abs(Pm - Pf))), "max_P_fp64": float(np.max(np.abs(Pf))),
+            "P_fp64_sample": [float(x) for x in Pf[::40]], "P_mixed_sample": [float(x) for x in Pm[::40]],
+            "ecoll_sample": [float(x) for x in ecoll[::40]], "seconds": time.perf_counter() - t0}
+
+
 def reference_arm(args, world, rank):
     if rank != 0:
         return
@@ -255,6 +294,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accuracy", type=int, default=0,
+                    help="run the mixed-vs-FP64 accuracy study for this many steps instead of the benchmark")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -268,6 +309,9 @@ def main():
         torch.distributed.init_process_group("nccl")
     qd = entry.load_package()
     qd.load_library()
+    if args.accuracy:
+        print(json.dumps({"accuracy": accuracy(qd, args.accuracy)}), flush=True)
+        return
     gpu_index = local
     if os.environ.get("CUDA_VISIBLE_DEVICES"):
         vis = os.environ["CUDA_VISIBLE_DEVICES"].split(",")

@@ -102,9 +102,28 @@ __device__ inline void fft_stage(typename CT<R>::T *buf, int N, int nrows, int r
       if (Ns > 1) {
 #pragma unroll
         for (int r = 1; r < RAD; r++) {
-          C w = tw[r * k * tstep];
-          if (inv) w.y = -w.y;
-          v[q][r] = cmulg(v[q][r], w);
+          const int idx = r * k * tstep;
+          C w = tw[idx];
+          if constexpr (std::is_same<R, float>::value) {
+            // twiddle as a three-shear rotation (determinant exactly 1): the
+            // table holds (-tan(b/2), sin(b)) of b = the twiddle angle shifted
+            // by pi where |angle| > pi/2 (then the vector is negated first)
+            const bool flip = 4 * idx > N && 4 * idx < 3 * N;
+            const float tt = inv ? -w.x : w.x, ss = inv ? -w.y : w.y;
+            float x = v[q][r].x, y = v[q][r].y;
+            if (flip) {
+              x = -x;
+              y = -y;
+            }
+            x = fmaf(tt, y, x);
+            y = fmaf(ss, x, y);
+            x = fmaf(tt, y, x);
+            v[q][r].x = x;
+            v[q][r].y = y;
+          } else {
+            if (inv) w.y = -w.y;
+            v[q][r] = cmulg(v[q][r], w);
+          }
         }
       }
       dft<R, RAD>(v[q], inv);
@@ -342,13 +361,18 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
   p.rows_per_cta = largest_divisor_at_most(n2, std::max(1, FFT_THREADS * MAXV / n1));
   p.rows_per_cta = std::min(p.rows_per_cta, largest_divisor_at_most(n2, 64));
   p.cols_per_cta = largest_divisor_at_most(n1, std::min(32, std::max(1, FFT_THREADS * MAXV / n2)));
+  // FP64 twiddles exp(-2 pi i t/n); FP32 twiddles as three-shear rotation
+  // coefficients (-tan(b/2), sin(b)) with b the angle reduced to [-pi/2, pi/2]
+  // by a shift of pi where 4t lies strictly between n and 3n
   auto make = [](int n, double2 **d, float2 **f) {
     std::vector<double2> hd(n);
     std::vector<float2> hf(n);
     for (int t = 0; t < n; t++) {
       const double a = -2.0 * M_PI * (double)t / (double)n;
       hd[t] = make_double2(std::cos(a), std::sin(a));
-      hf[t] = make_float2((float)hd[t].x, (float)hd[t].y);
+      double b = std::remainder(a, 2.0 * M_PI);
+      if (4LL * t > n && 4LL * t < 3LL * n) b += b > 0 ? -M_PI : M_PI;
+      hf[t] = make_float2((float)(-std::tan(0.5 * b)), (float)std::sin(b));
     }
     QD_CUDA(cudaMalloc(d, n * sizeof(double2)));
     QD_CUDA(cudaMalloc(f, n * sizeof(float2)));

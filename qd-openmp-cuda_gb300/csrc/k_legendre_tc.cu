@@ -6,18 +6,27 @@
 // m = 2*point + {re, im}, so C[m][n] = sum_k A[m][k] B[n][k] with B the real
 // (weighted) associated-Legendre matrix.
 //
-// Precision: every FP32 value x is split into three BF16 terms
-// x = a0 + a1 + a2 (a1 = bf16(x - a0), a2 = bf16(x - a0 - a1)); the products
-// a_i b_j with i + j <= 2 (six of them) are accumulated in one FP32 TMEM
-// accumulator, which reproduces an FP32-accurate product.  B (constant per
-// Omega block) is split once at set-up, in FP64, into its shared-memory image.
+// Precision (3-term BF16 split, exact accumulation): each row m of A is scaled
+// by a power of two s_m >= max_k |A[m][k]| and each column n of B by t_n, so
+// |a|, |b| <= 1.  Three integer slices are taken by round-to-nearest,
+//   i0 = rn(256 a), i1 = rn(256 (256 a - i0)), i2 = rn(256 (... - i1)),
+// with |i0| <= 256, |i1|, |i2| <= 128: every slice is an integer that BF16
+// holds exactly.  Products of slices are grouped by order,
+//   D0 = sum_k i0 j0,  D1 = sum_k (i0 j1 + i1 j0),  D2 = sum_k (i0 j2 + i1 j1 + i2 j0),
+// each an integer below 96 * 81920 < 2^24 for K <= 192, so the three FP32
+// TMEM accumulators hold them exactly whatever the tensor core's internal
+// rounding.  C = s_m t_n 2^-16 (D0 + 2^-8 (D1 + 2^-8 D2)) is then formed with
+// two round-to-nearest FP32 operations.  (A single accumulator of all six
+// products loses about 2e-6 of the norm per forward+backward pair to biased
+// accumulation rounding; the exact form has no such bias.)
 //
 // Per CTA: 64 points (M = 128 real rows) x all N columns.  Four warps stage
-// the A tile (FP64 load -> FP32 -> forward: absorbing mask and exp(-iV dt) as
-// an exactly area-preserving three-shear rotation -> BF16x3 split) into the
-// SWIZZLE_NONE K-major canonical layout; one thread issues the tcgen05.mma
-// chain; the commit arrives on an mbarrier; the four warps read their 32 TMEM
-// lanes back (tcgen05.ld 32x32b), convert to FP64 and store.  The backward
+// the A tile (FP64 load -> FP32; forward: absorbing mask and exp(-iV dt) as an
+// exactly area-preserving three-shear rotation) into an FP32 buffer; each
+// thread then scales and slices one row into the SWIZZLE_NONE K-major
+// canonical layout; one thread issues the tcgen05.mma chain; the commit
+// arrives on an mbarrier; each thread reads its own row (TMEM lane) back with
+// tcgen05.ld 32x32b, recombines, converts to FP64 and stores.  The backward
 // epilogue also reduces the module and potential energy.
 #include <cuda_bf16.h>
 
@@ -128,31 +137,62 @@ __constant__ int c_pair_b[6] = {0, 1, 0, 2, 1, 0};
 // byte size of the B image of one block: 3 terms x Npad x Kpad BF16
 __host__ __device__ inline int64_t tc_bimg_bytes(int Np, int Kp) { return 3LL * Np * Kp * 2; }
 
+// TMEM columns for three Np-wide accumulators (power of two >= 32)
+__host__ __device__ inline uint32_t tc_tmem_cols(int Np) {
+  const int need = 3 * Np;
+  return need <= 32 ? 32u : need <= 64 ? 64u : need <= 128 ? 128u : need <= 256 ? 256u : 512u;
+}
+
 // ---------------------------------------------------------------------------
 // B images: element (n, k) of term t at t*Np*Kp*2 + (n/8)*SBO + (k/8)*128 +
 // (n%8)*16 + (k%8)*2 bytes with SBO = Kp/8*128 (SWIZZLE_NONE, K-major).
 // fwd: B(n = l, k = theta) = w_k P_l(x_k) = Bf[k*nl + n]
 // bwd: B(n = theta, k = l) = P_l(x_n)     = Bb[k*nth + n]
+// One CTA per (block, column n): the column scale t_n = 2^e (smallest power
+// of two >= max_k |B(n, k)|) and the three integer slices of B(n, k)/t_n.
 __global__ void k_build_tc_bimage(const BlockDesc *__restrict__ blocks, const double *__restrict__ Bsrc, int nth,
-                                  int fwd, const int64_t *__restrict__ img_off, uint16_t *__restrict__ img) {
+                                  int fwd, const int64_t *__restrict__ img_off, uint16_t *__restrict__ img,
+                                  float *__restrict__ bscale) {
+  __shared__ double red[32];
   const BlockDesc bd = blocks[blockIdx.y];
   const int Kv = fwd ? nth : bd.nl, Nv = fwd ? bd.nl : nth;
   const int Kp = (Kv + 15) & ~15, Np = (Nv + 15) & ~15;
+  const int n = blockIdx.x;
+  if (n >= Np) return;
   uint16_t *out = img + img_off[blockIdx.y] / 2;
   const int SBOe = Kp / 8 * 64;   // in elements
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Np * Kp; q += gridDim.x * blockDim.x) {
-    const int n = q / Kp, k = q % Kp;
-    double b = 0.0;
-    if (n < Nv && k < Kv) b = fwd ? Bsrc[bd.bmat0 + (int64_t)k * bd.nl + n] : Bsrc[bd.bmat0 + (int64_t)k * nth + n];
-    const __nv_bfloat16 b0 = __double2bfloat16(b);
-    const double r1 = b - (double)__bfloat162float(b0);
-    const __nv_bfloat16 b1 = __double2bfloat16(r1);
-    const double r2 = r1 - (double)__bfloat162float(b1);
-    const __nv_bfloat16 b2 = __double2bfloat16(r2);
-    const int64_t e = (int64_t)(n / 8) * SBOe + (k / 8) * 64 + (n % 8) * 8 + (k % 8);
-    out[e] = __bfloat16_as_ushort(b0);
-    out[(int64_t)Np * Kp + e] = __bfloat16_as_ushort(b1);
-    out[2LL * Np * Kp + e] = __bfloat16_as_ushort(b2);
+  auto val = [&](int k) -> double {
+    if (n >= Nv || k >= Kv) return 0.0;
+    return fwd ? Bsrc[bd.bmat0 + (int64_t)k * bd.nl + n] : Bsrc[bd.bmat0 + (int64_t)k * nth + n];
+  };
+  // block-wide max |B(n, :)| (max via -sum of negated maxima is not needed: use a
+  // shared reduction with fmax)
+  double mx = 0.0;
+  for (int k = threadIdx.x; k < Kp; k += blockDim.x) mx = fmax(mx, fabs(val(k)));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) m = fmax(m, red[w]);
+    red[0] = m;
+  }
+  __syncthreads();
+  mx = red[0];
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);          // mx = f 2^e, f in [0.5, 1)  ->  |B| / 2^e < 1
+  const double inv = ldexp(1.0, -e);
+  if (threadIdx.x == 0) bscale[(int64_t)blockIdx.y * 256 + n] = (float)ldexp(1.0, e);
+  for (int k = threadIdx.x; k < Kp; k += blockDim.x) {
+    const double b = val(k) * inv * 256.0;
+    const double i0 = rint(b);
+    const double r1 = (b - i0) * 256.0;
+    const double i1 = rint(r1);
+    const double i2 = rint((r1 - i1) * 256.0);
+    const int64_t el = (int64_t)(n / 8) * SBOe + (k / 8) * 64 + (n % 8) * 8 + (k % 8);
+    out[el] = __bfloat16_as_ushort(__double2bfloat16(i0));
+    out[(int64_t)Np * Kp + el] = __bfloat16_as_ushort(__double2bfloat16(i1));
+    out[2LL * Np * Kp + el] = __bfloat16_as_ushort(__double2bfloat16(i2));
   }
 }
 
@@ -163,6 +203,7 @@ struct TcArgs {
   const BlockDesc *blocks;
   const uint16_t *bimg;      // B images
   const int64_t *bimg_off;   // per block byte offset
+  const float *bscale;       // per block (x256) column scales t_n
   const float2 *vph;         // fwd: half-angle shears of exp(-iV dt) [k][p] (may be null)
   const float *d1, *d2;      // fwd: absorbing masks (may be null)
   const float *w;            // bwd: quadrature weights
@@ -198,11 +239,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
   const uint32_t SBO_A = (uint32_t)(Kp / 8 * 128), SBO_B = SBO_A;
   const uint32_t A_TERM = 16u * SBO_A;                 // 128 rows
   const uint32_t B_TERM = (uint32_t)(Np / 8) * SBO_B;
+  const int LDF = Kp + 1;                              // padded FP32 staging row
   unsigned char *sA = smem;
   unsigned char *sB = smem + 3 * A_TERM;
+  float *sF = reinterpret_cast<float *>(sB + 3 * B_TERM);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t p0 = (int64_t)blockIdx.x * TC_POINTS;
-  const uint32_t ncols = Np <= 32 ? 32 : (Np <= 64 ? 64 : (Np <= 128 ? 128 : 256));
+  const uint32_t ncols = tc_tmem_cols(Np);
 
   if (warp == 0) tmem_alloc(smem_u32(&tmem_base_s), ncols);
   if (tid == 0) {
@@ -217,52 +260,70 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
     const int n16 = (int)(tc_bimg_bytes(Np, Kp) / 16);
     for (int q = tid; q < n16; q += TC_THREADS) dst[q] = __ldg(src + q);
   }
-  // ---- A tile: (point, group of 8 k) items
+  // ---- phase 1: A tile as FP32 rows (row 2p = re, 2p+1 = im), phases applied
   {
     const double2 *A = FWD ? P.A + (int64_t)blockIdx.y * g.nth * g.npt : P.A + (int64_t)bd.slab0 * g.npt;
-    const int kgs = Kp / 8;
-    for (int it = tid; it < TC_POINTS * kgs; it += TC_THREADS) {
-      const int pl = it % TC_POINTS, kg = it / TC_POINTS;
+    for (int it = tid; it < TC_POINTS * Kp; it += TC_THREADS) {
+      const int pl = it % TC_POINTS, k = it / TC_POINTS;
       const int64_t p = p0 + pl;
-      uint32_t wre[3][4], wim[3][4];
-      float msk = 1.0f;
-      if (FWD && P.d1 && p < g.npt) msk = P.d1[p % g.n1] * P.d2[p / g.n1];
-#pragma unroll
-      for (int e = 0; e < 8; e++) {
-        const int k = kg * 8 + e;
-        float x = 0.0f, y = 0.0f;
-        if (k < Kv && p < g.npt) {
-          const double2 v = A[(int64_t)k * g.npt + p];
-          x = (float)v.x;
-          y = (float)v.y;
-          if (FWD) {
+      float x = 0.0f, y = 0.0f;
+      if (k < Kv && p < g.npt) {
+        const double2 v = A[(int64_t)k * g.npt + p];
+        x = (float)v.x;
+        y = (float)v.y;
+        if (FWD) {
+          if (P.d1) {
+            const float msk = P.d1[p % g.n1] * P.d2[p / g.n1];
             x *= msk;
             y *= msk;
-            if (P.vph) rot_lift2(x, y, __ldg(P.vph + (int64_t)k * g.npt + p));
           }
-        }
-        uint16_t a[3], b[3];
-        split3(x, a[0], a[1], a[2]);
-        split3(y, b[0], b[1], b[2]);
-#pragma unroll
-        for (int t = 0; t < 3; t++) {
-          if (e & 1) {
-            wre[t][e >> 1] |= (uint32_t)a[t] << 16;
-            wim[t][e >> 1] |= (uint32_t)b[t] << 16;
-          } else {
-            wre[t][e >> 1] = a[t];
-            wim[t][e >> 1] = b[t];
-          }
+          if (P.vph) rot_lift2(x, y, __ldg(P.vph + (int64_t)k * g.npt + p));
         }
       }
-      const int mre = 2 * pl, mim = 2 * pl + 1;
-      const uint32_t ore = (uint32_t)(mre / 8) * SBO_A + (mre % 8) * 16 + kg * 128;
-      const uint32_t oim = (uint32_t)(mim / 8) * SBO_A + (mim % 8) * 16 + kg * 128;
+      sF[(2 * pl) * LDF + k] = x;
+      sF[(2 * pl + 1) * LDF + k] = y;
+    }
+  }
+  __syncthreads();
+  // ---- phase 2: thread `tid` scales and slices row m = tid
+  float srow = 1.0f;
+  {
+    const int m = tid;
+    const float *row = sF + m * LDF;
+    float mx = 0.0f;
+    for (int k = 0; k < Kp; k++) mx = fmaxf(mx, fabsf(row[k]));
+    // rows below 1e-30 (far below any value that reaches a norm or a flux)
+    // are set to zero so that the power-of-two scale stays a normal float
+    int e = 0;
+    if (mx >= 1e-30f) frexpf(mx, &e);
+    const float inv = mx >= 1e-30f ? ldexpf(1.0f, -e) * 256.0f : 0.0f;
+    srow = ldexpf(1.0f, e - 16);          // s_m 2^-16 (the two 2^-8 of i0 j0)
+    const uint32_t orow = (uint32_t)(m / 8) * SBO_A + (m % 8) * 16;
+    for (int kg = 0; kg < Kp / 8; kg++) {
+      uint32_t w[3][4];
 #pragma unroll
-      for (int t = 0; t < 3; t++) {
-        *reinterpret_cast<uint4 *>(sA + t * A_TERM + ore) = make_uint4(wre[t][0], wre[t][1], wre[t][2], wre[t][3]);
-        *reinterpret_cast<uint4 *>(sA + t * A_TERM + oim) = make_uint4(wim[t][0], wim[t][1], wim[t][2], wim[t][3]);
+      for (int e8 = 0; e8 < 8; e8++) {
+        const float a = row[kg * 8 + e8] * inv;      // exact power-of-two scaling
+        const float i0 = rintf(a);
+        const float r1 = (a - i0) * 256.0f;          // exact
+        const float i1 = rintf(r1);
+        const float i2 = rintf((r1 - i1) * 256.0f);
+        const uint16_t h0 = __bfloat16_as_ushort(__float2bfloat16_rn(i0));
+        const uint16_t h1 = __bfloat16_as_ushort(__float2bfloat16_rn(i1));
+        const uint16_t h2 = __bfloat16_as_ushort(__float2bfloat16_rn(i2));
+        if (e8 & 1) {
+          w[0][e8 >> 1] |= (uint32_t)h0 << 16;
+          w[1][e8 >> 1] |= (uint32_t)h1 << 16;
+          w[2][e8 >> 1] |= (uint32_t)h2 << 16;
+        } else {
+          w[0][e8 >> 1] = h0;
+          w[1][e8 >> 1] = h1;
+          w[2][e8 >> 1] = h2;
+        }
       }
+#pragma unroll
+      for (int t = 0; t < 3; t++)
+        *reinterpret_cast<uint4 *>(sA + t * A_TERM + orow + kg * 128) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
     }
   }
   // make the generic-proxy shared stores visible to the tensor core (async proxy)
@@ -278,9 +339,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
     for (int s = 0; s < Kp / 16; s++) {
 #pragma unroll
       for (int q = 0; q < 6; q++) {
+        const int d = c_pair_a[q] + c_pair_b[q];            // slice order -> accumulator
         const uint64_t ad = make_desc(a0 + c_pair_a[q] * A_TERM + s * 256, 128, SBO_A);
         const uint64_t bdsc = make_desc(b0 + c_pair_b[q] * B_TERM + s * 256, 128, SBO_B);
-        mma_bf16(tmem, ad, bdsc, idesc, (s | q) != 0);
+        const bool first = s == 0 && (q == 0 || q == 1 || q == 3);
+        mma_bf16(tmem + (uint32_t)(d * Np), ad, bdsc, idesc, first ? 0u : 1u);
       }
     }
     mma_commit(smem_u32(&mbar));
@@ -301,25 +364,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
   }
   tc_fence_after();
 
-  // ---- epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31
+  // ---- epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31; row m = tid
   const int m = 32 * warp + lane;
   const int pl = m >> 1, c = m & 1;
   const int64_t p = p0 + pl;
+  const float *tsc = P.bscale + (int64_t)blockIdx.y * 256;
   float mod = 0.0f, pe = 0.0f;
   double *Cd = reinterpret_cast<double *>(P.C);
+  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
   for (int n0 = 0; n0 < Np; n0 += 16) {
-    float v[16];
-    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)n0, v);
+    float d0[16], d1[16], d2[16];
+    tmem_ld16(trow + (uint32_t)n0, d0);
+    tmem_ld16(trow + (uint32_t)(Np + n0), d1);
+    tmem_ld16(trow + (uint32_t)(2 * Np + n0), d2);
     if (!ok || p >= g.npt) continue;
 #pragma unroll
     for (int q = 0; q < 16; q++) {
       const int n = n0 + q;
       if (n >= Nv) break;
+      const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc[n]);
       if (FWD) {
-        Cd[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = (double)v[q];
+        Cd[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = (double)v;
       } else {
-        Cd[2 * (((int64_t)blockIdx.y * g.nth + n) * g.npt + p) + c] = (double)v[q];
-        const float v2 = v[q] * v[q];
+        Cd[2 * (((int64_t)blockIdx.y * g.nth + n) * g.npt + p) + c] = (double)v;
+        const float v2 = v * v;
         mod = fmaf(__ldg(P.w + n), v2, mod);
         pe = fmaf(__ldg(P.wv + (int64_t)n * g.npt + p), v2, pe);
       }
@@ -341,22 +409,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
   }
 }
 
-// Dynamic shared memory of one launch: the A and B tiles, and at least
-// ncols * 456 bytes so that no more than 512/ncols CTAs share an SM (the
-// TMEM columns that their allocations need never exceed the SM's 512).
+// Dynamic shared memory of one launch: the BF16 slices of A and B and the
+// FP32 staging rows, and at least enough that no more than 512/ncols CTAs fit
+// on an SM (233472 bytes of shared memory), so the TMEM columns that their
+// allocations need never exceed the SM's 512.
 size_t tc_smem_bytes(int Kp, int Np) {
-  const size_t need = (size_t)3 * 16 * (Kp / 8 * 128) + (size_t)tc_bimg_bytes(Np, Kp);
-  const size_t ncols = Np <= 32 ? 32 : (Np <= 64 ? 64 : (Np <= 128 ? 128 : 256));
-  return std::max(need, ncols * 456 + 1024);
+  const size_t need = (size_t)3 * 16 * (Kp / 8 * 128) + (size_t)tc_bimg_bytes(Np, Kp) + (size_t)128 * (Kp + 1) * 4;
+  const size_t ctas = 512 / tc_tmem_cols(Np);
+  return std::max(need, (size_t)233472 / (ctas + 1) + 1024);
 }
+
+bool tc_shape_ok(int Kp, int Np) { return Kp <= 192 && Np <= 160 && tc_smem_bytes(Kp, Np) <= 200 * 1024; }
 
 int legendre_tc_part_tiles(const Grid &g) { return (int)((g.npt + TC_POINTS - 1) / TC_POINTS); }
 
 void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, double2 *psi_j,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
-                            int *status_w) {
+                            int *status_w, const float *bscale) {
   TcArgs a{};
+  a.bscale = bscale;
   a.g = g;
   a.A = psi_th;
   a.C = psi_j;
@@ -375,8 +447,9 @@ void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th
 void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j, double2 *psi_th,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
-                            const int *status, int *status_w) {
+                            const int *status, int *status_w, const float *bscale) {
   TcArgs a{};
+  a.bscale = bscale;
   a.g = g;
   a.A = psi_j;
   a.C = psi_th;
@@ -399,8 +472,8 @@ void tc_set_smem_limit(size_t bytes) {
 }
 
 void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,
-                            bool fwd, const int64_t *img_off, uint16_t *img) {
-  k_build_tc_bimage<<<dim3(8, n_blocks), 256, 0, s>>>(blocks, Bsrc, nth, fwd ? 1 : 0, img_off, img);
+                            bool fwd, const int64_t *img_off, uint16_t *img, float *bscale, int max_np) {
+  k_build_tc_bimage<<<dim3(max_np, n_blocks), 128, 0, s>>>(blocks, Bsrc, nth, fwd ? 1 : 0, img_off, img, bscale);
 }
 
 }  // namespace qd

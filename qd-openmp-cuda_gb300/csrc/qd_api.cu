@@ -285,6 +285,7 @@ struct qd_session {
   FFTPlan fft{};
   // mixed form: tensor-core Legendre images and FP32 three-shear tables
   uint16_t *img_f = nullptr, *img_b = nullptr;
+  float *bscale_f = nullptr, *bscale_b = nullptr;
   int64_t *imgoff_f = nullptr, *imgoff_b = nullptr;
   size_t smem_f = 0, smem_b = 0;
   float2 *vph = nullptr, *vph0 = nullptr, *lrotR = nullptr, *lrotr = nullptr, *lkinR = nullptr, *lkinr = nullptr;
@@ -371,7 +372,7 @@ qd_session::~qd_session() {
                   tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, d_pgroup0,
                   part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
                   flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
-                  img_f, img_b, imgoff_f, imgoff_b, vph, vph0, lrotR, lrotr, lkinR, lkinr, wf, wvf, d1f, d2f,
+                  img_f, img_b, bscale_f, bscale_b, imgoff_f, imgoff_b, vph, vph0, lrotR, lrotr, lkinR, lkinr, wf, wvf, d1f, d2f,
                   T1f, T2f};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -426,7 +427,7 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
   cudaStream_t st = s->stream;
   const Grid &g = s->g;
   launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_j, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f,
-                         first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status);
+                         first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status, s->bscale_f);
   prof_mark(st, "legendre_forward");
   if (s->any_coupled) {
     launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
@@ -452,7 +453,7 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
     prof_mark(st, "rotational_energy");
   }
   launch_legendre_tc_bwd(st, g, s->psi_j, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf, s->wvf,
-                         s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status);
+                         s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b);
   prof_mark(st, "legendre_backward");
   enqueue_tail(s);
 }
@@ -685,18 +686,25 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
       tb += 3LL * r16(g.nth) * r16(bd.nl) * 2;
       s->smem_b = std::max(s->smem_b, tc_smem_bytes(r16(bd.nl), r16(g.nth)));
     }
-    const size_t limit = 200 * 1024;
-    if (s->smem_f > limit || s->smem_b > limit) {
+    bool ok = true;
+    for (const BlockDesc &bd : s->h_blocks)
+      ok = ok && tc_shape_ok(r16(g.nth), r16(bd.nl)) && tc_shape_ok(r16(bd.nl), r16(g.nth));
+    if (!ok) {
       if (s->precision == QD_PRECISION_MIXED)
-        throw Error{QD_ERR_UNSUPPORTED, "mixed form: n_theta and l_max+1 above the tensor-core tile limit"};
+        throw Error{QD_ERR_UNSUPPORTED, "mixed form: n_theta and l_max+1 above the tensor-core tile limit "
+                                        "(contraction <= 192, columns <= 160)"};
     } else {
       tc_set_smem_limit(std::max(s->smem_f, s->smem_b));
       s->imgoff_f = dupload(of.data(), of.size(), st);
       s->imgoff_b = dupload(ob.data(), ob.size(), st);
       s->img_f = dalloc<uint16_t>((size_t)tf / 2);
       s->img_b = dalloc<uint16_t>((size_t)tb / 2);
-      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bf, g.nth, true, s->imgoff_f, s->img_f);
-      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bb, g.nth, false, s->imgoff_b, s->img_b);
+      s->bscale_f = dalloc<float>((size_t)s->n_blocks * 256);
+      s->bscale_b = dalloc<float>((size_t)s->n_blocks * 256);
+      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bf, g.nth, true, s->imgoff_f, s->img_f, s->bscale_f,
+                             r16(s->max_nl));
+      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bb, g.nth, false, s->imgoff_b, s->img_b, s->bscale_b,
+                             r16(g.nth));
     }
   }
 
@@ -1103,7 +1111,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       case QD_STAGE_FORWARD_LEGENDRE:
         if (s->precision == QD_PRECISION_MIXED)
           launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_j, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f, nullptr,
-                                 nullptr, nullptr, s->smem_f, s->status, s->status);
+                                 nullptr, nullptr, s->smem_f, s->status, s->status, s->bscale_f);
         else
           launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, nullptr,
                                   nullptr, s->status);
@@ -1111,7 +1119,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       case QD_STAGE_BACKWARD_LEGENDRE:
         if (s->precision == QD_PRECISION_MIXED)
           launch_legendre_tc_bwd(st, g, s->psi_j, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf,
-                                 s->wvf, s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status);
+                                 s->wvf, s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b);
         else
           launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
                                   s->part_modpe, s->t_modpe, s->status);

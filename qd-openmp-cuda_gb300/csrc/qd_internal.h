@@ -203,17 +203,18 @@ void launch_build_float_tables(cudaStream_t s, const Grid &g, const double *w, c
 // tcgen05 BF16x3 Legendre contraction
 struct TcArgs;
 size_t tc_smem_bytes(int Kp, int Np);
+bool tc_shape_ok(int Kp, int Np);
 void tc_set_smem_limit(size_t bytes);
 void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,
-                            bool fwd, const int64_t *img_off, uint16_t *img);
+                            bool fwd, const int64_t *img_off, uint16_t *img, float *bscale, int max_np);
 void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, double2 *psi_j,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
-                            int *status_w);
+                            int *status_w, const float *bscale);
 void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j, double2 *psi_th,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
-                            const int *status, int *status_w);
+                            const int *status, int *status_w, const float *bscale);
 int legendre_tc_part_tiles(const Grid &g);
 
 void launch_build_half_v(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,

@@ -98,12 +98,13 @@ def test_evolve_matches_oracle(qd, oracle, gpu, case):
     assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-9 * max(1e-30, np.abs(crp).max())
 
 
-def test_fp64_500_steps_reference_grid(qd, oracle, gpu):
-    """64x32x24, J=0, dt=10, 500 steps: relative |dpsi| <= 1e-10 and |dP| <= 1e-8 (relative to max P)."""
+def test_fp64_1000_steps_reference_grid(qd, oracle, gpu):
+    """64x32x24, J=0, dt=10, 1000 steps: relative |dpsi| <= 1e-10 and |dP| <= 1e-8 (relative to max P)."""
     cfg = qd.inputs.CONFIGS["fh2_j0_64x32x24"]
     d = qd.inputs.build_fh2data(cfg)
+    d["time"]["total_steps"] = 1000
     o = oracle.Oracle(qd.inputs.build_fh2data(cfg))
-    o.run(cfg.total_steps)
+    o.run(1000)
     qd.cudaOpenMPEvolution(d)
     assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-10
     crp = o.crp()
