@@ -102,7 +102,13 @@ def algorithmic(kernel: str, d: dict, flux_chunk: int = 32):
         flops = sum(4.0 * npt * nth * nl for nl in nls)
         if prec == 0:
             return "fp64", flops, "TFLOP/s"
-        return "tensor", flops, "TFLOP/s"
+        # BF16x3 on tensor cores: 6 products per real multiply-add keep the
+        # tensor pipe far below its peak at K <= 96; HBM bounds the kernel
+        if kernel == "legendre_forward":   # psi_theta + V shears in, psi_j out
+            byts = sum(16.0 * npt * nth + 8.0 * npt * nth + 16.0 * npt * nl for nl in nls)
+        else:                              # psi_j in, psi_theta out, w V (FP32) in
+            byts = sum(16.0 * npt * nl + 16.0 * npt * nth + 4.0 * npt * nth for nl in nls)
+        return "hbm", byts, "GB/s"
     if kernel == "fft_rows_forward" or kernel == "fft_cols_kinetic":
         return "hbm", 32.0 * npt * snl, "GB/s"
     if kernel == "fft_rows_inverse":
