@@ -209,6 +209,29 @@ int qd_session_set_psi(qd_session *s, int32_t which, int32_t block, const double
 /* energies of the last completed step or stage: [n_blocks][6] */
 int qd_session_get_energies(qd_session *s, double *host_out, size_t n_doubles);
 
+/* ------------------------------------------------------ allocation-free call */
+
+/* Rotational energy of one Omega block, computed without allocating any device
+   memory.  It has no counterpart in the reference.  It is for callers that
+   cannot call cudaMalloc: code whose device memory is all owned by another
+   allocator (a framework's caching pool such as PyTorch's or MATLAB gpuArray's)
+   or a loop in which the device synchronisation of cudaMalloc is not allowed.
+   psi_j: device pointer to the block's Legendre-space slabs l = omega..l_max,
+   [l_max-omega+1][n2][n1] complex (interleaved doubles).  rotational_energy:
+   device pointer to one double, receiving dr1 dr2 sum_l l(l+1)
+   sum (1/(2 m1 R^2) + 1/(2 m2 r^2)) |psi_l|^2, the same quantity as the
+   session's rotational energy.  stream: a cudaStream_t, or NULL for the default
+   stream.  The per-CTA partial sums live in a fixed 512 KiB device array of the
+   library (every GPU that loads the library holds it until exit), so
+   l_max - omega + 1 may be at most 4096; larger values return QD_ERR_INVALID.
+   All calls share that array, so calls that overlap on the GPU (on different
+   streams, or on different host threads) race.  The first call on each device
+   looks up the array's device address with that device current; make that
+   first call before any stream capture. */
+int qd_rotational_energy_noalloc(const double *psi_j, int32_t n1, int32_t n2, int32_t omega, int32_t l_max,
+                                 double r1_left, double r1_dr, double r1_mass, double r2_left, double r2_dr,
+                                 double r2_mass, double *rotational_energy, void *stream);
+
 /* ------------------------------------------------------------ diagnostics */
 
 /* Runs n_steps regular time steps eagerly with a CUDA event after every

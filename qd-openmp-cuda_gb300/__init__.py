@@ -94,7 +94,8 @@ _lib = None
 EXPORTED = ("qd_evolve", "qd_evolve_batch", "qd_last_error", "qd_version", "qd_session_create",
             "qd_session_destroy", "qd_session_run", "qd_session_synchronize", "qd_session_download",
             "qd_session_upload", "qd_session_stream", "qd_session_info", "qd_session_apply", "qd_session_get_psi",
-            "qd_session_set_psi", "qd_session_get_energies", "qd_session_profile", "qd_device_fma_peaks")
+            "qd_session_set_psi", "qd_session_get_energies", "qd_session_profile", "qd_device_fma_peaks",
+            "qd_rotational_energy_noalloc")
 
 
 def library_path() -> Path:
@@ -131,6 +132,9 @@ def load_library():
     lib.qd_session_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double),
                                        P(C.c_int32), C.c_int32, P(C.c_int32)]
     lib.qd_device_fma_peaks.argtypes = [P(C.c_double), P(C.c_double)]
+    lib.qd_rotational_energy_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                                 C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                                 C.c_double, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 

@@ -13,7 +13,7 @@ BUILD = HERE / "_build"
 LIB = HERE / "libqd.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-SOURCES = ["qd_api.cu", "k_pointwise.cu", "k_legendre.cu", "k_fft.cu", "k_coriolis.cu", "k_flux.cu", "k_diag.cu", "k_legendre_tc.cu"]
+SOURCES = ["qd_api.cu", "k_pointwise.cu", "k_legendre.cu", "k_fft.cu", "k_coriolis.cu", "k_flux.cu", "k_diag.cu", "k_legendre_tc.cu", "k_noalloc.cu"]
 
 
 def nvcc() -> str:
