@@ -300,6 +300,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="only build the workload and run this many steps of --precision (for ncu captures)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--accuracy", type=int, default=0,
                     help="run the mixed-vs-FP64 accuracy study for this many steps instead of the benchmark")
     args = ap.parse_args()
@@ -317,6 +320,14 @@ def main():
     qd.load_library()
     if args.accuracy:
         print(json.dumps({"accuracy": accuracy(qd, args.accuracy)}), flush=True)
+        return
+    if args.profile_steps:
+        d = qd.inputs.build_fh2data(qd.inputs.CONFIGS[WORKLOAD])
+        d["options"]["precision"] = 1 if args.precision == "mixed" else 0
+        with qd.Session(d) as s:
+            s.run(args.profile_steps)
+            s.synchronize()
+        print(json.dumps({"profile_steps": args.profile_steps, "precision": args.precision}), flush=True)
         return
     gpu_index = local
     if os.environ.get("CUDA_VISIBLE_DEVICES"):

@@ -36,7 +36,7 @@
 namespace qd {
 
 namespace {
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 256;     // 8 warps: staging, slicing and epilogue; thread 0 issues the MMAs
 constexpr int TC_POINTS = 64;        // 128 real rows
 constexpr uint64_t WAIT_NS = 1000000000ull;   // give up waiting for the MMA chain after 1 s
 
@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
   __shared__ uint64_t mbar;
   __shared__ uint32_t tmem_base_s;
   __shared__ double red[32];
+  __shared__ float srow_s[128];
   const BlockDesc bd = P.blocks[blockIdx.y];
   const Grid &g = P.g;
   const int Kv = FWD ? g.nth : bd.nl, Nv = FWD ? bd.nl : g.nth;
@@ -260,35 +261,48 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
     const int n16 = (int)(tc_bimg_bytes(Np, Kp) / 16);
     for (int q = tid; q < n16; q += TC_THREADS) dst[q] = __ldg(src + q);
   }
-  // ---- phase 1: A tile as FP32 rows (row 2p = re, 2p+1 = im), phases applied
+  // ---- phase 1: A tile as FP32 rows (row 2p = re, 2p+1 = im), phases applied.
+  // Eight independent loads per thread are in flight before any is used.
   {
     const double2 *A = FWD ? P.A + (int64_t)blockIdx.y * g.nth * g.npt : P.A + (int64_t)bd.slab0 * g.npt;
-    for (int it = tid; it < TC_POINTS * Kp; it += TC_THREADS) {
-      const int pl = it % TC_POINTS, k = it / TC_POINTS;
-      const int64_t p = p0 + pl;
-      float x = 0.0f, y = 0.0f;
-      if (k < Kv && p < g.npt) {
-        const double2 v = A[(int64_t)k * g.npt + p];
-        x = (float)v.x;
-        y = (float)v.y;
-        if (FWD) {
+    const int total = TC_POINTS * Kp;
+    constexpr int U = 8;
+    for (int base = tid; base < total; base += TC_THREADS * U) {
+      double2 v[U];
+      float2 ts[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int it = base + u * TC_THREADS;
+        const int pl = it % TC_POINTS, k = it / TC_POINTS;
+        const int64_t p = p0 + pl;
+        const bool in = it < total && k < Kv && p < g.npt;
+        v[u] = in ? A[(int64_t)k * g.npt + p] : make_double2(0.0, 0.0);
+        if (FWD) ts[u] = (in && P.vph) ? __ldg(P.vph + (int64_t)k * g.npt + p) : make_float2(0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int it = base + u * TC_THREADS;
+        if (it >= total) break;
+        const int pl = it % TC_POINTS, k = it / TC_POINTS;
+        const int64_t p = p0 + pl;
+        float x = (float)v[u].x, y = (float)v[u].y;
+        if (FWD && p < g.npt) {
           if (P.d1) {
             const float msk = P.d1[p % g.n1] * P.d2[p / g.n1];
             x *= msk;
             y *= msk;
           }
-          if (P.vph) rot_lift2(x, y, __ldg(P.vph + (int64_t)k * g.npt + p));
+          if (P.vph) rot_lift2(x, y, ts[u]);
         }
+        sF[(2 * pl) * LDF + k] = x;
+        sF[(2 * pl + 1) * LDF + k] = y;
       }
-      sF[(2 * pl) * LDF + k] = x;
-      sF[(2 * pl + 1) * LDF + k] = y;
     }
   }
   __syncthreads();
-  // ---- phase 2: thread `tid` scales and slices row m = tid
-  float srow = 1.0f;
+  // ---- phase 2: threads 2m and 2m+1 scale and slice row m (halves of K)
   {
-    const int m = tid;
+    const int m = tid >> 1, half = tid & 1;
     const float *row = sF + m * LDF;
     float mx = 0.0f;
     for (int k = 0; k < Kp; k++) mx = fmaxf(mx, fabsf(row[k]));
@@ -297,9 +311,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
     int e = 0;
     if (mx >= 1e-30f) frexpf(mx, &e);
     const float inv = mx >= 1e-30f ? ldexpf(1.0f, -e) * 256.0f : 0.0f;
-    srow = ldexpf(1.0f, e - 16);          // s_m 2^-16 (the two 2^-8 of i0 j0)
+    if (half == 0) srow_s[m] = ldexpf(1.0f, e - 16);   // s_m 2^-16 (the two 2^-8 of i0 j0)
     const uint32_t orow = (uint32_t)(m / 8) * SBO_A + (m % 8) * 16;
-    for (int kg = 0; kg < Kp / 8; kg++) {
+    const int kgs = Kp / 8;
+    for (int kg = half; kg < kgs; kg += 2) {
       uint32_t w[3][4];
 #pragma unroll
       for (int e8 = 0; e8 < 8; e8++) {
@@ -364,15 +379,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
   }
   tc_fence_after();
 
-  // ---- epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31; row m = tid
-  const int m = 32 * warp + lane;
+  // ---- epilogue: warp w reads TMEM lanes 32(w%4) .. +31 (rows), column chunks
+  // n0 = 16 (w/4) + 32 j; row m -> point m/2, component m%2
+  const int quarter = warp & 3, cgrp = warp >> 2;
+  const int m = 32 * quarter + lane;
   const int pl = m >> 1, c = m & 1;
   const int64_t p = p0 + pl;
+  const float srow = srow_s[m];
   const float *tsc = P.bscale + (int64_t)blockIdx.y * 256;
   float mod = 0.0f, pe = 0.0f;
   double *Cd = reinterpret_cast<double *>(P.C);
-  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
-  for (int n0 = 0; n0 < Np; n0 += 16) {
+  const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
+  for (int n0 = 16 * cgrp; n0 < Np; n0 += 32) {
     float d0[16], d1[16], d2[16];
     tmem_ld16(trow + (uint32_t)n0, d0);
     tmem_ld16(trow + (uint32_t)(Np + n0), d1);
