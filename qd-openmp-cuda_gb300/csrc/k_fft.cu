@@ -174,10 +174,15 @@ __device__ inline void lift2(float &x, float &y, float2 ts) {
   x = fmaf(ts.x, y, x);
 }
 
+// storage (FP64) <-> arithmetic type; FP32 conversions use integer instructions
 template <typename R> __device__ inline typename CT<R>::T from_d(double2 v) {
-  return CT<R>::make((R)v.x, (R)v.y);
+  if constexpr (std::is_same<R, float>::value)
+    return make_float2(d2f_rn(v.x), d2f_rn(v.y));
+  else
+    return v;
 }
-template <typename C> __device__ inline double2 to_d(C v) { return make_double2((double)v.x, (double)v.y); }
+__device__ inline double2 to_d(double2 v) { return v; }
+__device__ inline double2 to_d(float2 v) { return make_double2(f2d(v.x), f2d(v.y)); }
 
 }  // namespace
 
@@ -238,9 +243,9 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ 
         lift2(x, y, __ldg(liftr + (int64_t)l * g.n2 + j));
       }
       if (fscale != 0.0f) {
-        v = make_double2((double)x, (double)y);
+        v = make_double2(f2d(x), f2d(y));
       } else {
-        v = make_double2((double)x * scale, (double)y * scale);
+        v = make_double2(f2d(x) * scale, f2d(y) * scale);
       }
       if (re_part) {
         const float Rr = (float)(g.left1 + i * g.dr1), rr = (float)(g.left2 + j * g.dr2);

@@ -169,6 +169,65 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_dev(int64_t ns2, int 
   }
 }
 
+// Mixed form of the transform: products and the 32-step partial sums in FP32
+// (phases computed in FP64 and rounded once, surface values converted with
+// integer instructions), each chunk's sum added into the FP64 accumulators.
+namespace {
+constexpr int FLUX_EB32 = 16;
+}
+
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_f32(int64_t ns2, int nE, int n_blocks, const int *count_p,
+                                                               int cap, const double2 *__restrict__ buf,
+                                                               const double2 *__restrict__ phase,
+                                                               double2 *__restrict__ acc, const int *status) {
+  if (status && *status) return;
+  const int count = min(min(*count_p, cap), FLUX_MAXC);
+  if (count <= 0) return;
+  __shared__ float2 ph[FLUX_MAXC][FLUX_EB32];
+  const int b = blockIdx.z;
+  const int e0 = blockIdx.y * FLUX_EB32;
+  for (int q = threadIdx.x; q < count * FLUX_EB32; q += blockDim.x) {
+    const int n = q / FLUX_EB32, e = q % FLUX_EB32;
+    const double2 v = e0 + e < nE ? phase[(int64_t)n * nE + e0 + e] : make_double2(0.0, 0.0);
+    ph[n][e] = make_float2(d2f_rn(v.x), d2f_rn(v.y));
+  }
+  __syncthreads();
+  const int64_t s = (int64_t)blockIdx.x * FLUX_THREADS + threadIdx.x;
+  if (s >= ns2) return;
+  float2 a[FLUX_EB32];
+#pragma unroll
+  for (int e = 0; e < FLUX_EB32; e++) a[e] = make_float2(0.0f, 0.0f);
+  for (int n = 0; n < count; n++) {
+    const double2 vd = buf[((int64_t)n * n_blocks + b) * ns2 + s];
+    const float vx = d2f_rn(vd.x), vy = d2f_rn(vd.y);
+#pragma unroll
+    for (int e = 0; e < FLUX_EB32; e++) {
+      const float2 p = ph[n][e];
+      a[e].x = fmaf(p.x, vx, fmaf(-p.y, vy, a[e].x));
+      a[e].y = fmaf(p.x, vy, fmaf(p.y, vx, a[e].y));
+    }
+  }
+  const int64_t ns = ns2 / 2;
+  const int c = (int)(s / ns);
+  const int64_t kq = s % ns;
+#pragma unroll
+  for (int e = 0; e < FLUX_EB32; e++) {
+    if (e0 + e >= nE) break;
+    double2 *dst = acc + (((int64_t)b * 2 + c) * nE + e0 + e) * ns + kq;
+    double2 v = *dst;
+    v.x += f2d(a[e].x);
+    v.y += f2d(a[e].y);
+    *dst = v;
+  }
+}
+
+void launch_flux_dft_f32(cudaStream_t s, int64_t ns2, int nE, int n_blocks, const int *count_p, int cap,
+                         const double2 *buf, const double2 *phase, double2 *acc, const int *status) {
+  dim3 grid((unsigned)((ns2 + FLUX_THREADS - 1) / FLUX_THREADS), (unsigned)((nE + FLUX_EB32 - 1) / FLUX_EB32),
+            (unsigned)n_blocks);
+  k_flux_dft_f32<<<grid, FLUX_THREADS, 0, s>>>(ns2, nE, n_blocks, count_p, cap, buf, phase, acc, status);
+}
+
 // P(E) per problem: one CTA per (E, problem)
 __global__ void k_flux_crp(Grid g, int nE, const int *__restrict__ pblock0, const double2 *__restrict__ acc,
                            const double *__restrict__ w, const double *__restrict__ eta_sq, double *__restrict__ crp) {

@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
         if (it >= total) break;
         const int pl = it % TC_POINTS, k = it / TC_POINTS;
         const int64_t p = p0 + pl;
-        float x = (float)v[u].x, y = (float)v[u].y;
+        float x = d2f_rn(v[u].x), y = d2f_rn(v[u].y);
         if (FWD && p < g.npt) {
           if (P.d1) {
             const float msk = P.d1[p % g.n1] * P.d2[p / g.n1];
@@ -402,9 +402,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
       if (n >= Nv) break;
       const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc[n]);
       if (FWD) {
-        Cd[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = (double)v;
+        Cd[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = f2d(v);
       } else {
-        Cd[2 * (((int64_t)blockIdx.y * g.nth + n) * g.npt + p) + c] = (double)v;
+        Cd[2 * (((int64_t)blockIdx.y * g.nth + n) * g.npt + p) + c] = f2d(v);
         const float v2 = v * v;
         mod = fmaf(__ldg(P.w + n), v2, mod);
         pe = fmaf(__ldg(P.wv + (int64_t)n * g.npt + p), v2, pe);

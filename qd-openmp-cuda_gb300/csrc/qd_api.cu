@@ -394,9 +394,14 @@ static void enqueue_flux_dft(qd_session *s) {
                                                                    s->dt, s->flux_phase);
   prof_mark(s->stream, "flux_phase");
   const int64_t ns2 = 2LL * s->g.nth * s->g.n1;
-  dim3 grid((unsigned)((ns2 + 127) / 128), (unsigned)((nE + 7) / 8), (unsigned)s->n_blocks);
-  k_flux_dft_dev<<<grid, 128, 0, s->stream>>>(ns2, nE, s->n_blocks, s->flux_count, cap, s->flux_buf, s->flux_phase,
-                                               s->flux_acc, s->status);
+  if (s->precision == QD_PRECISION_MIXED) {
+    launch_flux_dft_f32(s->stream, ns2, nE, s->n_blocks, s->flux_count, cap, s->flux_buf, s->flux_phase,
+                        s->flux_acc, s->status);
+  } else {
+    dim3 grid((unsigned)((ns2 + 127) / 128), (unsigned)((nE + 7) / 8), (unsigned)s->n_blocks);
+    k_flux_dft_dev<<<grid, 128, 0, s->stream>>>(ns2, nE, s->n_blocks, s->flux_count, cap, s->flux_buf,
+                                                 s->flux_phase, s->flux_acc, s->status);
+  }
   prof_mark(s->stream, "flux_dft");
   k_flux_reset<<<1, 1, 0, s->stream>>>(s->flux_count);
   prof_mark(s->stream, "flux_reset");
@@ -510,8 +515,8 @@ static void enqueue_tail(qd_session *s) {
     k_flux_begin<<<1, 1, 0, st>>>(s->d_step, s->flux_count, s->flux_t0, s->dt, s->flux_slot, s->flux.chunk,
                                   s->status);
     const int64_t ns = (int64_t)g.nth * g.n1;
-    dim3 grid((unsigned)std::min<int64_t>((ns + 255) / 256, 64), (unsigned)s->n_blocks);
-    k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
+    dim3 grid((unsigned)((ns + 127) / 128), (unsigned)s->n_blocks);
+    k_flux_extract_dev<<<grid, 128, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
                                              s->flux_buf, s->n_blocks, s->flux_slot, s->status);
     prof_mark(st, "flux_extract");
   }

@@ -21,6 +21,34 @@ inline unsigned grid_for(int64_t n, int threads, int max_blocks = 152 * 16) {
   return (unsigned)b;
 }
 
+// FP64 <-> FP32 conversion with integer instructions.  On GB300 the F2F
+// conversion instructions issue on the FP64 pipe (1/58 of the FP32 rate), so
+// kernels that compute in FP32 on FP64 storage convert with bit operations:
+//   d2f_rn: round to nearest even; |x| < 2^-126 -> signed zero; overflow -> inf;
+//           NaN -> NaN.
+//   f2d:    exact; FP32 subnormals -> signed zero.
+__device__ inline float d2f_rn(double x) {
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  const uint32_t sign = hi & 0x80000000u;
+  const uint32_t ef = (hi >> 20) & 0x7ffu;
+  if (ef == 0x7ffu) return __uint_as_float(sign | 0x7f800000u | ((hi & 0xfffffu) | lo ? 0x400000u : 0u));
+  const int e = (int)ef - 896;   // rebias 1023 -> 127
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const uint32_t rem = lo & 0x1fffffffu;
+  m += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  return __uint_as_float(sign | (((uint32_t)e << 23) + m));   // a mantissa carry rounds up the exponent
+}
+
+__device__ inline double f2d(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  if (e == 0u) return __hiloint2double((int)sign, 0);
+  if (e == 0xffu) return __hiloint2double((int)(sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u)), 0);
+  return __hiloint2double((int)(sign | ((e + 896u) << 20) | (m >> 3)), (int)(m << 29));
+}
+
 // Deterministic block-wide sum (fixed shuffle tree then fixed smem tree);
 // every thread gets the result.  red must hold 32 doubles; all threads call.
 __device__ inline double block_sum(double v, double *red) {
