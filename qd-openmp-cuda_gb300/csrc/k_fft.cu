@@ -83,20 +83,31 @@ __device__ inline void dft(typename CT<R>::T *v, bool inv) {
 // so that shared-memory accesses stay contiguous.
 template <typename R, int RAD, bool COLS>
 __device__ inline void fft_stage(typename CT<R>::T *buf, int N, int nrows, int rs, int es, int Ns,
-                                 const typename CT<R>::T *__restrict__ tw, bool inv) {
+                                 const typename CT<R>::T *__restrict__ tw, bool inv, const FastDiv &fnbf,
+                                 const FastDiv &fNs, const FastDiv &frows) {
   using C = typename CT<R>::T;
   constexpr int NB = (MAXV + RAD - 1) / RAD;
   const int nbf = N / RAD;
   const int total = nrows * nbf;
   const int tstep = N / (Ns * RAD);
   C v[NB][RAD];
+  int dst_base[NB];
 #pragma unroll
   for (int q = 0; q < NB; q++) {
     const int t = threadIdx.x + FFT_THREADS * q;
     if (t < total) {
-      const int row = COLS ? (t % nrows) : (t / nbf);
-      const int jj = COLS ? (t / nrows) : (t % nbf);
-      const int k = jj % Ns;
+      int row, jj;
+      if (COLS) {
+        const int qq = (int)fdiv(frows, (uint32_t)t);
+        row = t - qq * nrows;
+        jj = qq;
+      } else {
+        row = (int)fdiv(fnbf, (uint32_t)t);
+        jj = t - row * nbf;
+      }
+      const int qn = (int)fdiv(fNs, (uint32_t)jj);
+      const int k = jj - qn * Ns;
+      dst_base[q] = row * rs + (qn * Ns * RAD + k) * es;
 #pragma unroll
       for (int r = 0; r < RAD; r++) v[q][r] = buf[row * rs + (jj + r * nbf) * es];
       if (Ns > 1) {
@@ -134,31 +145,31 @@ __device__ inline void fft_stage(typename CT<R>::T *buf, int N, int nrows, int r
   for (int q = 0; q < NB; q++) {
     const int t = threadIdx.x + FFT_THREADS * q;
     if (t < total) {
-      const int row = COLS ? (t % nrows) : (t / nbf);
-      const int jj = COLS ? (t / nrows) : (t % nbf);
-      const int k = jj % Ns;
-      const int dst = (jj / Ns) * Ns * RAD + k;
 #pragma unroll
-      for (int r = 0; r < RAD; r++) buf[row * rs + (dst + r * Ns) * es] = v[q][r];
+      for (int r = 0; r < RAD; r++) buf[dst_base[q] + r * Ns * es] = v[q][r];
     }
   }
   __syncthreads();
 }
 
+// radix sequence of one transform length with the stage divisors precomputed
 struct Radices {
   int n, nst;
   int rad[16];
+  FastDiv nbf[16];   // n / rad[s]
+  FastDiv ns[16];    // product of the radices before stage s
+  FastDiv fn;        // n
 };
 
 template <typename R, bool COLS>
 __device__ inline void fft_run(typename CT<R>::T *buf, const Radices &rd, int nrows, int rs, int es,
-                               const typename CT<R>::T *__restrict__ tw, bool inv) {
+                               const typename CT<R>::T *__restrict__ tw, bool inv, const FastDiv &frows) {
   int Ns = 1;
   for (int s = 0; s < rd.nst; s++) {
     const int rad = rd.rad[s];
-    if (rad == 4) fft_stage<R, 4, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv);
-    else if (rad == 2) fft_stage<R, 2, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv);
-    else fft_stage<R, 3, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv);
+    if (rad == 4) fft_stage<R, 4, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
+    else if (rad == 2) fft_stage<R, 2, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
+    else fft_stage<R, 3, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
     Ns *= rad;
   }
 }
@@ -188,48 +199,65 @@ __device__ inline double2 to_d(float2 v) { return make_double2(f2d(v.x), f2d(v.y
 
 // ---------------------------------------------------------- rows forward
 template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ psi, Radices rd, int nrows,
-                                                          int64_t n_rows_total, const typename CT<R>::T *__restrict__ tw,
+__global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2 : 1) k_fft_rows(double2 *__restrict__ psi, Radices rd, int nrows,
+                                                          int n_rows_total, const typename CT<R>::T *__restrict__ tw,
                                                           int inv, Grid g, double scale,
                                                           const SlabDesc *__restrict__ slabs,
                                                           const double2 *__restrict__ tabE,
                                                           double *__restrict__ re_part, int re_tiles,
                                                           const int *status, const float2 *__restrict__ liftR,
-                                                          const float2 *__restrict__ liftr, float fscale) {
+                                                          const float2 *__restrict__ liftr, float fscale,
+                                                          FastDiv fn2) {
   if (status && *status) return;
   using C = typename CT<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf = reinterpret_cast<C *>(smem_raw);
   __shared__ double red[32];
   const int N = rd.n;
-  const int64_t row0 = (int64_t)blockIdx.x * nrows;
+  const int row0 = blockIdx.x * nrows;
   const int n = nrows * N;
   // FP32 path: the rotational phase as separable three-shear rotations,
   // before the forward transform or after the inverse one
   const bool lift = std::is_same<R, float>::value && liftR != nullptr;
-  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
-    const int64_t grow = row0 + e / N;
-    C v = grow < n_rows_total ? from_d<R>(psi[grow * N + (e % N)]) : CT<R>::make(0, 0);
-    if (lift && !inv && grow < n_rows_total) {
-      const int l = slabs[grow / g.n2].l, i = e % N, j = (int)(grow % g.n2);
-      float x = (float)v.x, y = (float)v.y;
-      lift2(x, y, __ldg(liftR + (int64_t)l * g.n1 + i));
-      lift2(x, y, __ldg(liftr + (int64_t)l * g.n2 + j));
-      v.x = x;
-      v.y = y;
+  {
+    // all of this thread's loads are issued before any is used
+    double2 raw[MAXV];
+#pragma unroll
+    for (int u = 0; u < MAXV; u++) {
+      const int e = threadIdx.x + FFT_THREADS * u;
+      const int grow = row0 + (int)fdiv(rd.fn, (uint32_t)e);
+      raw[u] = (e < n && grow < n_rows_total) ? psi[(int64_t)row0 * N + e] : make_double2(0.0, 0.0);
     }
-    buf[e] = v;
+#pragma unroll
+    for (int u = 0; u < MAXV; u++) {
+      const int e = threadIdx.x + FFT_THREADS * u;
+      if (e >= n) break;
+      const int rl = (int)fdiv(rd.fn, (uint32_t)e);
+      const int grow = row0 + rl;
+      C v = from_d<R>(raw[u]);
+      if (lift && !inv && grow < n_rows_total) {
+        const int sl = (int)fdiv(fn2, (uint32_t)grow);
+        const int l = slabs[sl].l, i = e - rl * N, j = grow - sl * g.n2;
+        float x = (float)v.x, y = (float)v.y;
+        lift2(x, y, __ldg(liftR + (int64_t)l * g.n1 + i));
+        lift2(x, y, __ldg(liftr + (int64_t)l * g.n2 + j));
+        v.x = x;
+        v.y = y;
+      }
+      buf[e] = v;
+    }
   }
   __syncthreads();
-  fft_run<R, false>(buf, rd, nrows, N, 1, tw, inv != 0);
+  fft_run<R, false>(buf, rd, nrows, N, 1, tw, inv != 0, rd.fn);
   double re = 0.0;
   float ref = 0.0f;
   for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
-    const int64_t grow = row0 + e / N;
+    const int rl = (int)fdiv(rd.fn, (uint32_t)e);
+    const int grow = row0 + rl;
     if (grow >= n_rows_total) continue;
-    const int i = e % N;
-    const int64_t sl = grow / g.n2;
-    const int j = (int)(grow % g.n2);
+    const int i = e - rl * N;
+    const int sl = (int)fdiv(fn2, (uint32_t)grow);
+    const int j = grow - sl * g.n2;
     if (std::is_same<R, float>::value && inv) {
       float x = (float)buf[e].x, y = (float)buf[e].y;
       double2 v;
@@ -253,7 +281,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ 
         const float s2 = fscale != 0.0f ? 1.0f : (float)(scale * scale);
         ref = fmaf((float)l * (float)(l + 1) * I * s2, x * x + y * y, ref);
       }
-      psi[grow * N + i] = v;
+      psi[(int64_t)grow * N + i] = v;
       continue;
     }
     double2 v = to_d(buf[e]);
@@ -268,7 +296,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ 
       const double I = 1.0 / (2 * g.m1 * Rr * Rr) + 1.0 / (2 * g.m2 * rr * rr);
       re += (double)l * (l + 1) * I * (v.x * v.x + v.y * v.y);
     }
-    psi[grow * N + i] = v;
+    psi[(int64_t)grow * N + i] = v;
   }
   if (re_part) {
     re = block_sum(re + (double)ref, red);
@@ -282,14 +310,14 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_rows(double2 *__restrict__ 
 
 // ------------------------------------- columns: forward, kinetic, inverse
 template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS) k_fft_cols(double2 *__restrict__ psi, Radices rd, int ncols, Grid g,
+__global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2 : 1) k_fft_cols(double2 *__restrict__ psi, Radices rd, int ncols, Grid g,
                                                           const typename CT<R>::T *__restrict__ tw,
                                                           const double2 *__restrict__ tab_kin,
                                                           const double *__restrict__ T1, const double *__restrict__ T2,
                                                           double *__restrict__ ke_part, int ke_tiles,
                                                           const int *status, const float2 *__restrict__ kinR,
                                                           const float2 *__restrict__ kinr, const float *__restrict__ T1f,
-                                                          const float *__restrict__ T2f) {
+                                                          const float *__restrict__ T2f, FastDiv fncols) {
   if (status && *status) return;
   using C = typename CT<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -302,16 +330,26 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_cols(double2 *__restrict__ 
   const int i0 = tile * ncols;
   double2 *p = psi + sl * g.npt + i0;
   const int n = ncols * N;
-  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
-    const int t = e / ncols, c = e % ncols;
-    buf[e] = from_d<R>(p[(int64_t)t * g.n1 + c]);
+  {
+    double2 raw[MAXV];
+#pragma unroll
+    for (int u = 0; u < MAXV; u++) {
+      const int e = threadIdx.x + FFT_THREADS * u;
+      const int t = (int)fdiv(fncols, (uint32_t)e);
+      raw[u] = e < n ? p[(int64_t)t * g.n1 + (e - t * ncols)] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < MAXV; u++) {
+      const int e = threadIdx.x + FFT_THREADS * u;
+      if (e < n) buf[e] = from_d<R>(raw[u]);
+    }
   }
   __syncthreads();
-  fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, false);
+  fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, false, fncols);
   double ke = 0.0;
   float kef = 0.0f;
   for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
-    const int t = e / ncols, c = e % ncols;
+    const int t = (int)fdiv(fncols, (uint32_t)e), c = e - t * ncols;
     if (std::is_same<R, float>::value && kinR) {
       float x = (float)buf[e].x, y = (float)buf[e].y;
       lift2(x, y, __ldg(kinR + i0 + c));
@@ -328,9 +366,9 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_cols(double2 *__restrict__ 
   }
   ke += (double)kef;
   __syncthreads();
-  fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, true);
+  fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, true, fncols);
   for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
-    const int t = e / ncols, c = e % ncols;
+    const int t = (int)fdiv(fncols, (uint32_t)e), c = e - t * ncols;
     p[(int64_t)t * g.n1 + c] = to_d(buf[e]);
   }
   if (ke_part) {
@@ -411,12 +449,25 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
                                  const double *T2, double *ke_part, const double2 *tabE, double *re_part,
                                  const int *status, const FFTLift *lf) {
   using C = typename CT<R>::T;
-  Radices r1{p.n1, p.nst1, {}}, r2{p.n2, p.nst2, {}};
-  for (int q = 0; q < p.nst1; q++) r1.rad[q] = p.rad1[q];
-  for (int q = 0; q < p.nst2; q++) r2.rad[q] = p.rad2[q];
+  auto radices = [](int n, int nst, const int *rad) {
+    Radices r{};
+    r.n = n;
+    r.nst = nst;
+    r.fn = make_fastdiv((uint32_t)n);
+    int ns = 1;
+    for (int q = 0; q < nst; q++) {
+      r.rad[q] = rad[q];
+      r.nbf[q] = make_fastdiv((uint32_t)(n / rad[q]));
+      r.ns[q] = make_fastdiv((uint32_t)ns);
+      ns *= rad[q];
+    }
+    return r;
+  };
+  const Radices r1 = radices(p.n1, p.nst1, p.rad1), r2 = radices(p.n2, p.nst2, p.rad2);
+  const FastDiv fn2 = make_fastdiv((uint32_t)g.n2), fncols = make_fastdiv((uint32_t)p.cols_per_cta);
   const C *tw1 = std::is_same<R, double>::value ? (const C *)p.tw1_d : (const C *)p.tw1_f;
   const C *tw2 = std::is_same<R, double>::value ? (const C *)p.tw2_d : (const C *)p.tw2_f;
-  const int64_t rows = (int64_t)n_slabs * g.n2;
+  const int rows = n_slabs * g.n2;
   const size_t sm_rows = (size_t)p.rows_per_cta * p.n1 * sizeof(C);
   const size_t sm_cols = (size_t)p.cols_per_cta * p.n2 * sizeof(C);
   const unsigned nrow_ctas = (unsigned)(rows / p.rows_per_cta);
@@ -425,17 +476,17 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
   const float fscale = pow2 ? (float)scale : 0.0f;
   k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 0, g, 1.0, slabs,
                                                         nullptr, nullptr, 0, status, lf ? lf->proR : nullptr,
-                                                        lf ? lf->pror : nullptr, 0.0f);
+                                                        lf ? lf->pror : nullptr, 0.0f, fn2);
   prof_mark(s, "fft_rows_forward");
   const unsigned ncol_ctas = (unsigned)(n_slabs * (p.n1 / p.cols_per_cta));
   k_fft_cols<R><<<ncol_ctas, FFT_THREADS, sm_cols, s>>>(psi_j, r2, p.cols_per_cta, g, tw2, tab_kin, T1, T2, ke_part,
                                                         fft_col_tiles(p), status, lf ? lf->kinR : nullptr,
                                                         lf ? lf->kinr : nullptr, lf ? lf->T1f : nullptr,
-                                                        lf ? lf->T2f : nullptr);
+                                                        lf ? lf->T2f : nullptr, fncols);
   prof_mark(s, "fft_cols_kinetic");
   k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 1, g, scale, slabs,
                                                         tabE, re_part, fft_row_tiles(p), status,
-                                                        lf ? lf->epiR : nullptr, lf ? lf->epir : nullptr, fscale);
+                                                        lf ? lf->epiR : nullptr, lf ? lf->epir : nullptr, fscale, fn2);
   prof_mark(s, "fft_rows_inverse");
 }
 

@@ -267,6 +267,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
     const double2 *A = FWD ? P.A + (int64_t)blockIdx.y * g.nth * g.npt : P.A + (int64_t)bd.slab0 * g.npt;
     const int total = TC_POINTS * Kp;
     constexpr int U = 8;
+    static_assert(TC_THREADS % TC_POINTS == 0, "a thread stages one point");
+    // every item of this thread has the same point (it % 64 == tid % 64)
+    const int64_t pme = p0 + (tid % TC_POINTS);
+    float msk = 1.0f;
+    if (FWD && P.d1 && pme < g.npt) {
+      const int ip = (int)(pme % g.n1);
+      msk = P.d1[ip] * P.d2[(int)(pme / g.n1)];
+    }
     for (int base = tid; base < total; base += TC_THREADS * U) {
       double2 v[U];
       float2 ts[U];
@@ -287,11 +295,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
         const int64_t p = p0 + pl;
         float x = d2f_rn(v[u].x), y = d2f_rn(v[u].y);
         if (FWD && p < g.npt) {
-          if (P.d1) {
-            const float msk = P.d1[p % g.n1] * P.d2[p / g.n1];
-            x *= msk;
-            y *= msk;
-          }
+          x *= msk;
+          y *= msk;
           if (P.vph) rot_lift2(x, y, ts[u]);
         }
         sF[(2 * pl) * LDF + k] = x;

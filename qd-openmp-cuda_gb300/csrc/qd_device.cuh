@@ -21,6 +21,28 @@ inline unsigned grid_for(int64_t n, int threads, int max_blocks = 152 * 16) {
   return (unsigned)b;
 }
 
+// Division by a runtime divisor d with a precomputed magic number
+// (round-up method): q = (t + ((x - t) >> 1)) >> (s - 1), t = umulhi(x, m),
+// exact for every 32-bit x.  Replaces the long integer-division sequences in
+// index arithmetic.
+struct FastDiv {
+  uint32_t d, m, s;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f{d, 0u, 0u};
+  if (d <= 1) return f;
+  uint32_t s = 0;
+  while ((1ull << s) < d) s++;
+  f.s = s;
+  f.m = (uint32_t)(((((uint64_t)1 << 32) * (((uint64_t)1 << s) - d)) / d) + 1);
+  return f;
+}
+__device__ inline uint32_t fdiv(const FastDiv &f, uint32_t x) {
+  if (f.d <= 1) return x;
+  const uint32_t t = __umulhi(x, f.m);
+  return (t + ((x - t) >> 1)) >> (f.s - 1);
+}
+
 // FP64 <-> FP32 conversion with integer instructions.  On GB300 the F2F
 // conversion instructions issue on the FP64 pipe (1/58 of the FP32 rate), so
 // kernels that compute in FP32 on FP64 storage convert with bit operations:
