@@ -18,8 +18,11 @@
 #include "qd_internal.h"
 #include "qd_device.cuh"
 
+#include <cooperative_groups.h>
 #include <cmath>
 #include <vector>
+
+namespace cg = cooperative_groups;
 
 namespace qd {
 
@@ -377,6 +380,116 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
   }
 }
 
+// ------------------------------------------------- single-pass slab FFT (FP32)
+// One thread-block cluster of C CTAs per Legendre slab.  CTA c owns the rows
+// r in [c n2/C, (c+1) n2/C) in Xr and, after the first exchange, the columns
+// kR in [c n1/C, (c+1) n1/C) in Xc; the exchange reads and writes the other
+// CTAs' shared memory directly (distributed shared memory).  HBM sees one read
+// and one write per point instead of three of each.
+__global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_slab_cluster(
+    double2 *__restrict__ psi, Radices r1d, Radices r2d, int C, Grid g, const SlabDesc *__restrict__ slabs,
+    const float2 *__restrict__ tw1, const float2 *__restrict__ tw2, FFTLift lf, double *__restrict__ ke_part,
+    double *__restrict__ re_part, float fscale, double scale, FastDiv fcols, const int *status) {
+  if (status && *status) return;   // uniform over the cluster: every CTA reads the same flag
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  const int n1 = g.n1, n2 = g.n2;
+  const int rows = n2 / C, cols = n1 / C;
+  float2 *Xr = reinterpret_cast<float2 *>(smem_raw);   // [rows][n1]
+  float2 *Xc = Xr + rows * n1;                          // [n2][cols]
+  const int c = (int)cluster.block_rank();
+  const int sl = blockIdx.x / C;
+  const int l = slabs[sl].l;
+  double2 *P = psi + (int64_t)sl * g.npt;
+  const int r0 = c * rows, k0 = c * cols;
+  const int n = rows * n1;   // == n2 * cols
+
+  // 1. rows -> Xr (FP32), rotational phase before the forward transform
+  {
+    double2 raw[MAXV];
+#pragma unroll
+    for (int u = 0; u < MAXV; u++) {
+      const int e = threadIdx.x + FFT_THREADS * u;
+      raw[u] = e < n ? P[(int64_t)r0 * n1 + e] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < MAXV; u++) {
+      const int e = threadIdx.x + FFT_THREADS * u;
+      if (e >= n) break;
+      float x = d2f_rn(raw[u].x), y = d2f_rn(raw[u].y);
+      if (lf.proR) {
+        const int rl = (int)fdiv(r1d.fn, (uint32_t)e);
+        const int i = e - rl * n1;
+        lift2(x, y, __ldg(lf.proR + (int64_t)l * n1 + i));
+        lift2(x, y, __ldg(lf.pror + (int64_t)l * n2 + r0 + rl));
+      }
+      Xr[e] = make_float2(x, y);
+    }
+  }
+  __syncthreads();
+  fft_run<float, false>(Xr, r1d, rows, n1, 1, tw1, false, r1d.fn);
+  cluster.sync();
+  // 2. gather the columns of this CTA from every CTA's rows
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int t = (int)fdiv(fcols, (uint32_t)e), cc = e - t * cols;   // row t (r index), column k0 + cc
+    const int owner = t / rows;
+    const float2 *src = cluster.map_shared_rank(Xr, owner);
+    Xc[e] = src[(t - owner * rows) * n1 + k0 + cc];
+  }
+  __syncthreads();
+  fft_run<float, true>(Xc, r2d, cols, 1, cols, tw2, false, fcols);
+  float kef = 0.0f;
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int t = (int)fdiv(fcols, (uint32_t)e), cc = e - t * cols;
+    float x = Xc[e].x, y = Xc[e].y;
+    lift2(x, y, __ldg(lf.kinR + k0 + cc));
+    lift2(x, y, __ldg(lf.kinr + t));
+    kef = fmaf(__ldg(lf.T1f + k0 + cc) + __ldg(lf.T2f + t), x * x + y * y, kef);
+    Xc[e] = make_float2(x, y);
+  }
+  __syncthreads();
+  fft_run<float, true>(Xc, r2d, cols, 1, cols, tw2, true, fcols);
+  cluster.sync();   // every CTA has finished reading the rows it gathered
+  // 3. scatter the columns back into the owners' rows
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int t = (int)fdiv(fcols, (uint32_t)e), cc = e - t * cols;
+    const int owner = t / rows;
+    float2 *dst = cluster.map_shared_rank(Xr, owner);
+    dst[(t - owner * rows) * n1 + k0 + cc] = Xc[e];
+  }
+  cluster.sync();   // every scatter into this CTA's rows has landed
+  fft_run<float, false>(Xr, r1d, rows, n1, 1, tw1, true, r1d.fn);
+  // 4. scale, rotational phase after the inverse transform, rotational energy, store
+  float ref = 0.0f;
+  const float s2 = fscale != 0.0f ? 1.0f : (float)(scale * scale);
+  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+    const int rl = (int)fdiv(r1d.fn, (uint32_t)e);
+    const int i = e - rl * n1, j = r0 + rl;
+    float x = Xr[e].x, y = Xr[e].y;
+    if (fscale != 0.0f) {
+      x *= fscale;
+      y *= fscale;
+    }
+    if (lf.epiR) {
+      lift2(x, y, __ldg(lf.epiR + (int64_t)l * n1 + i));
+      lift2(x, y, __ldg(lf.epir + (int64_t)l * n2 + j));
+    }
+    if (re_part) {
+      const float Rr = (float)(g.left1 + i * g.dr1), rr = (float)(g.left2 + j * g.dr2);
+      const float I = 1.0f / (2.0f * (float)g.m1 * Rr * Rr) + 1.0f / (2.0f * (float)g.m2 * rr * rr);
+      ref = fmaf((float)l * (float)(l + 1) * I * s2, x * x + y * y, ref);
+    }
+    P[(int64_t)r0 * n1 + e] = fscale != 0.0f ? make_double2(f2d(x), f2d(y)) : make_double2(f2d(x) * scale, f2d(y) * scale);
+  }
+  const double ke = block_sum((double)kef, red);
+  const double re = block_sum((double)ref, red);
+  if (threadIdx.x == 0) {
+    if (ke_part) ke_part[(int64_t)sl * C + c] = ke;
+    if (re_part) re_part[(int64_t)sl * C + c] = re;
+  }
+}
+
 // ------------------------------------------------------------- host side
 bool fft_factor(int n, int *rad, int *nst) {
   int k = 0;
@@ -394,6 +507,20 @@ static int largest_divisor_at_most(int n, int cap) {
   return 1;
 }
 
+// Cluster size of the single-pass FP32 slab FFT: the smallest C in {1,2,4,8}
+// dividing n1 and n2 whose two FP32 buffers (2 n1 n2 / C * 8 bytes) fit in
+// 100 KB and whose per-thread stage load stays within MAXV; 0 = not usable.
+static int choose_cluster(int n1, int n2) {
+  for (int C = 1; C <= 8; C *= 2) {
+    if (n1 % C || n2 % C) continue;
+    const int64_t per = (int64_t)n1 * n2 / C;
+    if (per * 8 * 2 > 100 * 1024) continue;
+    if (per > (int64_t)FFT_THREADS * MAXV) continue;
+    return C;
+  }
+  return 0;
+}
+
 void fft_plan_init(FFTPlan &p, int n1, int n2) {
   p.n1 = n1;
   p.n2 = n2;
@@ -401,6 +528,7 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
     throw Error{QD_ERR_UNSUPPORTED, "FFT grid sizes must factor into 2 and 3"};
   if (n1 > FFT_THREADS * MAXV || n2 > FFT_THREADS * MAXV)
     throw Error{QD_ERR_UNSUPPORTED, "FFT grid size above 4096"};
+  p.cluster = choose_cluster(n1, n2);
   p.rows_per_cta = largest_divisor_at_most(n2, std::max(1, FFT_THREADS * MAXV / n1));
   p.rows_per_cta = std::min(p.rows_per_cta, largest_divisor_at_most(n2, 64));
   p.cols_per_cta = largest_divisor_at_most(n1, std::min(32, std::max(1, FFT_THREADS * MAXV / n2)));
@@ -429,6 +557,9 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
   QD_CUDA(cudaFuncSetAttribute(k_fft_cols<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   QD_CUDA(cudaFuncSetAttribute(k_fft_rows<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   QD_CUDA(cudaFuncSetAttribute(k_fft_cols<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  QD_CUDA(cudaFuncSetAttribute(k_fft_slab_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  if (p.cluster > 1)
+    QD_CUDA(cudaFuncSetAttribute(k_fft_slab_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 0));
 }
 
 void fft_plan_free(FFTPlan &p) {
@@ -440,8 +571,16 @@ void fft_plan_free(FFTPlan &p) {
   p.tw1_f = p.tw2_f = nullptr;
 }
 
-int fft_col_tiles(const FFTPlan &p) { return p.n1 / p.cols_per_cta; }
-int fft_row_tiles(const FFTPlan &p) { return p.n2 / p.rows_per_cta; }
+// partial-sum tiles per slab: the single-pass FP32 form writes one per CTA of
+// the cluster, the three-pass forms one per column / row tile
+int fft_col_tiles(const FFTPlan &p, int precision) {
+  return (precision == QD_PRECISION_MIXED && p.cluster) ? p.cluster : p.n1 / p.cols_per_cta;
+}
+int fft_row_tiles(const FFTPlan &p, int precision) {
+  return (precision == QD_PRECISION_MIXED && p.cluster) ? p.cluster : p.n2 / p.rows_per_cta;
+}
+
+
 
 template <typename R>
 static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j,
@@ -474,18 +613,37 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
   const double scale = 1.0 / ((double)g.n1 * g.n2);
   const bool pow2 = ((g.n1 * g.n2) & (g.n1 * g.n2 - 1)) == 0;
   const float fscale = pow2 ? (float)scale : 0.0f;
+  if (std::is_same<R, float>::value && p.cluster && lf && lf->kinR) {
+    const int C = p.cluster;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(n_slabs * C));
+    cfg.blockDim = dim3(FFT_THREADS);
+    cfg.dynamicSmemBytes = (size_t)2 * g.n1 * g.n2 / C * sizeof(float2);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    QD_CUDA(cudaLaunchKernelEx(&cfg, k_fft_slab_cluster, psi_j, r1, r2, C, g, slabs, p.tw1_f, p.tw2_f, *lf, ke_part,
+                               re_part, fscale, scale, make_fastdiv((uint32_t)(g.n1 / C)), status));
+    prof_mark(s, "fft_slab");
+    return;
+  }
   k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 0, g, 1.0, slabs,
                                                         nullptr, nullptr, 0, status, lf ? lf->proR : nullptr,
                                                         lf ? lf->pror : nullptr, 0.0f, fn2);
   prof_mark(s, "fft_rows_forward");
   const unsigned ncol_ctas = (unsigned)(n_slabs * (p.n1 / p.cols_per_cta));
   k_fft_cols<R><<<ncol_ctas, FFT_THREADS, sm_cols, s>>>(psi_j, r2, p.cols_per_cta, g, tw2, tab_kin, T1, T2, ke_part,
-                                                        fft_col_tiles(p), status, lf ? lf->kinR : nullptr,
+                                                        fft_col_tiles(p, QD_PRECISION_FP64), status, lf ? lf->kinR : nullptr,
                                                         lf ? lf->kinr : nullptr, lf ? lf->T1f : nullptr,
                                                         lf ? lf->T2f : nullptr, fncols);
   prof_mark(s, "fft_cols_kinetic");
   k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 1, g, scale, slabs,
-                                                        tabE, re_part, fft_row_tiles(p), status,
+                                                        tabE, re_part, fft_row_tiles(p, QD_PRECISION_FP64), status,
                                                         lf ? lf->epiR : nullptr, lf ? lf->epir : nullptr, fscale, fn2);
   prof_mark(s, "fft_rows_inverse");
 }

@@ -770,8 +770,8 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
 
   // energies and partials
   s->t_modpe = s->precision == QD_PRECISION_MIXED ? legendre_tc_part_tiles(g) : legendre_bwd_part_tiles(g);
-  s->t_ke = fft_col_tiles(s->fft);
-  s->t_re = s->any_coupled ? 16 : fft_row_tiles(s->fft);
+  s->t_ke = fft_col_tiles(s->fft, s->precision);
+  s->t_re = s->any_coupled ? 16 : fft_row_tiles(s->fft, s->precision);
   s->t_ce = coriolis_tiles(g);
   s->part_modpe = dalloc<double>((size_t)s->n_blocks * s->t_modpe * 2);
   s->part_ke = dalloc<double>((size_t)s->n_slabs * s->t_ke);

@@ -117,6 +117,7 @@ struct FFTPlan {
   double2 *tw2_d;  float2 *tw2_f;
   int rows_per_cta;
   int cols_per_cta;
+  int cluster;   // CTAs per slab of the single-pass FP32 FFT (0: three-pass form)
 };
 // FP32 three-shear phase tables of the mixed form (float2 (t, s) per entry,
 // see lift tables below); null entries are skipped.
@@ -136,8 +137,8 @@ void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, int pre
                         const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1,
                         const double *T2, double *ke_part, const double2 *tabE, const double *I1,
                         const double *I2, double *re_part, const int *status, const FFTLift *lift = nullptr);
-int fft_col_tiles(const FFTPlan &p);
-int fft_row_tiles(const FFTPlan &p);
+int fft_col_tiles(const FFTPlan &p, int precision);
+int fft_row_tiles(const FFTPlan &p, int precision);
 
 // rotational energy partials only (for stage-by-stage use)
 void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, const SlabDesc *slabs,
