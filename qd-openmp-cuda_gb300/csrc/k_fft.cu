@@ -84,12 +84,12 @@ __device__ inline void dft(typename CT<R>::T *v, bool inv) {
 // One Stockham stage on nrows independent transforms of length N stored at
 // buf[row*rs + x*es].  COLS selects which index varies fastest across threads
 // so that shared-memory accesses stay contiguous.
-template <typename R, int RAD, bool COLS>
+template <typename R, int RAD, bool COLS, int THREADS = FFT_THREADS, int MV = MAXV>
 __device__ inline void fft_stage(typename CT<R>::T *buf, int N, int nrows, int rs, int es, int Ns,
                                  const typename CT<R>::T *__restrict__ tw, bool inv, const FastDiv &fnbf,
                                  const FastDiv &fNs, const FastDiv &frows) {
   using C = typename CT<R>::T;
-  constexpr int NB = (MAXV + RAD - 1) / RAD;
+  constexpr int NB = (MV + RAD - 1) / RAD;
   const int nbf = N / RAD;
   const int total = nrows * nbf;
   const int tstep = N / (Ns * RAD);
@@ -97,7 +97,7 @@ __device__ inline void fft_stage(typename CT<R>::T *buf, int N, int nrows, int r
   int dst_base[NB];
 #pragma unroll
   for (int q = 0; q < NB; q++) {
-    const int t = threadIdx.x + FFT_THREADS * q;
+    const int t = threadIdx.x + THREADS * q;
     if (t < total) {
       int row, jj;
       if (COLS) {
@@ -146,7 +146,7 @@ __device__ inline void fft_stage(typename CT<R>::T *buf, int N, int nrows, int r
   __syncthreads();
 #pragma unroll
   for (int q = 0; q < NB; q++) {
-    const int t = threadIdx.x + FFT_THREADS * q;
+    const int t = threadIdx.x + THREADS * q;
     if (t < total) {
 #pragma unroll
       for (int r = 0; r < RAD; r++) buf[dst_base[q] + r * Ns * es] = v[q][r];
@@ -164,15 +164,18 @@ struct Radices {
   FastDiv fn;        // n
 };
 
-template <typename R, bool COLS>
+template <typename R, bool COLS, int THREADS = FFT_THREADS, int MV = MAXV>
 __device__ inline void fft_run(typename CT<R>::T *buf, const Radices &rd, int nrows, int rs, int es,
                                const typename CT<R>::T *__restrict__ tw, bool inv, const FastDiv &frows) {
   int Ns = 1;
   for (int s = 0; s < rd.nst; s++) {
     const int rad = rd.rad[s];
-    if (rad == 4) fft_stage<R, 4, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
-    else if (rad == 2) fft_stage<R, 2, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
-    else fft_stage<R, 3, COLS>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
+    if (rad == 4)
+      fft_stage<R, 4, COLS, THREADS, MV>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
+    else if (rad == 2)
+      fft_stage<R, 2, COLS, THREADS, MV>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
+    else
+      fft_stage<R, 3, COLS, THREADS, MV>(buf, rd.n, nrows, rs, es, Ns, tw, inv, rd.nbf[s], rd.ns[s], frows);
     Ns *= rad;
   }
 }
@@ -386,7 +389,10 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
 // kR in [c n1/C, (c+1) n1/C) in Xc; the exchange reads and writes the other
 // CTAs' shared memory directly (distributed shared memory).  HBM sees one read
 // and one write per point instead of three of each.
-__global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_slab_cluster(
+constexpr int SLAB_THREADS = 512;
+constexpr int SLAB_MV = 8;   // values per thread per stage: n1 n2 / C <= 4096
+
+__global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
     double2 *__restrict__ psi, Radices r1d, Radices r2d, int C, Grid g, const SlabDesc *__restrict__ slabs,
     const float2 *__restrict__ tw1, const float2 *__restrict__ tw2, FFTLift lf, double *__restrict__ ke_part,
     double *__restrict__ re_part, float fscale, double scale, FastDiv fcols, const int *status) {
@@ -404,18 +410,19 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_slab_cluster(
   double2 *P = psi + (int64_t)sl * g.npt;
   const int r0 = c * rows, k0 = c * cols;
   const int n = rows * n1;   // == n2 * cols
+  const int tid = threadIdx.x;
 
   // 1. rows -> Xr (FP32), rotational phase before the forward transform
   {
-    double2 raw[MAXV];
+    double2 raw[SLAB_MV];
 #pragma unroll
-    for (int u = 0; u < MAXV; u++) {
-      const int e = threadIdx.x + FFT_THREADS * u;
+    for (int u = 0; u < SLAB_MV; u++) {
+      const int e = tid + SLAB_THREADS * u;
       raw[u] = e < n ? P[(int64_t)r0 * n1 + e] : make_double2(0.0, 0.0);
     }
 #pragma unroll
-    for (int u = 0; u < MAXV; u++) {
-      const int e = threadIdx.x + FFT_THREADS * u;
+    for (int u = 0; u < SLAB_MV; u++) {
+      const int e = tid + SLAB_THREADS * u;
       if (e >= n) break;
       float x = d2f_rn(raw[u].x), y = d2f_rn(raw[u].y);
       if (lf.proR) {
@@ -428,19 +435,31 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_slab_cluster(
     }
   }
   __syncthreads();
-  fft_run<float, false>(Xr, r1d, rows, n1, 1, tw1, false, r1d.fn);
+  fft_run<float, false, SLAB_THREADS, SLAB_MV>(Xr, r1d, rows, n1, 1, tw1, false, r1d.fn);
   cluster.sync();
-  // 2. gather the columns of this CTA from every CTA's rows
-  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
-    const int t = (int)fdiv(fcols, (uint32_t)e), cc = e - t * cols;   // row t (r index), column k0 + cc
-    const int owner = t / rows;
-    const float2 *src = cluster.map_shared_rank(Xr, owner);
-    Xc[e] = src[(t - owner * rows) * n1 + k0 + cc];
+  // 2. gather the columns of this CTA from every CTA's rows (all loads issued first)
+  {
+    float2 v[SLAB_MV];
+#pragma unroll
+    for (int u = 0; u < SLAB_MV; u++) {
+      const int e = tid + SLAB_THREADS * u;
+      if (e < n) {
+        const int t = (int)fdiv(fcols, (uint32_t)e), cc = e - t * cols;
+        const int owner = t / rows;
+        const float2 *src = cluster.map_shared_rank(Xr, owner);
+        v[u] = src[(t - owner * rows) * n1 + k0 + cc];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < SLAB_MV; u++) {
+      const int e = tid + SLAB_THREADS * u;
+      if (e < n) Xc[e] = v[u];
+    }
   }
   __syncthreads();
-  fft_run<float, true>(Xc, r2d, cols, 1, cols, tw2, false, fcols);
+  fft_run<float, true, SLAB_THREADS, SLAB_MV>(Xc, r2d, cols, 1, cols, tw2, false, fcols);
   float kef = 0.0f;
-  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+  for (int e = tid; e < n; e += SLAB_THREADS) {
     const int t = (int)fdiv(fcols, (uint32_t)e), cc = e - t * cols;
     float x = Xc[e].x, y = Xc[e].y;
     lift2(x, y, __ldg(lf.kinR + k0 + cc));
@@ -449,21 +468,21 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_slab_cluster(
     Xc[e] = make_float2(x, y);
   }
   __syncthreads();
-  fft_run<float, true>(Xc, r2d, cols, 1, cols, tw2, true, fcols);
+  fft_run<float, true, SLAB_THREADS, SLAB_MV>(Xc, r2d, cols, 1, cols, tw2, true, fcols);
   cluster.sync();   // every CTA has finished reading the rows it gathered
   // 3. scatter the columns back into the owners' rows
-  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+  for (int e = tid; e < n; e += SLAB_THREADS) {
     const int t = (int)fdiv(fcols, (uint32_t)e), cc = e - t * cols;
     const int owner = t / rows;
     float2 *dst = cluster.map_shared_rank(Xr, owner);
     dst[(t - owner * rows) * n1 + k0 + cc] = Xc[e];
   }
   cluster.sync();   // every scatter into this CTA's rows has landed
-  fft_run<float, false>(Xr, r1d, rows, n1, 1, tw1, true, r1d.fn);
+  fft_run<float, false, SLAB_THREADS, SLAB_MV>(Xr, r1d, rows, n1, 1, tw1, true, r1d.fn);
   // 4. scale, rotational phase after the inverse transform, rotational energy, store
   float ref = 0.0f;
   const float s2 = fscale != 0.0f ? 1.0f : (float)(scale * scale);
-  for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
+  for (int e = tid; e < n; e += SLAB_THREADS) {
     const int rl = (int)fdiv(r1d.fn, (uint32_t)e);
     const int i = e - rl * n1, j = r0 + rl;
     float x = Xr[e].x, y = Xr[e].y;
@@ -484,7 +503,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_slab_cluster(
   }
   const double ke = block_sum((double)kef, red);
   const double re = block_sum((double)ref, red);
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     if (ke_part) ke_part[(int64_t)sl * C + c] = ke;
     if (re_part) re_part[(int64_t)sl * C + c] = re;
   }
@@ -515,7 +534,7 @@ static int choose_cluster(int n1, int n2) {
     if (n1 % C || n2 % C) continue;
     const int64_t per = (int64_t)n1 * n2 / C;
     if (per * 8 * 2 > 100 * 1024) continue;
-    if (per > (int64_t)FFT_THREADS * MAXV) continue;
+    if (per > (int64_t)SLAB_THREADS * SLAB_MV) continue;
     return C;
   }
   return 0;
@@ -617,7 +636,7 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
     const int C = p.cluster;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)(n_slabs * C));
-    cfg.blockDim = dim3(FFT_THREADS);
+    cfg.blockDim = dim3(SLAB_THREADS);
     cfg.dynamicSmemBytes = (size_t)2 * g.n1 * g.n2 / C * sizeof(float2);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
