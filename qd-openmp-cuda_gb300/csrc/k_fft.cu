@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
   fft_run<float, false, SLAB_THREADS, SLAB_MV>(Xr, r1d, rows, n1, 1, tw1, true, r1d.fn);
   // 4. scale, rotational phase after the inverse transform, rotational energy, store
   float ref = 0.0f;
-  const float s2 = fscale != 0.0f ? 1.0f : (float)(scale * scale);
+  const float lls2 = (float)l * (float)(l + 1) * (fscale != 0.0f ? 1.0f : (float)(scale * scale));
   for (int e = tid; e < n; e += SLAB_THREADS) {
     const int rl = (int)fdiv(r1d.fn, (uint32_t)e);
     const int i = e - rl * n1, j = r0 + rl;
@@ -495,9 +495,8 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
       lift2(x, y, __ldg(lf.epir + (int64_t)l * n2 + j));
     }
     if (re_part) {
-      const float Rr = (float)(g.left1 + i * g.dr1), rr = (float)(g.left2 + j * g.dr2);
-      const float I = 1.0f / (2.0f * (float)g.m1 * Rr * Rr) + 1.0f / (2.0f * (float)g.m2 * rr * rr);
-      ref = fmaf((float)l * (float)(l + 1) * I * s2, x * x + y * y, ref);
+      const float I = __ldg(lf.I1f + i) + __ldg(lf.I2f + j);
+      ref = fmaf(lls2 * I, x * x + y * y, ref);
     }
     P[(int64_t)r0 * n1 + e] = fscale != 0.0f ? make_double2(f2d(x), f2d(y)) : make_double2(f2d(x) * scale, f2d(y) * scale);
   }

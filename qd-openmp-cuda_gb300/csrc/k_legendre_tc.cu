@@ -244,6 +244,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
   unsigned char *sA = smem;
   unsigned char *sB = smem + 3 * A_TERM;
   float *sF = reinterpret_cast<float *>(sB + 3 * B_TERM);
+  float *sWV = sF + 128 * LDF;   // backward: w_k V(k, p) of the tile, [k][64]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t p0 = (int64_t)blockIdx.x * TC_POINTS;
   const uint32_t ncols = tc_tmem_cols(Np);
@@ -254,6 +255,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
 
+  // ---- backward: w_k V(k, p) of the tile, needed by the epilogue
+  if (!FWD) {
+    for (int q = tid; q < Np * TC_POINTS; q += TC_THREADS) {
+      const int k = q / TC_POINTS, pl2 = q % TC_POINTS;
+      const int64_t p = p0 + pl2;
+      sWV[q] = (k < Nv && p < g.npt) ? __ldg(P.wv + (int64_t)k * g.npt + p) : 0.0f;
+    }
+  }
   // ---- B image -> shared memory
   {
     const uint4 *src = reinterpret_cast<const uint4 *>(P.bimg + P.bimg_off[blockIdx.y] / 2);
@@ -412,7 +421,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
         Cd[2 * (((int64_t)blockIdx.y * g.nth + n) * g.npt + p) + c] = f2d(v);
         const float v2 = v * v;
         mod = fmaf(__ldg(P.w + n), v2, mod);
-        pe = fmaf(__ldg(P.wv + (int64_t)n * g.npt + p), v2, pe);
+        pe = fmaf(sWV[n * TC_POINTS + pl], v2, pe);
       }
     }
   }
@@ -437,7 +446,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
 // on an SM (233472 bytes of shared memory), so the TMEM columns that their
 // allocations need never exceed the SM's 512.
 size_t tc_smem_bytes(int Kp, int Np) {
-  const size_t need = (size_t)3 * 16 * (Kp / 8 * 128) + (size_t)tc_bimg_bytes(Np, Kp) + (size_t)128 * (Kp + 1) * 4;
+  const size_t need = (size_t)3 * 16 * (Kp / 8 * 128) + (size_t)tc_bimg_bytes(Np, Kp) + (size_t)128 * (Kp + 1) * 4 +
+                      (size_t)Np * TC_POINTS * 4;
   const size_t ctas = 512 / tc_tmem_cols(Np);
   return std::max(need, (size_t)233472 / (ctas + 1) + 1024);
 }

@@ -175,7 +175,8 @@ void launch_build_lift_kin(cudaStream_t s, int n, const double *T, double dt, fl
 __global__ void k_build_float_tables(Grid g, const double *__restrict__ w, const double *__restrict__ pot,
                                      const double *__restrict__ d1, const double *__restrict__ d2,
                                      const double *__restrict__ T1, const double *__restrict__ T2, float *wf,
-                                     float *wvf, float *d1f, float *d2f, float *T1f, float *T2f) {
+                                     float *wvf, float *d1f, float *d2f, float *T1f, float *T2f, float *I1f,
+                                     float *I2f) {
   const int64_t n = g.npt * g.nth;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(q / g.npt);
@@ -183,10 +184,14 @@ __global__ void k_build_float_tables(Grid g, const double *__restrict__ w, const
     if (q < g.nth) wf[q] = (float)w[q];
     if (q < g.n1) {
       T1f[q] = (float)T1[q];
+      const double R = g.left1 + (double)q * g.dr1;
+      I1f[q] = (float)(1.0 / (2.0 * g.m1 * R * R));
       if (d1f) d1f[q] = (float)d1[q];
     }
     if (q < g.n2) {
       T2f[q] = (float)T2[q];
+      const double r = g.left2 + (double)q * g.dr2;
+      I2f[q] = (float)(1.0 / (2.0 * g.m2 * r * r));
       if (d2f) d2f[q] = (float)d2[q];
     }
   }
@@ -194,9 +199,10 @@ __global__ void k_build_float_tables(Grid g, const double *__restrict__ w, const
 
 void launch_build_float_tables(cudaStream_t s, const Grid &g, const double *w, const double *pot, const double *d1,
                                const double *d2, const double *T1, const double *T2, float *wf, float *wvf,
-                               float *d1f, float *d2f, float *T1f, float *T2f) {
+                               float *d1f, float *d2f, float *T1f, float *T2f, float *I1f, float *I2f) {
   const int64_t n = g.npt * g.nth;
-  k_build_float_tables<<<grid_for(n, 256), 256, 0, s>>>(g, w, pot, d1, d2, T1, T2, wf, wvf, d1f, d2f, T1f, T2f);
+  k_build_float_tables<<<grid_for(n, 256), 256, 0, s>>>(g, w, pot, d1, d2, T1, T2, wf, wvf, d1f, d2f, T1f, T2f, I1f,
+                                                       I2f);
 }
 
 // ------------------------------------------------------------ energies

@@ -290,6 +290,7 @@ struct qd_session {
   size_t smem_f = 0, smem_b = 0;
   float2 *vph = nullptr, *vph0 = nullptr, *lrotR = nullptr, *lrotr = nullptr, *lkinR = nullptr, *lkinr = nullptr;
   float *wf = nullptr, *wvf = nullptr, *d1f = nullptr, *d2f = nullptr, *T1f = nullptr, *T2f = nullptr;
+  float *I1f = nullptr, *I2f = nullptr;
   int steps = 0;   // host mirror of time.steps
   int launches_per_step = 0;
   cudaGraphExec_t graph_chunk = nullptr;
@@ -373,7 +374,7 @@ qd_session::~qd_session() {
                   part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
                   flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
                   img_f, img_b, bscale_f, bscale_b, imgoff_f, imgoff_b, vph, vph0, lrotR, lrotr, lkinR, lkinr, wf, wvf, d1f, d2f,
-                  T1f, T2f};
+                  T1f, T2f, I1f, I2f};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   fft_plan_free(fft);
@@ -448,6 +449,8 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
   lf.kinr = s->lkinr;
   lf.T1f = s->T1f;
   lf.T2f = s->T2f;
+  lf.I1f = s->I1f;
+  lf.I2f = s->I2f;
   launch_fft_kinetic(st, g, s->fft, QD_PRECISION_MIXED, s->psi_j, s->d_slabs, s->n_slabs, nullptr, s->T1, s->T2,
                      s->part_ke, nullptr, s->I1, s->I2, s->any_coupled ? nullptr : s->part_re, s->status, &lf);
   if (s->any_coupled) {
@@ -640,12 +643,14 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   s->wvf = dalloc<float>((size_t)nth_pt);
   s->T1f = dalloc<float>((size_t)g.n1);
   s->T2f = dalloc<float>((size_t)g.n2);
+  s->I1f = dalloc<float>((size_t)g.n1);
+  s->I2f = dalloc<float>((size_t)g.n2);
   if (s->has_mask) {
     s->d1f = dalloc<float>((size_t)g.n1);
     s->d2f = dalloc<float>((size_t)g.n2);
   }
   launch_build_float_tables(st, g, s->w, s->pot, s->d1, s->d2, s->T1, s->T2, s->wf, s->wvf, s->d1f, s->d2f, s->T1f,
-                            s->T2f);
+                            s->T2f, s->I1f, s->I2f);
   if (!fp64) {
     s->vph = dalloc<float2>((size_t)nth_pt);
     s->vph0 = dalloc<float2>((size_t)nth_pt);
@@ -1166,6 +1171,8 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
           lf.kinr = kr;
           lf.T1f = s->T1f;
           lf.T2f = s->T2f;
+          lf.I1f = s->I1f;
+          lf.I2f = s->I2f;
         }
         launch_fft_kinetic(st, g, s->fft, s->precision, s->psi_j, s->d_slabs, s->n_slabs, tab, s->T1, s->T2,
                            s->part_ke, nullptr, s->I1, s->I2, nullptr, s->status, &lf);

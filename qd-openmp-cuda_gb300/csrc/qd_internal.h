@@ -126,6 +126,7 @@ struct FFTLift {
   const float2 *epiR, *epir;   // after the inverse transform
   const float2 *kinR, *kinr;   // [n1], [n2]: kinetic phase
   const float *T1f, *T2f;      // kinetic energy tables in FP32
+  const float *I1f, *I2f;      // 1/(2 m R^2), 1/(2 m r^2) in FP32 (rotational energy)
 };
 bool fft_factor(int n, int *rad, int *nst);
 void fft_plan_init(FFTPlan &p, int n1, int n2);
@@ -201,7 +202,7 @@ void launch_build_lift_rot(cudaStream_t s, int n, int l_max, double left, double
 void launch_build_lift_kin(cudaStream_t s, int n, const double *T, double dt, float2 *out);
 void launch_build_float_tables(cudaStream_t s, const Grid &g, const double *w, const double *pot, const double *d1,
                                const double *d2, const double *T1, const double *T2, float *wf, float *wvf,
-                               float *d1f, float *d2f, float *T1f, float *T2f);
+                               float *d1f, float *d2f, float *T1f, float *T2f, float *I1f, float *I2f);
 
 // tcgen05 BF16x3 Legendre contraction
 struct TcArgs;
