@@ -404,6 +404,10 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
   const int rows = n2 / C, cols = n1 / C;
   float2 *Xr = reinterpret_cast<float2 *>(smem_raw);   // [rows][n1]
   float2 *Xc = Xr + rows * n1;                          // [n2][cols]
+  float2 *tws1 = Xc + n2 * cols;                        // twiddle shears of n1 and n2
+  float2 *tws2 = tws1 + n1;
+  for (int q = threadIdx.x; q < n1; q += SLAB_THREADS) tws1[q] = __ldg(tw1 + q);
+  for (int q = threadIdx.x; q < n2; q += SLAB_THREADS) tws2[q] = __ldg(tw2 + q);
   const int c = (int)cluster.block_rank();
   const int sl = blockIdx.x / C;
   const int l = slabs[sl].l;
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
 #pragma unroll
     for (int u = 0; u < SLAB_MV; u++) {
       const int e = tid + SLAB_THREADS * u;
-      raw[u] = e < n ? P[(int64_t)r0 * n1 + e] : make_double2(0.0, 0.0);
+      raw[u] = e < n ? __ldcs(P + (int64_t)r0 * n1 + e) : make_double2(0.0, 0.0);
     }
 #pragma unroll
     for (int u = 0; u < SLAB_MV; u++) {
@@ -435,7 +439,7 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
     }
   }
   __syncthreads();
-  fft_run<float, false, SLAB_THREADS, SLAB_MV>(Xr, r1d, rows, n1, 1, tw1, false, r1d.fn);
+  fft_run<float, false, SLAB_THREADS, SLAB_MV>(Xr, r1d, rows, n1, 1, tws1, false, r1d.fn);
   cluster.sync();
   // 2. gather the columns of this CTA from every CTA's rows (all loads issued first)
   {
@@ -457,7 +461,7 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
     }
   }
   __syncthreads();
-  fft_run<float, true, SLAB_THREADS, SLAB_MV>(Xc, r2d, cols, 1, cols, tw2, false, fcols);
+  fft_run<float, true, SLAB_THREADS, SLAB_MV>(Xc, r2d, cols, 1, cols, tws2, false, fcols);
   float kef = 0.0f;
   for (int e = tid; e < n; e += SLAB_THREADS) {
     const int t = (int)fdiv(fcols, (uint32_t)e), cc = e - t * cols;
@@ -468,7 +472,7 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
     Xc[e] = make_float2(x, y);
   }
   __syncthreads();
-  fft_run<float, true, SLAB_THREADS, SLAB_MV>(Xc, r2d, cols, 1, cols, tw2, true, fcols);
+  fft_run<float, true, SLAB_THREADS, SLAB_MV>(Xc, r2d, cols, 1, cols, tws2, true, fcols);
   cluster.sync();   // every CTA has finished reading the rows it gathered
   // 3. scatter the columns back into the owners' rows
   for (int e = tid; e < n; e += SLAB_THREADS) {
@@ -478,7 +482,7 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
     dst[(t - owner * rows) * n1 + k0 + cc] = Xc[e];
   }
   cluster.sync();   // every scatter into this CTA's rows has landed
-  fft_run<float, false, SLAB_THREADS, SLAB_MV>(Xr, r1d, rows, n1, 1, tw1, true, r1d.fn);
+  fft_run<float, false, SLAB_THREADS, SLAB_MV>(Xr, r1d, rows, n1, 1, tws1, true, r1d.fn);
   // 4. scale, rotational phase after the inverse transform, rotational energy, store
   float ref = 0.0f;
   const float lls2 = (float)l * (float)(l + 1) * (fscale != 0.0f ? 1.0f : (float)(scale * scale));
@@ -498,7 +502,8 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
       const float I = __ldg(lf.I1f + i) + __ldg(lf.I2f + j);
       ref = fmaf(lls2 * I, x * x + y * y, ref);
     }
-    P[(int64_t)r0 * n1 + e] = fscale != 0.0f ? make_double2(f2d(x), f2d(y)) : make_double2(f2d(x) * scale, f2d(y) * scale);
+    __stcs(P + (int64_t)r0 * n1 + e,
+           fscale != 0.0f ? make_double2(f2d(x), f2d(y)) : make_double2(f2d(x) * scale, f2d(y) * scale));
   }
   const double ke = block_sum((double)kef, red);
   const double re = block_sum((double)ref, red);
@@ -532,7 +537,7 @@ static int choose_cluster(int n1, int n2) {
   for (int C = 1; C <= 8; C *= 2) {
     if (n1 % C || n2 % C) continue;
     const int64_t per = (int64_t)n1 * n2 / C;
-    if (per * 8 * 2 > 100 * 1024) continue;
+    if ((per * 2 + n1 + n2) * 8 > 100 * 1024) continue;
     if (per > (int64_t)SLAB_THREADS * SLAB_MV) continue;
     return C;
   }
@@ -636,7 +641,7 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)(n_slabs * C));
     cfg.blockDim = dim3(SLAB_THREADS);
-    cfg.dynamicSmemBytes = (size_t)2 * g.n1 * g.n2 / C * sizeof(float2);
+    cfg.dynamicSmemBytes = ((size_t)2 * g.n1 * g.n2 / C + g.n1 + g.n2) * sizeof(float2);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;

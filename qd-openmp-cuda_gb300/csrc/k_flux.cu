@@ -51,6 +51,56 @@ void launch_flux_extract(cudaStream_t s, const Grid &g, const FluxConfig &f, con
   k_flux_extract<<<grid, 256, 0, s>>>(g, f.n_grad, f.n_ds, psi_th, half_v, fd, buf, n_blocks, slot, status);
 }
 
+// Mixed form of the surface extraction: FP32 arithmetic on the FP64 state
+// (exp(-i V dt/2) as three-shear rotations, FP32 stencil weights), values
+// stored in FP64 for the FP64 accumulation.
+__device__ inline void lift2f(float &x, float &y, float2 ts) {
+  x = fmaf(ts.x, y, x);
+  y = fmaf(ts.y, x, y);
+  x = fmaf(ts.x, y, x);
+  x = fmaf(ts.x, y, x);
+  y = fmaf(ts.y, x, y);
+  x = fmaf(ts.x, y, x);
+}
+
+__global__ void k_flux_extract_f32(Grid g, int n_grad, int n_ds, const double2 *__restrict__ psi_th,
+                                   const float2 *__restrict__ hv, const float *__restrict__ fd,
+                                   double2 *__restrict__ buf, int n_blocks, const int *slot_p, const int *status) {
+  if (status && *status) return;
+  const int slot = *slot_p;
+  const int b = blockIdx.y;
+  const int h = (n_grad - 1) / 2;
+  const int64_t ns = (int64_t)g.nth * g.n1;
+  double2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
+  const double2 *p = psi_th + (int64_t)b * g.nth * g.npt;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= ns) return;
+  const int i = (int)(q % g.n1), k = (int)(q / g.n1);
+  float Ax = 0.0f, Ay = 0.0f, Dx = 0.0f, Dy = 0.0f;
+  for (int gg = 0; gg < n_grad; gg++) {
+    const int j = n_ds - h + gg;
+    const double2 a = p[((int64_t)k * g.n2 + j) * g.n1 + i];
+    float x = d2f_rn(a.x), y = d2f_rn(a.y);
+    lift2f(x, y, __ldg(hv + ((int64_t)k * n_grad + gg) * g.n1 + i));
+    const float c = __ldg(fd + gg);
+    Dx = fmaf(c, x, Dx);
+    Dy = fmaf(c, y, Dy);
+    if (gg == h) {
+      Ax = x;
+      Ay = y;
+    }
+  }
+  out[q] = make_double2(f2d(Ax), f2d(Ay));
+  out[ns + q] = make_double2(f2d(Dx), f2d(Dy));
+}
+
+void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const double2 *psi_th, int n_blocks,
+                             const float2 *half_v, const float *fd, double2 *buf, const int *slot, const int *status) {
+  const int64_t ns = (int64_t)g.nth * g.n1;
+  dim3 grid((unsigned)((ns + 127) / 128), (unsigned)n_blocks);
+  k_flux_extract_f32<<<grid, 128, 0, s>>>(g, f.n_grad, f.n_ds, psi_th, half_v, fd, buf, n_blocks, slot, status);
+}
+
 // phase[n][E] = dt exp(i E (t0 + n dt))
 __global__ void k_flux_phase(const double *__restrict__ E, int nE, int count, double t0, double dt,
                              double2 *__restrict__ phase) {

@@ -172,6 +172,25 @@ void launch_build_lift_kin(cudaStream_t s, int n, const double *T, double dt, fl
   k_build_lift_kin<<<(n + 255) / 256, 256, 0, s>>>(n, T, dt, out);
 }
 
+__global__ void k_build_half_v_lift(Grid g, int n_grad, int n_ds, const double *__restrict__ pot, double dt,
+                                    float2 *__restrict__ hv) {
+  const int h = (n_grad - 1) / 2;
+  const int64_t n = (int64_t)g.nth * n_grad * g.n1;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % g.n1);
+    const int gg = (int)((q / g.n1) % n_grad);
+    const int k = (int)(q / ((int64_t)g.n1 * n_grad));
+    const int j = n_ds - h + gg;
+    hv[q] = lift_coeffs(-0.5 * dt * pot[((int64_t)k * g.n2 + j) * g.n1 + i]);
+  }
+}
+
+void launch_build_half_v_lift(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
+                              float2 *half_v) {
+  const int64_t n = (int64_t)g.nth * f.n_grad * g.n1;
+  k_build_half_v_lift<<<grid_for(n, 256), 256, 0, s>>>(g, f.n_grad, f.n_ds, pot, dt, half_v);
+}
+
 __global__ void k_build_float_tables(Grid g, const double *__restrict__ w, const double *__restrict__ pot,
                                      const double *__restrict__ d1, const double *__restrict__ d2,
                                      const double *__restrict__ T1, const double *__restrict__ T2, float *wf,
@@ -240,8 +259,9 @@ void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, cons
 __global__ void k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__restrict__ blocks,
                                   const int *__restrict__ pblock0, const CoriolisGroup *__restrict__ groups,
                                   const int *__restrict__ pgroup0, int ce_n, double *__restrict__ energies,
-                                  double *__restrict__ rec, const int *__restrict__ d_step, int rec_base,
-                                  int rec_cap, int n_blocks, double norm_tol, int *status, int *status_step) {
+                                  double *__restrict__ rec, int *__restrict__ d_step, int rec_base,
+                                  int rec_cap, int n_blocks, double norm_tol, int *status, int *status_step,
+                                  StepTail tail) {
   if (*status) return;
   __shared__ double red[32];
   const int pr = blockIdx.x;
@@ -305,14 +325,41 @@ __global__ void k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__res
   if (threadIdx.x == 0 && ep.have_mod && total_module > 1.0 + norm_tol) {
     if (atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
   }
+  // End of a full step: the last CTA to finish books this step's flux slot and
+  // advances the step counter (no separate one-thread launches).
+  if (tail.done && threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(tail.done, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      *tail.done = 0u;
+      if (atomicAdd(status, 0) == 0) {
+        if (tail.flux_count) {
+          const int c = *tail.flux_count;
+          if (c >= tail.cap) {
+            atomicCAS(status, 0, QD_ERR_INVALID);
+            *tail.flux_slot = 0;
+          } else {
+            if (c == 0) *tail.flux_t0 = (step + 1) * tail.dt;
+            *tail.flux_slot = c;
+            *tail.flux_count = c + 1;
+          }
+        }
+        *d_step = step + 1;
+      }
+    }
+  }
 }
 
 void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &ep, const BlockDesc *blocks,
                              const int *pblock0, int n_problems, const CoriolisGroup *groups, const int *pgroup0,
                              int ce_n, double *energies, double *rec, const int *d_step, int rec_base, int rec_cap,
-                             double norm_tol, int *status, int *status_step, int n_blocks) {
-  k_energy_finalize<<<n_problems, 256, 0, st>>>(g, ep, blocks, pblock0, groups, pgroup0, ce_n, energies, rec, d_step,
-                                               rec_base, rec_cap, n_blocks, norm_tol, status, status_step);
+                             double norm_tol, int *status, int *status_step, int n_blocks, const StepTail *tail) {
+  StepTail t{};
+  if (tail) t = *tail;
+  k_energy_finalize<<<n_problems, 256, 0, st>>>(g, ep, blocks, pblock0, groups, pgroup0, ce_n, energies, rec,
+                                               const_cast<int *>(d_step), rec_base, rec_cap, n_blocks, norm_tol,
+                                               status, status_step, t);
 }
 
 }  // namespace qd

@@ -281,6 +281,9 @@ struct qd_session {
   double2 *flux_buf = nullptr, *flux_acc = nullptr, *flux_phase = nullptr, *half_v = nullptr;
   double *fd = nullptr, *flux_E = nullptr, *flux_eta = nullptr, *crp = nullptr, *flux_t0 = nullptr;
   int *flux_count = nullptr, *flux_slot = nullptr;
+  unsigned *step_done = nullptr;
+  float2 *half_v_lift = nullptr;
+  float *fdf = nullptr;
   int flux_pending = 0;
   FFTPlan fft{};
   // mixed form: tensor-core Legendre images and FP32 three-shear tables
@@ -374,7 +377,7 @@ qd_session::~qd_session() {
                   part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
                   flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
                   img_f, img_b, bscale_f, bscale_b, imgoff_f, imgoff_b, vph, vph0, lrotR, lrotr, lkinR, lkinr, wf, wvf, d1f, d2f,
-                  T1f, T2f, I1f, I2f};
+                  T1f, T2f, I1f, I2f, step_done, half_v_lift, fdf};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   fft_plan_free(fft);
@@ -510,27 +513,38 @@ static void enqueue_tail(qd_session *s) {
   cudaStream_t st = s->stream;
   const Grid &g = s->g;
   EnergyParts ep = energy_parts(s, true, true, true, s->any_coupled);
+  StepTail tail{};
+  tail.done = s->step_done;
+  if (s->flux.enabled) {
+    tail.flux_count = s->flux_count;
+    tail.flux_slot = s->flux_slot;
+    tail.flux_t0 = s->flux_t0;
+    tail.cap = s->flux.chunk;
+    tail.dt = s->dt;
+  }
   launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                           s->max_group_n, s->energies, s->rec, s->d_step, s->rec_base, s->rec_cap, s->norm_tol,
-                          s->status, s->status_step, s->n_blocks);
+                          s->status, s->status_step, s->n_blocks, &tail);
   prof_mark(st, "energy_finalize");
   if (s->flux.enabled) {
-    k_flux_begin<<<1, 1, 0, st>>>(s->d_step, s->flux_count, s->flux_t0, s->dt, s->flux_slot, s->flux.chunk,
-                                  s->status);
-    const int64_t ns = (int64_t)g.nth * g.n1;
-    dim3 grid((unsigned)((ns + 127) / 128), (unsigned)s->n_blocks);
-    k_flux_extract_dev<<<grid, 128, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
-                                             s->flux_buf, s->n_blocks, s->flux_slot, s->status);
+    if (s->precision == QD_PRECISION_MIXED) {
+      launch_flux_extract_f32(st, g, s->flux, s->psi_th, s->n_blocks, s->half_v_lift, s->fdf, s->flux_buf,
+                              s->flux_slot, s->status);
+    } else {
+      const int64_t ns = (int64_t)g.nth * g.n1;
+      dim3 grid((unsigned)((ns + 127) / 128), (unsigned)s->n_blocks);
+      k_flux_extract_dev<<<grid, 128, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
+                                               s->flux_buf, s->n_blocks, s->flux_slot, s->status);
+    }
     prof_mark(st, "flux_extract");
   }
-  k_step_end<<<1, 1, 0, st>>>(s->d_step, s->status, nullptr, nullptr, 0.0, 0);
-  prof_mark(st, "step_end");
 }
 
 static int count_launches_per_step(qd_session *s) {
-  int n = 1 + 3 + 1 + 1 + 1;   // fwd, fft x3, bwd, finalize, step_end
-  if (s->any_coupled) n += 3;  // coriolis x2, rot energy
-  if (s->flux.enabled) n += 2;
+  const bool slab = s->precision == QD_PRECISION_MIXED && s->fft.cluster;
+  int n = 1 + (slab ? 1 : 3) + 1 + 1;   // fwd, fft, bwd, finalize (+ step counter)
+  if (s->any_coupled) n += 3;           // coriolis x2, rot energy
+  if (s->flux.enabled) n += 1;          // surface extraction
   return n;
 }
 
@@ -787,6 +801,8 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   s->status = dalloc<int>(1);
   s->status_step = dalloc<int>(1);
   s->d_step = dalloc<int>(1);
+  s->step_done = dalloc<unsigned>(1);
+  QD_CUDA(cudaMemsetAsync(s->step_done, 0, sizeof(unsigned), st));
   QD_CUDA(cudaMemsetAsync(s->status, 0, sizeof(int), st));
   QD_CUDA(cudaMemsetAsync(s->status_step, 0, sizeof(int), st));
   QD_CUDA(cudaMemcpyAsync(s->d_step, &s->steps, sizeof(int), cudaMemcpyHostToDevice, st));
@@ -818,6 +834,12 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     s->flux_count = dalloc<int>(1);
     s->flux_slot = dalloc<int>(1);
     QD_CUDA(cudaMemsetAsync(s->flux_count, 0, sizeof(int), st));
+    if (s->precision == QD_PRECISION_MIXED) {
+      s->half_v_lift = dalloc<float2>((size_t)g.nth * c.n_gradient_points * g.n1);
+      launch_build_half_v_lift(st, g, s->flux, s->pot, s->dt, s->half_v_lift);
+      std::vector<float> fdw32(fdw.begin(), fdw.end());
+      s->fdf = dupload(fdw32.data(), fdw32.size(), st);
+    }
     for (int p = 0; p < n_problems; p++) {
       double2 *dst = s->flux_acc + (int64_t)s->h_pblock0[p] * 2 * c.n_energies * ns;
       const size_t bytes = (size_t)s->probs[p].n_omegas * 2 * c.n_energies * ns * sizeof(double2);
