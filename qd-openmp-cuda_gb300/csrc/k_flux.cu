@@ -77,17 +77,32 @@ __global__ void k_flux_extract_f32(Grid g, int n_grad, int n_ds, const double2 *
   if (q >= ns) return;
   const int i = (int)(q % g.n1), k = (int)(q / g.n1);
   float Ax = 0.0f, Ay = 0.0f, Dx = 0.0f, Dy = 0.0f;
-  for (int gg = 0; gg < n_grad; gg++) {
-    const int j = n_ds - h + gg;
-    const double2 a = p[((int64_t)k * g.n2 + j) * g.n1 + i];
-    float x = d2f_rn(a.x), y = d2f_rn(a.y);
-    lift2f(x, y, __ldg(hv + ((int64_t)k * n_grad + gg) * g.n1 + i));
-    const float c = __ldg(fd + gg);
-    Dx = fmaf(c, x, Dx);
-    Dy = fmaf(c, y, Dy);
-    if (gg == h) {
-      Ax = x;
-      Ay = y;
+  constexpr int GB = 8;   // stencil rows loaded together
+  for (int g0 = 0; g0 < n_grad; g0 += GB) {
+    double2 a[GB];
+    float2 ts[GB];
+#pragma unroll
+    for (int u = 0; u < GB; u++) {
+      const int gg = g0 + u;
+      if (gg < n_grad) {
+        a[u] = p[((int64_t)k * g.n2 + (n_ds - h + gg)) * g.n1 + i];
+        ts[u] = __ldg(hv + ((int64_t)k * n_grad + gg) * g.n1 + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < GB; u++) {
+      const int gg = g0 + u;
+      if (gg < n_grad) {
+        float x = d2f_rn(a[u].x), y = d2f_rn(a[u].y);
+        lift2f(x, y, ts[u]);
+        const float c = __ldg(fd + gg);
+        Dx = fmaf(c, x, Dx);
+        Dy = fmaf(c, y, Dy);
+        if (gg == h) {
+          Ax = x;
+          Ay = y;
+        }
+      }
     }
   }
   out[q] = make_double2(f2d(Ax), f2d(Ay));

@@ -251,29 +251,30 @@ void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, cons
   k_rot_energy<<<dim3(tiles, n_slabs), 256, 0, s>>>(g, psi_j, slabs, re_part, tiles, status);
 }
 
-// One CTA per problem: per block, sum the partial arrays in a fixed order,
-// scale, write energies[b][6] and the step record; then the norm guard of
-// print_energies (cudaOpenMP2.cu:425-445).  Coupling-energy partials are laid
-// out [group][ce_n][tiles]; a block collects them from every group (one per l)
-// of its problem that contains its Omega.
+// Energy finalisation.  One CTA per (quantity, block) sums that block's
+// partial array in a fixed order (deterministic) and writes energies[b][q];
+// the last CTA to finish then forms the totals, the step record and the norm
+// guard of print_energies (cudaOpenMP2.cu:425-445), and, at the end of a full
+// step, books the flux slot and advances the step counter.  Quantities:
+// 0 module + potential, 1 kinetic, 2 rotational, 3 Coriolis.  Coupling-energy
+// partials are laid out [group][ce_n][tiles]; a block collects them from every
+// group (one per l) of its problem that contains its Omega.
 __global__ void k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__restrict__ blocks,
-                                  const int *__restrict__ pblock0, const CoriolisGroup *__restrict__ groups,
-                                  const int *__restrict__ pgroup0, int ce_n, double *__restrict__ energies,
-                                  double *__restrict__ rec, int *__restrict__ d_step, int rec_base,
-                                  int rec_cap, int n_blocks, double norm_tol, int *status, int *status_step,
-                                  StepTail tail) {
-  if (*status) return;
+                                  const int *__restrict__ pblock0, int n_problems,
+                                  const CoriolisGroup *__restrict__ groups, const int *__restrict__ pgroup0,
+                                  int ce_n, double *__restrict__ energies, double *__restrict__ rec,
+                                  int *__restrict__ d_step, int rec_base, int rec_cap, int n_blocks, double norm_tol,
+                                  int *status, int *status_step, StepTail tail, unsigned *done) {
+  if (*status) return;   // set before this launch: every CTA returns, the counter is untouched
   __shared__ double red[32];
-  const int pr = blockIdx.x;
-  const int b0 = pblock0[pr], b1 = pblock0[pr + 1];
+  __shared__ bool last;
+  const int qty = blockIdx.x, b = blockIdx.y;
+  const BlockDesc bd = blocks[b];
   const double dV = g.dr1 * g.dr2;
-  const int step = *d_step;
-  double total_module = 0.0;
-  for (int b = b0; b < b1; b++) {
-    const BlockDesc bd = blocks[b];
-    double e[6];
-    for (int q = 0; q < 6; q++) e[q] = energies[b * 6 + q];
-    if (ep.have_mod) {
+  const bool have = (qty == 0 && ep.have_mod) || (qty == 1 && ep.have_ke) || (qty == 2 && ep.have_re) ||
+                    (qty == 3 && ep.have_ce);
+  if (have) {
+    if (qty == 0) {
       double m = 0.0, pe = 0.0;
       for (int t = threadIdx.x; t < ep.mod_pe_tiles; t += blockDim.x) {
         m += ep.mod_pe[((int64_t)b * ep.mod_pe_tiles + t) * 2 + 0];
@@ -281,26 +282,23 @@ __global__ void k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__res
       }
       m = block_sum(m, red);
       pe = block_sum(pe, red);
-      e[E_MODULE] = m * dV;
-      e[E_POTENTIAL] = pe * dV;
-    }
-    if (ep.have_ke) {
-      double k = 0.0;
-      const int64_t n = (int64_t)bd.nl * ep.ke_tiles;
-      for (int64_t t = threadIdx.x; t < n; t += blockDim.x) k += ep.ke[(int64_t)bd.slab0 * ep.ke_tiles + t];
-      k = block_sum(k, red);
-      e[E_KINETIC] = k * dV / ((double)g.n1 * g.n2);
-    }
-    if (ep.have_re) {
-      double r = 0.0;
-      const int64_t n = (int64_t)bd.nl * ep.re_tiles;
-      for (int64_t t = threadIdx.x; t < n; t += blockDim.x) r += ep.re[(int64_t)bd.slab0 * ep.re_tiles + t];
-      r = block_sum(r, red);
-      e[E_ROTATIONAL] = r * dV;
-    }
-    if (ep.have_ce) {
+      if (threadIdx.x == 0) {
+        energies[b * 6 + E_MODULE] = m * dV;
+        energies[b * 6 + E_POTENTIAL] = pe * dV;
+      }
+    } else if (qty == 1 || qty == 2) {
+      const double *part = qty == 1 ? ep.ke : ep.re;
+      const int tiles = qty == 1 ? ep.ke_tiles : ep.re_tiles;
+      double v = 0.0;
+      const int64_t n = (int64_t)bd.nl * tiles;
+      for (int64_t t = threadIdx.x; t < n; t += blockDim.x) v += part[(int64_t)bd.slab0 * tiles + t];
+      v = block_sum(v, red);
+      if (threadIdx.x == 0)
+        energies[b * 6 + (qty == 1 ? E_KINETIC : E_ROTATIONAL)] = qty == 1 ? v * dV / ((double)g.n1 * g.n2) : v * dV;
+    } else {
       double c = 0.0;
       if (groups) {
+        const int pr = bd.problem;
         for (int gi = pgroup0[pr]; gi < pgroup0[pr + 1]; gi++) {
           const CoriolisGroup gr = groups[gi];
           const int o = bd.omega - gr.omega_lo;
@@ -310,43 +308,50 @@ __global__ void k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__res
         }
       }
       c = block_sum(c, red);
-      e[E_CORIOLIS] = c * dV;
+      if (threadIdx.x == 0) energies[b * 6 + E_CORIOLIS] = c * dV;
     }
-    e[E_TOTAL] = e[E_POTENTIAL] + e[E_KINETIC] + e[E_ROTATIONAL] + e[E_CORIOLIS];
-    total_module += e[E_MODULE];
-    if (threadIdx.x == 0) {
-      for (int q = 0; q < 6; q++) energies[b * 6 + q] = e[q];
-      const int slot = step - rec_base;
-      if (rec && slot >= 0 && slot < rec_cap)
-        for (int q = 0; q < 6; q++) rec[((int64_t)slot * n_blocks + b) * 6 + q] = e[q];
-    }
-    __syncthreads();
   }
-  if (threadIdx.x == 0 && ep.have_mod && total_module > 1.0 + norm_tol) {
-    if (atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
-  }
-  // End of a full step: the last CTA to finish books this step's flux slot and
-  // advances the step counter (no separate one-thread launches).
-  if (tail.done && threadIdx.x == 0) {
+  // ---- the last CTA: totals, records, norm guard, end-of-step bookkeeping
+  if (threadIdx.x == 0) {
     __threadfence();
-    const unsigned prev = atomicAdd(tail.done, 1u);
-    if (prev == gridDim.x - 1) {
-      __threadfence();
-      *tail.done = 0u;
-      if (atomicAdd(status, 0) == 0) {
-        if (tail.flux_count) {
-          const int c = *tail.flux_count;
-          if (c >= tail.cap) {
-            atomicCAS(status, 0, QD_ERR_INVALID);
-            *tail.flux_slot = 0;
-          } else {
-            if (c == 0) *tail.flux_t0 = (step + 1) * tail.dt;
-            *tail.flux_slot = c;
-            *tail.flux_count = c + 1;
-          }
-        }
-        *d_step = step + 1;
+    last = atomicAdd(done, 1u) == gridDim.x * gridDim.y - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int step = *d_step;
+  for (int bb = threadIdx.x; bb < n_blocks; bb += blockDim.x) {
+    double *e = energies + bb * 6;
+    e[E_TOTAL] = e[E_POTENTIAL] + e[E_KINETIC] + e[E_ROTATIONAL] + e[E_CORIOLIS];
+    const int slot = step - rec_base;
+    if (rec && slot >= 0 && slot < rec_cap)
+      for (int q = 0; q < 6; q++) rec[((int64_t)slot * n_blocks + bb) * 6 + q] = e[q];
+  }
+  if (ep.have_mod) {
+    for (int pr = 0; pr < n_problems; pr++) {
+      double m = 0.0;
+      for (int bb = pblock0[pr] + threadIdx.x; bb < pblock0[pr + 1]; bb += blockDim.x) m += energies[bb * 6 + E_MODULE];
+      m = block_sum(m, red);
+      if (threadIdx.x == 0 && m > 1.0 + norm_tol) {
+        if (atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
       }
+    }
+  }
+  if (threadIdx.x == 0) {
+    *done = 0u;
+    if (tail.done && atomicAdd(status, 0) == 0) {
+      if (tail.flux_count) {
+        const int c = *tail.flux_count;
+        if (c >= tail.cap) {
+          atomicCAS(status, 0, QD_ERR_INVALID);
+          *tail.flux_slot = 0;
+        } else {
+          if (c == 0) *tail.flux_t0 = (step + 1) * tail.dt;
+          *tail.flux_slot = c;
+          *tail.flux_count = c + 1;
+        }
+      }
+      *d_step = step + 1;
     }
   }
 }
@@ -354,12 +359,13 @@ __global__ void k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__res
 void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &ep, const BlockDesc *blocks,
                              const int *pblock0, int n_problems, const CoriolisGroup *groups, const int *pgroup0,
                              int ce_n, double *energies, double *rec, const int *d_step, int rec_base, int rec_cap,
-                             double norm_tol, int *status, int *status_step, int n_blocks, const StepTail *tail) {
+                             double norm_tol, int *status, int *status_step, int n_blocks, unsigned *done,
+                             const StepTail *tail) {
   StepTail t{};
   if (tail) t = *tail;
-  k_energy_finalize<<<n_problems, 256, 0, st>>>(g, ep, blocks, pblock0, groups, pgroup0, ce_n, energies, rec,
-                                               const_cast<int *>(d_step), rec_base, rec_cap, n_blocks, norm_tol,
-                                               status, status_step, t);
+  k_energy_finalize<<<dim3(4, n_blocks), 256, 0, st>>>(g, ep, blocks, pblock0, n_problems, groups, pgroup0, ce_n,
+                                                        energies, rec, const_cast<int *>(d_step), rec_base, rec_cap,
+                                                        n_blocks, norm_tol, status, status_step, t, done);
 }
 
 }  // namespace qd

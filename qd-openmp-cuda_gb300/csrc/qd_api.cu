@@ -339,15 +339,25 @@ __global__ void k_flux_extract_dev(Grid g, int n_grad, int n_ds, const double2 *
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(q % g.n1), k = (int)(q / g.n1);
     double2 A = make_double2(0.0, 0.0), D = make_double2(0.0, 0.0);
-    for (int gg = 0; gg < n_grad; gg++) {
-      const int j = n_ds - h + gg;
-      const double2 a = p[((int64_t)k * g.n2 + j) * g.n1 + i];
-      const double2 m = hv[((int64_t)k * n_grad + gg) * g.n1 + i];
-      const double2 v = make_double2(a.x * m.x - a.y * m.y, a.x * m.y + a.y * m.x);
-      const double c = fd[gg];
-      D.x = fma(c, v.x, D.x);
-      D.y = fma(c, v.y, D.y);
-      if (gg == h) A = v;
+    constexpr int GB = 8;   // stencil rows loaded together
+    for (int g0 = 0; g0 < n_grad; g0 += GB) {
+      double2 av[GB], mv[GB];
+#pragma unroll
+      for (int u = 0; u < GB; u++)
+        if (g0 + u < n_grad) {
+          av[u] = p[((int64_t)k * g.n2 + (n_ds - h + g0 + u)) * g.n1 + i];
+          mv[u] = hv[((int64_t)k * n_grad + g0 + u) * g.n1 + i];
+        }
+#pragma unroll
+      for (int u = 0; u < GB; u++)
+        if (g0 + u < n_grad) {
+          const double2 a = av[u], m = mv[u];
+          const double2 v = make_double2(a.x * m.x - a.y * m.y, a.x * m.y + a.y * m.x);
+          const double c = fd[g0 + u];
+          D.x = fma(c, v.x, D.x);
+          D.y = fma(c, v.y, D.y);
+          if (g0 + u == h) A = v;
+        }
     }
     out[q] = A;
     out[ns + q] = D;
@@ -524,7 +534,7 @@ static void enqueue_tail(qd_session *s) {
   }
   launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                           s->max_group_n, s->energies, s->rec, s->d_step, s->rec_base, s->rec_cap, s->norm_tol,
-                          s->status, s->status_step, s->n_blocks, &tail);
+                          s->status, s->status_step, s->n_blocks, s->step_done, &tail);
   prof_mark(st, "energy_finalize");
   if (s->flux.enabled) {
     if (s->precision == QD_PRECISION_MIXED) {
@@ -1173,7 +1183,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
           EnergyParts ep = energy_parts(s, false, false, false, true);
           launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                                   s->max_group_n, s->energies, nullptr, s->d_step, 0, 0, 1e300, s->status,
-                                  s->status_step, s->n_blocks);
+                                  s->status_step, s->n_blocks, s->step_done);
         }
         QD_CUDA(cudaStreamSynchronize(st));
         cudaFree(ph);
@@ -1204,7 +1214,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         EnergyParts ep = energy_parts(s, false, true, false, false);
         launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                                 s->max_group_n, s->energies, nullptr, s->d_step, 0, 0, 1e300, s->status,
-                                s->status_step, s->n_blocks);
+                                s->status_step, s->n_blocks, s->step_done);
         break;
       }
       case QD_STAGE_ENERGIES: {
@@ -1215,7 +1225,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         ep.re_tiles = t_re_saved;
         launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                                 s->max_group_n, s->energies, nullptr, s->d_step, 0, 0, 1e300, s->status,
-                                s->status_step, s->n_blocks);
+                                s->status_step, s->n_blocks, s->step_done);
         break;
       }
       case QD_STAGE_FLUX: {

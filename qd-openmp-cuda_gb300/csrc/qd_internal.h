@@ -169,7 +169,7 @@ struct EnergyParts {
 // End-of-step bookkeeping done by the last CTA of the energy finalisation:
 // flux slot and t0 of this step (when flux_count is set) and the step counter.
 struct StepTail {
-  unsigned *done;      // completion counter (null: do not advance the step)
+  unsigned *done;      // non-null: advance the step (end of a full step)
   int *flux_count, *flux_slot;
   double *flux_t0;
   int cap;
@@ -178,7 +178,7 @@ struct StepTail {
 void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &ep, const BlockDesc *blocks,
                              const int *pblock0, int n_problems, const CoriolisGroup *groups, const int *pgroup0,
                              int ce_n, double *energies, double *rec, const int *d_step, int rec_base, int rec_cap,
-                             double norm_tol, int *status, int *status_step, int n_blocks,
+                             double norm_tol, int *status, int *status_step, int n_blocks, unsigned *done,
                              const StepTail *tail = nullptr);
 void launch_build_half_v_lift(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
                               float2 *half_v);
