@@ -127,7 +127,7 @@ __device__ inline void split3(float x, uint16_t &a0, uint16_t &a1, uint16_t &a2)
   a2 = __bfloat16_as_ushort(b2);
 }
 
-__device__ inline int round16(int x) { return (x + 15) & ~15; }
+__host__ __device__ inline int round16(int x) { return (x + 15) & ~15; }
 
 // products a_i * b_j with i + j <= 2
 __constant__ int c_pair_a[6] = {0, 0, 1, 0, 1, 2};
@@ -441,6 +441,294 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised form.  Each CTA walks a contiguous range of
+// (block, 64-point tile) pairs.  Warps 0-3 (producers) stage and slice tile
+// t+1 while warps 4-7 (consumers) drain tile t from TMEM; thread 128 issues
+// the MMA chain of each tile.  Three mbarriers carry the hand-offs:
+//   slices_ready (128 producer arrivals)  -> the MMA may read A/B slices
+//   mma_done     (tcgen05.commit)         -> TMEM holds tile t; A/B reusable
+//   tmem_free    (128 consumer arrivals)  -> the next MMA may overwrite TMEM
+// Every wait is bounded (1 s); a timeout sets the error status and the CTA
+// stops issuing work, waits (bounded) for its MMAs, frees TMEM and returns.
+__device__ inline void named_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ inline void mbar_arrive(uint32_t a) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(a) : "memory");
+}
+__device__ inline bool mbar_wait_bounded(uint32_t a, uint32_t parity) {
+  const uint64_t t0 = globaltimer();
+  while (!mbar_try_wait(a, parity))
+    if (globaltimer() - t0 > WAIT_NS) return false;
+  return true;
+}
+
+struct TcTile {
+  int b, mt, Kv, Nv, Kp, Np;
+  uint32_t SBO, A_TERM, B_TERM;
+};
+
+template <bool FWD>
+__device__ inline TcTile tc_tile(const TcArgs &P, int tt, int mtiles) {
+  TcTile t;
+  t.b = tt / mtiles;
+  t.mt = tt - t.b * mtiles;
+  const int nl = P.blocks[t.b].nl;
+  t.Kv = FWD ? P.g.nth : nl;
+  t.Nv = FWD ? nl : P.g.nth;
+  t.Kp = round16(t.Kv);
+  t.Np = round16(t.Nv);
+  t.SBO = (uint32_t)(t.Kp / 8 * 128);
+  t.A_TERM = 16u * t.SBO;
+  t.B_TERM = (uint32_t)(t.Np / 8) * t.SBO;
+  return t;
+}
+
+template <bool FWD>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int mtiles, int n_tiles, int kp_max,
+                                                                   int np_max) {
+  if (P.status && *P.status) return;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t mb_ready, mb_done, mb_free;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ float srow_s[2][128];
+  __shared__ float red_s[8];
+  __shared__ int abort_p, abort_c, n_issued;
+  const Grid &g = P.g;
+  const uint32_t a_term_max = 16u * (uint32_t)(kp_max / 8 * 128);
+  const uint32_t b_term_max = (uint32_t)(np_max / 8) * (uint32_t)(kp_max / 8 * 128);
+  unsigned char *sA = smem;
+  unsigned char *sB = smem + 3 * a_term_max;
+  float *sF = reinterpret_cast<float *>(sB + 3 * b_term_max);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t ncols = 512;
+  const int t_begin = (int)((int64_t)blockIdx.x * n_tiles / gridDim.x);
+  const int t_end = (int)((int64_t)(blockIdx.x + 1) * n_tiles / gridDim.x);
+
+  if (warp == 0) tmem_alloc(smem_u32(&tmem_base_s), ncols);
+  if (tid == 0) {
+    mbar_init(smem_u32(&mb_ready), 128);
+    mbar_init(smem_u32(&mb_done), 1);
+    mbar_init(smem_u32(&mb_free), 128);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_p = 0;
+    abort_c = 0;
+    n_issued = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_s;
+
+  if (warp < 4) {
+    // =============================== producers: rows m = tid
+    int cur_b = -1;
+    for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
+      const TcTile T = tc_tile<FWD>(P, tt, mtiles);
+      const BlockDesc bd = P.blocks[T.b];
+      const int64_t p0 = (int64_t)T.mt * TC_POINTS;
+      const int LDF = T.Kp + 1;
+      // phase 1: A tile -> FP32 rows in sF (sF is ours alone)
+      {
+        const double2 *A = FWD ? P.A + (int64_t)T.b * g.nth * g.npt : P.A + (int64_t)bd.slab0 * g.npt;
+        const int pl = tid % TC_POINTS;
+        const int64_t p = p0 + pl;
+        float msk = 1.0f;
+        if (FWD && P.d1 && p < g.npt) msk = P.d1[(int)(p % g.n1)] * P.d2[(int)(p / g.n1)];
+        constexpr int U = 16;
+        const int nk = T.Kp / 2;   // this thread's k values: tid/64 + 2u
+        for (int u0 = 0; u0 < nk; u0 += U) {
+          double2 v[U];
+          float2 ts[U];
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            const int k = tid / TC_POINTS + 2 * (u0 + u);
+            const bool in = u0 + u < nk && k < T.Kv && p < g.npt;
+            v[u] = in ? A[(int64_t)k * g.npt + p] : make_double2(0.0, 0.0);
+            if (FWD) ts[u] = (in && P.vph) ? __ldg(P.vph + (int64_t)k * g.npt + p) : make_float2(0.0f, 0.0f);
+          }
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            if (u0 + u >= nk) break;
+            const int k = tid / TC_POINTS + 2 * (u0 + u);
+            float x = d2f_rn(v[u].x), y = d2f_rn(v[u].y);
+            if (FWD) {
+              x *= msk;
+              y *= msk;
+              if (P.vph) rot_lift2(x, y, ts[u]);
+            }
+            sF[(2 * pl) * LDF + k] = x;
+            sF[(2 * pl + 1) * LDF + k] = y;
+          }
+        }
+      }
+      named_bar(1, 128);
+      // the MMA of the previous tile must be done before A (and B) are rewritten;
+      // one thread waits and the group decides together (no divergent exit)
+      if (tid == 0 && it > 0 && !mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((it - 1) & 1))) {
+        if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_CUDA);
+        abort_p = 1;
+      }
+      named_bar(1, 128);
+      if (abort_p) break;
+      if (T.b != cur_b) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(P.bimg + P.bimg_off[T.b] / 2);
+        uint4 *dst = reinterpret_cast<uint4 *>(sB);
+        const int n16 = (int)(tc_bimg_bytes(T.Np, T.Kp) / 16);
+        for (int q = tid; q < n16; q += 128) dst[q] = __ldg(src + q);
+        cur_b = T.b;
+      }
+      // phase 2: scale and slice row m = tid
+      {
+        const int m = tid;
+        const float *row = sF + m * LDF;
+        float mx = 0.0f;
+        for (int k = 0; k < T.Kp; k++) mx = fmaxf(mx, fabsf(row[k]));
+        int e = 0;
+        if (mx >= 1e-30f) frexpf(mx, &e);
+        const float inv = mx >= 1e-30f ? ldexpf(1.0f, -e) * 256.0f : 0.0f;
+        srow_s[it & 1][m] = ldexpf(1.0f, e - 16);
+        const uint32_t orow = (uint32_t)(m / 8) * T.SBO + (m % 8) * 16;
+        for (int kg = 0; kg < T.Kp / 8; kg++) {
+          uint32_t w[3][4];
+#pragma unroll
+          for (int e8 = 0; e8 < 8; e8++) {
+            const float a = row[kg * 8 + e8] * inv;
+            const float i0 = rintf(a);
+            const float r1 = (a - i0) * 256.0f;
+            const float i1 = rintf(r1);
+            const float i2 = rintf((r1 - i1) * 256.0f);
+            const uint16_t h0 = __bfloat16_as_ushort(__float2bfloat16_rn(i0));
+            const uint16_t h1 = __bfloat16_as_ushort(__float2bfloat16_rn(i1));
+            const uint16_t h2 = __bfloat16_as_ushort(__float2bfloat16_rn(i2));
+            if (e8 & 1) {
+              w[0][e8 >> 1] |= (uint32_t)h0 << 16;
+              w[1][e8 >> 1] |= (uint32_t)h1 << 16;
+              w[2][e8 >> 1] |= (uint32_t)h2 << 16;
+            } else {
+              w[0][e8 >> 1] = h0;
+              w[1][e8 >> 1] = h1;
+              w[2][e8 >> 1] = h2;
+            }
+          }
+#pragma unroll
+          for (int t = 0; t < 3; t++)
+            *reinterpret_cast<uint4 *>(sA + t * T.A_TERM + orow + kg * 128) =
+                make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(smem_u32(&mb_ready));
+      named_bar(1, 128);   // sF is rewritten only after every producer has sliced
+    }
+  } else {
+    // =============================== consumers (+ the MMA issuer, thread 128)
+    const int ctid = tid - 128, quarter = warp & 3;
+    const int m = 32 * quarter + lane;
+    const int pl = m >> 1, c = m & 1;
+    for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
+      const TcTile T = tc_tile<FWD>(P, tt, mtiles);
+      const BlockDesc bd = P.blocks[T.b];
+      if (ctid == 0) {
+        bool ok = mbar_wait_bounded(smem_u32(&mb_ready), (uint32_t)(it & 1));
+        if (ok && it > 0) ok = mbar_wait_bounded(smem_u32(&mb_free), (uint32_t)((it - 1) & 1));
+        if (!ok) {
+          if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_CUDA);
+          abort_c = 1;
+        } else {
+          tc_fence_after();
+          const uint32_t idesc = make_idesc(128, T.Np);
+          const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+          for (int s = 0; s < T.Kp / 16; s++) {
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+              const int d = c_pair_a[q] + c_pair_b[q];
+              const uint64_t ad = make_desc(a0 + c_pair_a[q] * T.A_TERM + s * 256, 128, T.SBO);
+              const uint64_t bdsc = make_desc(b0 + c_pair_b[q] * T.B_TERM + s * 256, 128, T.SBO);
+              const bool first = s == 0 && (q == 0 || q == 1 || q == 3);
+              mma_bf16(tmem + (uint32_t)(d * T.Np), ad, bdsc, idesc, first ? 0u : 1u);
+            }
+          }
+          mma_commit(smem_u32(&mb_done));
+          n_issued = it + 1;
+          // this thread observes completion for the group
+          if (!mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)(it & 1))) {
+            if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_CUDA);
+            abort_c = 1;
+          }
+        }
+        tc_fence_before();
+      }
+      __syncwarp();
+      named_bar(2, 128);
+      if (abort_c) break;
+      tc_fence_after();
+      const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
+      const float srow = srow_s[it & 1][m];
+      const float *tsc = P.bscale + (int64_t)T.b * 256;
+      float mod = 0.0f, pe = 0.0f;
+      double *Cd = reinterpret_cast<double *>(P.C);
+      const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
+      for (int n0 = 0; n0 < T.Np; n0 += 16) {
+        float d0[16], d1[16], d2[16], wv[16];
+        if (!FWD) {
+#pragma unroll
+          for (int q = 0; q < 16; q++)
+            wv[q] = (n0 + q < T.Nv && p < g.npt) ? __ldg(P.wv + (int64_t)(n0 + q) * g.npt + p) : 0.0f;
+        }
+        tmem_ld16(trow + (uint32_t)n0, d0);
+        tmem_ld16(trow + (uint32_t)(T.Np + n0), d1);
+        tmem_ld16(trow + (uint32_t)(2 * T.Np + n0), d2);
+        if (p >= g.npt) continue;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const int n = n0 + q;
+          if (n >= T.Nv) break;
+          const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc[n]);
+          if (FWD) {
+            Cd[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = f2d(v);
+          } else {
+            Cd[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = f2d(v);
+            const float v2 = v * v;
+            mod = fmaf(__ldg(P.w + n), v2, mod);
+            pe = fmaf(wv[q], v2, pe);
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(smem_u32(&mb_free));
+      if (!FWD && P.part) {
+        // fixed-order reduction over the 128 consumer threads
+        for (int o = 16; o > 0; o >>= 1) {
+          mod += __shfl_down_sync(0xffffffffu, mod, o);
+          pe += __shfl_down_sync(0xffffffffu, pe, o);
+        }
+        if (lane == 0) {
+          red_s[quarter] = mod;
+          red_s[4 + quarter] = pe;
+        }
+        named_bar(2, 128);
+        if (ctid == 0) {
+          const double ms = (double)red_s[0] + red_s[1] + red_s[2] + red_s[3];
+          const double ps = (double)red_s[4] + red_s[5] + red_s[6] + red_s[7];
+          P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 0] = ms;
+          P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 1] = ps;
+        }
+        named_bar(2, 128);
+      }
+    }
+  }
+  // ---- drain: after a timeout, wait (bounded) for the last MMA chain issued
+  __syncthreads();
+  if (tid == 128 && (abort_p || abort_c) && n_issued > 0)
+    mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((n_issued - 1) & 1));
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, ncols);
+  }
+}
+
 // Dynamic shared memory of one launch: the BF16 slices of A and B and the
 // FP32 staging rows, and at least enough that no more than 512/ncols CTAs fit
 // on an SM (233472 bytes of shared memory), so the TMEM columns that their
@@ -456,10 +744,33 @@ bool tc_shape_ok(int Kp, int Np) { return Kp <= 192 && Np <= 160 && tc_smem_byte
 
 int legendre_tc_part_tiles(const Grid &g) { return (int)((g.npt + TC_POINTS - 1) / TC_POINTS); }
 
+// persistent launch: A/B slices for the largest tile and the FP32 staging rows,
+// and at least 120 KB so that one CTA (holding all 512 TMEM columns) runs per SM
+size_t tc_ws_smem_bytes(int kp_max, int np_max) {
+  const size_t need =
+      (size_t)3 * 16 * (kp_max / 8 * 128) + (size_t)tc_bimg_bytes(np_max, kp_max) + (size_t)128 * (kp_max + 1) * 4;
+  return std::max(need, (size_t)120 * 1024);
+}
+
+void launch_legendre_tc_ws(cudaStream_t s, bool fwd, const TcArgs &a, int n_blocks, int kp_max, int np_max) {
+  const int mtiles = legendre_tc_part_tiles(a.g);
+  const int n_tiles = mtiles * n_blocks;
+  int dev = 0, sms = 0;
+  QD_CUDA(cudaGetDevice(&dev));
+  QD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = std::min(n_tiles, sms);
+  const size_t smem = tc_ws_smem_bytes(kp_max, np_max);
+  if (fwd)
+    k_legendre_tc_ws<true><<<grid, TC_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
+  else
+    k_legendre_tc_ws<false><<<grid, TC_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
+}
+
+
 void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, double2 *psi_j,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
-                            int *status_w, const float *bscale) {
+                            int *status_w, const float *bscale, int max_nl) {
   TcArgs a{};
   a.bscale = bscale;
   a.g = g;
@@ -473,14 +784,14 @@ void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th
   a.d2 = d2f;
   a.status = status;
   a.status_w = status_w;
-  dim3 grid((unsigned)legendre_tc_part_tiles(g), (unsigned)n_blocks);
-  k_legendre_tc<true><<<grid, TC_THREADS, smem, s>>>(a);
+  (void)smem;
+  launch_legendre_tc_ws(s, true, a, n_blocks, round16(g.nth), round16(max_nl));
 }
 
 void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j, double2 *psi_th,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
-                            const int *status, int *status_w, const float *bscale) {
+                            const int *status, int *status_w, const float *bscale, int max_nl) {
   TcArgs a{};
   a.bscale = bscale;
   a.g = g;
@@ -495,13 +806,15 @@ void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j,
   a.n_part_tiles = n_part_tiles;
   a.status = status;
   a.status_w = status_w;
-  dim3 grid((unsigned)legendre_tc_part_tiles(g), (unsigned)n_blocks);
-  k_legendre_tc<false><<<grid, TC_THREADS, smem, s>>>(a);
+  (void)smem;
+  launch_legendre_tc_ws(s, false, a, n_blocks, round16(max_nl), round16(g.nth));
 }
 
 void tc_set_smem_limit(size_t bytes) {
   QD_CUDA(cudaFuncSetAttribute(k_legendre_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   QD_CUDA(cudaFuncSetAttribute(k_legendre_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
 }
 
 void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,

@@ -446,7 +446,7 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
   cudaStream_t st = s->stream;
   const Grid &g = s->g;
   launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_j, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f,
-                         first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status, s->bscale_f);
+                         first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status, s->bscale_f, s->max_nl);
   prof_mark(st, "legendre_forward");
   if (s->any_coupled) {
     launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
@@ -474,7 +474,7 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
     prof_mark(st, "rotational_energy");
   }
   launch_legendre_tc_bwd(st, g, s->psi_j, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf, s->wvf,
-                         s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b);
+                         s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b, s->max_nl);
   prof_mark(st, "legendre_backward");
   enqueue_tail(s);
 }
@@ -1153,7 +1153,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       case QD_STAGE_FORWARD_LEGENDRE:
         if (s->precision == QD_PRECISION_MIXED)
           launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_j, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f, nullptr,
-                                 nullptr, nullptr, s->smem_f, s->status, s->status, s->bscale_f);
+                                 nullptr, nullptr, s->smem_f, s->status, s->status, s->bscale_f, s->max_nl);
         else
           launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, nullptr,
                                   nullptr, s->status);
@@ -1161,7 +1161,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       case QD_STAGE_BACKWARD_LEGENDRE:
         if (s->precision == QD_PRECISION_MIXED)
           launch_legendre_tc_bwd(st, g, s->psi_j, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf,
-                                 s->wvf, s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b);
+                                 s->wvf, s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b, s->max_nl);
         else
           launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
                                   s->part_modpe, s->t_modpe, s->status);

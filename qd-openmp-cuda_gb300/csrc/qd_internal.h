@@ -229,11 +229,11 @@ void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_block
 void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, double2 *psi_j,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
-                            int *status_w, const float *bscale);
+                            int *status_w, const float *bscale, int max_nl);
 void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j, double2 *psi_th,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
-                            const int *status, int *status_w, const float *bscale);
+                            const int *status, int *status_w, const float *bscale, int max_nl);
 int legendre_tc_part_tiles(const Grid &g);
 
 void launch_build_half_v(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
