@@ -483,15 +483,18 @@ __device__ inline TcTile tc_tile(const TcArgs &P, int tt, int mtiles) {
   return t;
 }
 
+constexpr int WS_THREADS = 512;      // 8 producer warps + 8 consumer warps
+constexpr int WS_PROD = 256;
+
 template <bool FWD>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int mtiles, int n_tiles, int kp_max,
+__global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int mtiles, int n_tiles, int kp_max,
                                                                    int np_max) {
   if (P.status && *P.status) return;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t mb_ready, mb_done, mb_free;
   __shared__ uint32_t tmem_base_s;
   __shared__ float srow_s[2][128];
-  __shared__ float red_s[8];
+  __shared__ float red_s[16];
   __shared__ int abort_p, abort_c, n_issued;
   const Grid &g = P.g;
   const uint32_t a_term_max = 16u * (uint32_t)(kp_max / 8 * 128);
@@ -506,9 +509,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
 
   if (warp == 0) tmem_alloc(smem_u32(&tmem_base_s), ncols);
   if (tid == 0) {
-    mbar_init(smem_u32(&mb_ready), 128);
+    mbar_init(smem_u32(&mb_ready), WS_PROD);
     mbar_init(smem_u32(&mb_done), 1);
-    mbar_init(smem_u32(&mb_free), 128);
+    mbar_init(smem_u32(&mb_free), WS_THREADS - WS_PROD);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_p = 0;
     abort_c = 0;
@@ -519,29 +522,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
 
-  if (warp < 4) {
-    // =============================== producers: rows m = tid
+  if (tid < WS_PROD) {
+    // =============================== producers: 256 threads, two per row
     int cur_b = -1;
     for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
       const TcTile T = tc_tile<FWD>(P, tt, mtiles);
       const BlockDesc bd = P.blocks[T.b];
       const int64_t p0 = (int64_t)T.mt * TC_POINTS;
       const int LDF = T.Kp + 1;
-      // phase 1: A tile -> FP32 rows in sF (sF is ours alone)
+      const double2 *A = FWD ? P.A + (int64_t)T.b * g.nth * g.npt : P.A + (int64_t)bd.slab0 * g.npt;
+      // L2 prefetch of the next tile (128-byte lines of its k rows)
+      if (tt + 1 < t_end) {
+        const TcTile Tn = tc_tile<FWD>(P, tt + 1, mtiles);
+        const BlockDesc bn = P.blocks[Tn.b];
+        const double2 *An = FWD ? P.A + (int64_t)Tn.b * g.nth * g.npt : P.A + (int64_t)bn.slab0 * g.npt;
+        const int64_t pn = (int64_t)Tn.mt * TC_POINTS;
+        const int lines = Tn.Kv * 8;   // 64 points x 16 B = 8 lines per k row
+        for (int q = tid; q < lines; q += WS_PROD) {
+          const int k = q >> 3, ln = q & 7;
+          const int64_t pp = pn + ln * 8;
+          if (pp < g.npt) asm volatile("prefetch.global.L2 [%0];" ::"l"(An + (int64_t)k * g.npt + pp));
+          if (FWD && P.vph && (ln & 1) == 0 && pp < g.npt)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(P.vph + (int64_t)k * g.npt + pp));
+        }
+      }
+      // phase 1: A tile -> FP32 rows in sF
       {
-        const double2 *A = FWD ? P.A + (int64_t)T.b * g.nth * g.npt : P.A + (int64_t)bd.slab0 * g.npt;
         const int pl = tid % TC_POINTS;
         const int64_t p = p0 + pl;
         float msk = 1.0f;
         if (FWD && P.d1 && p < g.npt) msk = P.d1[(int)(p % g.n1)] * P.d2[(int)(p / g.n1)];
-        constexpr int U = 16;
-        const int nk = T.Kp / 2;   // this thread's k values: tid/64 + 2u
+        constexpr int U = 12;
+        const int nk = T.Kp / 4;   // this thread's k values: tid/64 + 4u
         for (int u0 = 0; u0 < nk; u0 += U) {
           double2 v[U];
           float2 ts[U];
 #pragma unroll
           for (int u = 0; u < U; u++) {
-            const int k = tid / TC_POINTS + 2 * (u0 + u);
+            const int k = tid / TC_POINTS + 4 * (u0 + u);
             const bool in = u0 + u < nk && k < T.Kv && p < g.npt;
             v[u] = in ? A[(int64_t)k * g.npt + p] : make_double2(0.0, 0.0);
             if (FWD) ts[u] = (in && P.vph) ? __ldg(P.vph + (int64_t)k * g.npt + p) : make_float2(0.0f, 0.0f);
@@ -549,7 +567,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
 #pragma unroll
           for (int u = 0; u < U; u++) {
             if (u0 + u >= nk) break;
-            const int k = tid / TC_POINTS + 2 * (u0 + u);
+            const int k = tid / TC_POINTS + 4 * (u0 + u);
             float x = d2f_rn(v[u].x), y = d2f_rn(v[u].y);
             if (FWD) {
               x *= msk;
@@ -561,34 +579,34 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
           }
         }
       }
-      named_bar(1, 128);
+      named_bar(1, WS_PROD);
       // the MMA of the previous tile must be done before A (and B) are rewritten;
       // one thread waits and the group decides together (no divergent exit)
       if (tid == 0 && it > 0 && !mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((it - 1) & 1))) {
         if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_CUDA);
         abort_p = 1;
       }
-      named_bar(1, 128);
+      named_bar(1, WS_PROD);
       if (abort_p) break;
       if (T.b != cur_b) {
         const uint4 *src = reinterpret_cast<const uint4 *>(P.bimg + P.bimg_off[T.b] / 2);
         uint4 *dst = reinterpret_cast<uint4 *>(sB);
         const int n16 = (int)(tc_bimg_bytes(T.Np, T.Kp) / 16);
-        for (int q = tid; q < n16; q += 128) dst[q] = __ldg(src + q);
+        for (int q = tid; q < n16; q += WS_PROD) dst[q] = __ldg(src + q);
         cur_b = T.b;
       }
-      // phase 2: scale and slice row m = tid
+      // phase 2: threads 2m and 2m+1 scale row m and slice one half of its k groups each
       {
-        const int m = tid;
+        const int m = tid >> 1, half = tid & 1;
         const float *row = sF + m * LDF;
         float mx = 0.0f;
         for (int k = 0; k < T.Kp; k++) mx = fmaxf(mx, fabsf(row[k]));
         int e = 0;
         if (mx >= 1e-30f) frexpf(mx, &e);
         const float inv = mx >= 1e-30f ? ldexpf(1.0f, -e) * 256.0f : 0.0f;
-        srow_s[it & 1][m] = ldexpf(1.0f, e - 16);
+        if (half == 0) srow_s[it & 1][m] = ldexpf(1.0f, e - 16);
         const uint32_t orow = (uint32_t)(m / 8) * T.SBO + (m % 8) * 16;
-        for (int kg = 0; kg < T.Kp / 8; kg++) {
+        for (int kg = half; kg < T.Kp / 8; kg += 2) {
           uint32_t w[3][4];
 #pragma unroll
           for (int e8 = 0; e8 < 8; e8++) {
@@ -618,11 +636,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(smem_u32(&mb_ready));
-      named_bar(1, 128);   // sF is rewritten only after every producer has sliced
+      named_bar(1, WS_PROD);   // sF is rewritten only after every producer has sliced
     }
   } else {
-    // =============================== consumers (+ the MMA issuer, thread 128)
-    const int ctid = tid - 128, quarter = warp & 3;
+    // =============================== consumers: 256 threads (+ the MMA issuer, thread 256)
+    const int ctid = tid - WS_PROD, cw = warp - WS_PROD / 32;
+    const int quarter = warp & 3, chalf = cw >> 2;
     const int m = 32 * quarter + lane;
     const int pl = m >> 1, c = m & 1;
     for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
@@ -659,7 +678,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         tc_fence_before();
       }
       __syncwarp();
-      named_bar(2, 128);
+      named_bar(2, WS_THREADS - WS_PROD);
       if (abort_c) break;
       tc_fence_after();
       const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
@@ -668,7 +687,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       float mod = 0.0f, pe = 0.0f;
       double *Cd = reinterpret_cast<double *>(P.C);
       const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
-      for (int n0 = 0; n0 < T.Np; n0 += 16) {
+      for (int n0 = 16 * chalf; n0 < T.Np; n0 += 32) {
         float d0[16], d1[16], d2[16], wv[16];
         if (!FWD) {
 #pragma unroll
@@ -697,29 +716,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       tc_fence_before();
       mbar_arrive(smem_u32(&mb_free));
       if (!FWD && P.part) {
-        // fixed-order reduction over the 128 consumer threads
+        // fixed-order reduction over the 256 consumer threads
         for (int o = 16; o > 0; o >>= 1) {
           mod += __shfl_down_sync(0xffffffffu, mod, o);
           pe += __shfl_down_sync(0xffffffffu, pe, o);
         }
         if (lane == 0) {
-          red_s[quarter] = mod;
-          red_s[4 + quarter] = pe;
+          red_s[cw] = mod;
+          red_s[8 + cw] = pe;
         }
-        named_bar(2, 128);
+        named_bar(2, WS_THREADS - WS_PROD);
         if (ctid == 0) {
-          const double ms = (double)red_s[0] + red_s[1] + red_s[2] + red_s[3];
-          const double ps = (double)red_s[4] + red_s[5] + red_s[6] + red_s[7];
+          double ms = 0.0, ps = 0.0;
+          for (int q = 0; q < 8; q++) {
+            ms += red_s[q];
+            ps += red_s[8 + q];
+          }
           P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 0] = ms;
           P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 1] = ps;
         }
-        named_bar(2, 128);
+        named_bar(2, WS_THREADS - WS_PROD);
       }
     }
   }
   // ---- drain: after a timeout, wait (bounded) for the last MMA chain issued
   __syncthreads();
-  if (tid == 128 && (abort_p || abort_c) && n_issued > 0)
+  if (tid == WS_PROD && (abort_p || abort_c) && n_issued > 0)
     mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((n_issued - 1) & 1));
   tc_fence_before();
   __syncthreads();
@@ -761,9 +783,9 @@ void launch_legendre_tc_ws(cudaStream_t s, bool fwd, const TcArgs &a, int n_bloc
   const int grid = std::min(n_tiles, sms);
   const size_t smem = tc_ws_smem_bytes(kp_max, np_max);
   if (fwd)
-    k_legendre_tc_ws<true><<<grid, TC_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
+    k_legendre_tc_ws<true><<<grid, WS_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
   else
-    k_legendre_tc_ws<false><<<grid, TC_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
+    k_legendre_tc_ws<false><<<grid, WS_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
 }
 
 
