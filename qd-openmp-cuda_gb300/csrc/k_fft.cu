@@ -513,6 +513,377 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
   }
 }
 
+// ------------------------------------ separable single-pass slab FFT (FP32)
+// The kinetic propagator is separable: with F = F1 (x) F2 and the phase
+// K = K1 (x) K2,  F^-1 K F = (F1^-1 K1 F1) (x) (F2^-1 K2 F2).  So each slab is
+// propagated by a complete forward-phase-inverse 1-D pass along R on every
+// row, then one along r on every column, with a single cluster exchange in
+// between (the 2-D form needs two).  Each 1-D transform of length N = A B is
+// done in registers: B threads hold A values each, a length-A DFT with
+// constant twiddles, the twiddles W_N^(j k1), one exchange through shared
+// memory, then A/B length-B DFTs per thread; the inverse retraces the steps.
+// Kinetic energy: sum (T1 + T2) |psi^|^2 over the 2-D spectrum equals
+// n2 sum T1 |F1 psi|^2 + (1/n1) sum T2 |F2 (n1 A1 psi)|^2, A1 the unitary row
+// propagator, so each pass accumulates its own term.
+namespace {
+// t = -tan(theta/2), s = sin(theta) of theta = u pi/8, u = 1..3
+__device__ __forceinline__ float rot_tan_half(int u) {
+  return u == 1 ? 0.198912367379658006911f : (u == 2 ? 0.414213562373095048802f : 0.668178637919298919998f);
+}
+__device__ __forceinline__ float rot_sin(int u) {
+  return u == 1 ? 0.382683432365089771728f : (u == 2 ? 0.707106781186547524401f : 0.923879532511286756128f);
+}
+
+// v *= exp(i u pi/8) for a compile-time-known integer u (after unrolling):
+// exact for multiples of pi/2, a three-shear rotation otherwise
+__device__ __forceinline__ void rot_pi8(float2 &v, int u) {
+  u = ((u % 16) + 16) % 16;
+  if (u > 8) u -= 16;   // (-8, 8]
+  if (u > 4 || u < -4) {
+    v.x = -v.x;
+    v.y = -v.y;
+    u += u > 0 ? -8 : 8;
+  }
+  if (u == 0) return;
+  if (u == 4) {   // * i
+    const float x = v.x;
+    v.x = -v.y;
+    v.y = x;
+    return;
+  }
+  if (u == -4) {   // * -i
+    const float x = v.x;
+    v.x = v.y;
+    v.y = -x;
+    return;
+  }
+  const int a = u > 0 ? u : -u;
+  const float t = u > 0 ? -rot_tan_half(a) : rot_tan_half(a);
+  const float s = u > 0 ? rot_sin(a) : -rot_sin(a);
+  float x = v.x, y = v.y;
+  x = fmaf(t, y, x);
+  y = fmaf(s, x, y);
+  x = fmaf(t, y, x);
+  v.x = x;
+  v.y = y;
+}
+
+// In-register DFT of N in {1, 2, 4, 8, 16} values in natural order; forward
+// exp(-2 pi i jk/N), inverse exp(+2 pi i jk/N), unnormalised.
+template <int N, bool INV> struct RegDFT {
+  static __device__ __forceinline__ void run(float2 *v) {
+    static_assert(N == 8 || N == 16, "register DFT length");
+    constexpr int P = 4, Q = N / 4;
+    float2 a[Q][P];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+#pragma unroll
+      for (int p = 0; p < P; p++) a[q][p] = v[q + Q * p];
+      RegDFT<4, INV>::run(a[q]);
+#pragma unroll
+      for (int k1 = 1; k1 < P; k1++) rot_pi8(a[q][k1], (INV ? 16 : -16) * q * k1 / N);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < P; k1++) {
+      float2 b[Q];
+#pragma unroll
+      for (int q = 0; q < Q; q++) b[q] = a[q][k1];
+      RegDFT<Q, INV>::run(b);
+#pragma unroll
+      for (int k2 = 0; k2 < Q; k2++) v[k1 + P * k2] = b[k2];
+    }
+  }
+};
+template <bool INV> struct RegDFT<1, INV> {
+  static __device__ __forceinline__ void run(float2 *) {}
+};
+template <bool INV> struct RegDFT<2, INV> {
+  static __device__ __forceinline__ void run(float2 *v) {
+    const float2 a = v[0], b = v[1];
+    v[0] = make_float2(a.x + b.x, a.y + b.y);
+    v[1] = make_float2(a.x - b.x, a.y - b.y);
+  }
+};
+template <bool INV> struct RegDFT<4, INV> {
+  static __device__ __forceinline__ void run(float2 *v) { dft<float, 4>(v, INV); }
+};
+
+// v *= W_n^(+-e) from the shared twiddle table (three shears, see fft_stage)
+__device__ __forceinline__ void tw_apply(float2 &v, const float2 *tab, int e, int n, bool inv) {
+  if (e == 0) return;
+  const float2 w = tab[e];
+  const float tt = inv ? -w.x : w.x, ss = inv ? -w.y : w.y;
+  float x = v.x, y = v.y;
+  if (4 * e > n && 4 * e < 3 * n) {
+    x = -x;
+    y = -y;
+  }
+  x = fmaf(tt, y, x);
+  y = fmaf(ss, x, y);
+  x = fmaf(tt, y, x);
+  v.x = x;
+  v.y = y;
+}
+}  // namespace
+
+// Layout: cluster of C CTAs per slab.  CTA c owns rows r in [c RPC, (c+1) RPC)
+// (RPC = THREADS / B1, B1 threads per row) and columns R in [c CPC, (c+1) CPC)
+// (CPC = n1 / C, B2 threads per column).  Row region of local row q: RS
+// floats2 at Xr + q RS, used as the row transposition buffer and then as the
+// row the other CTAs gather from.  Column transposition buffer Sc[k1][j][col].
+template <int A, int B1, int B2, int THREADS>
+__global__ void __launch_bounds__(THREADS, 2) k_fft_slab_sep(double2 *__restrict__ psi, Grid g,
+                                                             const SlabDesc *__restrict__ slabs,
+                                                             const float2 *__restrict__ tw1,
+                                                             const float2 *__restrict__ tw2, FFTLift lf,
+                                                             double *__restrict__ ke_part,
+                                                             double *__restrict__ re_part, float fscale,
+                                                             double scale, const int *status) {
+  constexpr int N1 = A * B1, N2 = A * B2;
+  constexpr int RPC = THREADS / B1;
+  constexpr int C = N2 / RPC;
+  constexpr int CPC = N1 / C;
+  constexpr int RS = A * (B1 + 1);
+  static_assert(THREADS % B1 == 0 && N2 % RPC == 0 && N1 % C == 0 && CPC * B2 == THREADS, "slab tiling");
+  static_assert(A % B1 == 0 && A % B2 == 0 && 32 % B1 == 0, "transform factors");
+  if (status && *status) return;   // uniform over the cluster
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  float2 *Xr = reinterpret_cast<float2 *>(smem_raw);
+  float2 *Sc = Xr + RPC * RS;
+  float2 *t1 = Sc + A * B2 * CPC;
+  float2 *t2 = t1 + N1;
+  const int tid = threadIdx.x;
+  for (int q = tid; q < N1; q += THREADS) t1[q] = __ldg(tw1 + q);
+  for (int q = tid; q < N2; q += THREADS) t2[q] = __ldg(tw2 + q);
+  const int c = (int)cluster.block_rank();
+  const int sl = blockIdx.x / C;
+  const int l = slabs[sl].l;
+  double2 *P = psi + (int64_t)sl * g.npt;
+  float ke1 = 0.0f, ke2 = 0.0f, ref = 0.0f;
+  float2 v[A];
+
+  // ======== rows: thread j of row group q holds x[j + B1 m], m < A
+  {
+    const int q = tid / B1, j = tid % B1;
+    const int r = c * RPC + q;
+    const double2 *src = P + (int64_t)r * N1 + j;
+    {
+      double2 raw[A];
+#pragma unroll
+      for (int m = 0; m < A; m++) raw[m] = __ldcs(src + B1 * m);
+#pragma unroll
+      for (int m = 0; m < A; m++) v[m] = make_float2(d2f_rn(raw[m].x), d2f_rn(raw[m].y));
+    }
+    if (lf.proR) {
+      const float2 pr = __ldg(lf.pror + (int64_t)l * N2 + r);
+#pragma unroll
+      for (int m = 0; m < A; m++) {
+        lift2(v[m].x, v[m].y, __ldg(lf.proR + (int64_t)l * N1 + j + B1 * m));
+        lift2(v[m].x, v[m].y, pr);
+      }
+    }
+    __syncthreads();   // twiddle tables
+    float2 *G = Xr + q * RS;
+    RegDFT<A, false>::run(v);
+#pragma unroll
+    for (int k1 = 1; k1 < A; k1++) tw_apply(v[k1], t1, j * k1, N1, false);
+#pragma unroll
+    for (int k1 = 0; k1 < A; k1++) G[k1 * (B1 + 1) + j] = v[k1];
+    __syncwarp();
+    // thread t now takes k1 = t + B1 h, h < A / B1, over all j
+    float2 w[A];
+#pragma unroll
+    for (int h = 0; h < A / B1; h++)
+#pragma unroll
+      for (int jj = 0; jj < B1; jj++) w[h * B1 + jj] = G[(j + B1 * h) * (B1 + 1) + jj];
+#pragma unroll
+    for (int h = 0; h < A / B1; h++) {
+      RegDFT<B1, false>::run(w + h * B1);
+#pragma unroll
+      for (int k2 = 0; k2 < B1; k2++) {   // frequency kR = k1 + A k2
+        const int kR = j + B1 * h + A * k2;
+        float2 &z = w[h * B1 + k2];
+        ke1 = fmaf(__ldg(lf.T1f + kR), z.x * z.x + z.y * z.y, ke1);
+        lift2(z.x, z.y, __ldg(lf.kinR + kR));
+      }
+      RegDFT<B1, true>::run(w + h * B1);
+#pragma unroll
+      for (int jj = 1; jj < B1; jj++) tw_apply(w[h * B1 + jj], t1, jj * (j + B1 * h), N1, true);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < A / B1; h++)
+#pragma unroll
+      for (int jj = 0; jj < B1; jj++) G[(j + B1 * h) * (B1 + 1) + jj] = w[h * B1 + jj];
+    __syncwarp();
+#pragma unroll
+    for (int k1 = 0; k1 < A; k1++) v[k1] = G[k1 * (B1 + 1) + j];
+    RegDFT<A, true>::run(v);
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < A; m++) G[j + B1 * m] = v[m];
+  }
+  cluster.sync();   // every row of the slab is in its owner's shared memory
+
+  // ======== columns: thread jc of column col holds x[r = jc + B2 m], m < A
+  const int col = tid % CPC, jc = tid / CPC;
+  const int R = c * CPC + col;
+#pragma unroll
+  for (int m = 0; m < A; m++) {
+    const int rr = jc + B2 * m;
+    const int owner = rr / RPC;
+    const float2 *src = cluster.map_shared_rank(Xr, owner);
+    v[m] = src[(rr - owner * RPC) * RS + R];
+  }
+  RegDFT<A, false>::run(v);
+  // the gathered values are consumed: other CTAs may finish once all arrive
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+#pragma unroll
+  for (int k1 = 1; k1 < A; k1++) tw_apply(v[k1], t2, jc * k1, N2, false);
+#pragma unroll
+  for (int k1 = 0; k1 < A; k1++) Sc[(k1 * B2 + jc) * CPC + col] = v[k1];
+  __syncthreads();
+  {
+    float2 w[A];
+#pragma unroll
+    for (int h = 0; h < A / B2; h++)
+#pragma unroll
+      for (int jj = 0; jj < B2; jj++) w[h * B2 + jj] = Sc[((jc + B2 * h) * B2 + jj) * CPC + col];
+#pragma unroll
+    for (int h = 0; h < A / B2; h++) {
+      RegDFT<B2, false>::run(w + h * B2);
+#pragma unroll
+      for (int k2 = 0; k2 < B2; k2++) {   // frequency kr = k1 + A k2
+        const int kr = jc + B2 * h + A * k2;
+        float2 &z = w[h * B2 + k2];
+        ke2 = fmaf(__ldg(lf.T2f + kr), z.x * z.x + z.y * z.y, ke2);
+        lift2(z.x, z.y, __ldg(lf.kinr + kr));
+      }
+      RegDFT<B2, true>::run(w + h * B2);
+#pragma unroll
+      for (int jj = 1; jj < B2; jj++) tw_apply(w[h * B2 + jj], t2, jj * (jc + B2 * h), N2, true);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < A / B2; h++)
+#pragma unroll
+      for (int jj = 0; jj < B2; jj++) Sc[((jc + B2 * h) * B2 + jj) * CPC + col] = w[h * B2 + jj];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k1 = 0; k1 < A; k1++) v[k1] = Sc[(k1 * B2 + jc) * CPC + col];
+  RegDFT<A, true>::run(v);
+
+  // ======== scale, rotational phase after the inverse transform, rotational energy, store
+  const float lls2 = (float)l * (float)(l + 1) * (fscale != 0.0f ? 1.0f : (float)(scale * scale));
+  const float2 eR = lf.epiR ? __ldg(lf.epiR + (int64_t)l * N1 + R) : make_float2(0.0f, 0.0f);
+  const float I1 = re_part ? __ldg(lf.I1f + R) : 0.0f;
+#pragma unroll
+  for (int m = 0; m < A; m++) {
+    const int rr = jc + B2 * m;
+    float x = v[m].x, y = v[m].y;
+    if (fscale != 0.0f) {
+      x *= fscale;
+      y *= fscale;
+    }
+    if (lf.epiR) {
+      lift2(x, y, eR);
+      lift2(x, y, __ldg(lf.epir + (int64_t)l * N2 + rr));
+    }
+    if (re_part) ref = fmaf(lls2 * (I1 + __ldg(lf.I2f + rr)), x * x + y * y, ref);
+    __stcs(P + (int64_t)rr * N1 + R,
+           fscale != 0.0f ? make_double2(f2d(x), f2d(y)) : make_double2(f2d(x) * scale, f2d(y) * scale));
+  }
+  const double ke = block_sum((double)N2 * (double)ke1 + (double)ke2 / (double)N1, red);
+  const double re = block_sum((double)ref, red);
+  if (tid == 0) {
+    if (ke_part) ke_part[(int64_t)sl * C + c] = ke;
+    if (re_part) re_part[(int64_t)sl * C + c] = re;
+  }
+  // no CTA leaves while another may still read its rows
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+namespace {
+// instantiations of the separable slab FFT: (n1, n2) -> (A, B1, B2, threads)
+struct SepShape {
+  int n1, n2, A, B1, B2, threads;
+};
+constexpr SepShape kSepShapes[] = {
+    {256, 128, 16, 16, 8, 256},
+    {64, 32, 8, 8, 4, 128},
+    {32, 16, 8, 4, 2, 32},
+    {16, 8, 4, 4, 2, 32},
+};
+constexpr int kNumSep = (int)(sizeof(kSepShapes) / sizeof(kSepShapes[0]));
+
+template <int A, int B1, int B2, int T>
+size_t sep_smem_bytes() {
+  constexpr int RPC = T / B1, C = A * B2 / RPC, CPC = A * B1 / C;
+  return ((size_t)RPC * A * (B1 + 1) + (size_t)A * B2 * CPC + A * B1 + A * B2) * sizeof(float2);
+}
+template <int A, int B1, int B2, int T>
+int sep_cluster() {
+  return A * B2 / (T / B1);
+}
+
+template <int A, int B1, int B2, int T>
+void sep_set_attr() {
+  QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)sep_smem_bytes<A, B1, B2, T>()));
+}
+
+template <int A, int B1, int B2, int T>
+void sep_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j, const SlabDesc *slabs, int n_slabs,
+                const FFTLift &lf, double *ke_part, double *re_part, float fscale, double scale, const int *status) {
+  const int C = sep_cluster<A, B1, B2, T>();
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)(n_slabs * C));
+  cfg.blockDim = dim3(T);
+  cfg.dynamicSmemBytes = sep_smem_bytes<A, B1, B2, T>();
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  QD_CUDA(cudaLaunchKernelEx(&cfg, k_fft_slab_sep<A, B1, B2, T>, psi_j, g, slabs, (const float2 *)p.tw1_f,
+                             (const float2 *)p.tw2_f, lf, ke_part, re_part, fscale, scale, status));
+}
+
+void sep_dispatch_attr(int id) {
+  switch (id) {
+    case 0: sep_set_attr<16, 16, 8, 256>(); break;
+    case 1: sep_set_attr<8, 8, 4, 128>(); break;
+    case 2: sep_set_attr<8, 4, 2, 32>(); break;
+    case 3: sep_set_attr<4, 4, 2, 32>(); break;
+  }
+}
+int sep_dispatch_cluster(int id) {
+  switch (id) {
+    case 0: return sep_cluster<16, 16, 8, 256>();
+    case 1: return sep_cluster<8, 8, 4, 128>();
+    case 2: return sep_cluster<8, 4, 2, 32>();
+    case 3: return sep_cluster<4, 4, 2, 32>();
+  }
+  return 0;
+}
+void sep_dispatch_launch(int id, cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j,
+                         const SlabDesc *slabs, int n_slabs, const FFTLift &lf, double *ke_part, double *re_part,
+                         float fscale, double scale, const int *status) {
+  switch (id) {
+    case 0: sep_launch<16, 16, 8, 256>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+    case 1: sep_launch<8, 8, 4, 128>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+    case 2: sep_launch<8, 4, 2, 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+    case 3: sep_launch<4, 4, 2, 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+  }
+}
+}  // namespace
+
 // ------------------------------------------------------------- host side
 bool fft_factor(int n, int *rad, int *nst) {
   int k = 0;
@@ -552,6 +923,13 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
   if (n1 > FFT_THREADS * MAXV || n2 > FFT_THREADS * MAXV)
     throw Error{QD_ERR_UNSUPPORTED, "FFT grid size above 4096"};
   p.cluster = choose_cluster(n1, n2);
+  p.sep = -1;
+  p.sep_cluster = 0;
+  for (int q = 0; q < kNumSep; q++)
+    if (kSepShapes[q].n1 == n1 && kSepShapes[q].n2 == n2) {
+      p.sep = q;
+      p.sep_cluster = sep_dispatch_cluster(q);
+    }
   p.rows_per_cta = largest_divisor_at_most(n2, std::max(1, FFT_THREADS * MAXV / n1));
   p.rows_per_cta = std::min(p.rows_per_cta, largest_divisor_at_most(n2, 64));
   p.cols_per_cta = largest_divisor_at_most(n1, std::min(32, std::max(1, FFT_THREADS * MAXV / n2)));
@@ -583,6 +961,7 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
   QD_CUDA(cudaFuncSetAttribute(k_fft_slab_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   if (p.cluster > 1)
     QD_CUDA(cudaFuncSetAttribute(k_fft_slab_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 0));
+  if (p.sep >= 0) sep_dispatch_attr(p.sep);
 }
 
 void fft_plan_free(FFTPlan &p) {
@@ -597,9 +976,11 @@ void fft_plan_free(FFTPlan &p) {
 // partial-sum tiles per slab: the single-pass FP32 form writes one per CTA of
 // the cluster, the three-pass forms one per column / row tile
 int fft_col_tiles(const FFTPlan &p, int precision) {
+  if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_cluster;
   return (precision == QD_PRECISION_MIXED && p.cluster) ? p.cluster : p.n1 / p.cols_per_cta;
 }
 int fft_row_tiles(const FFTPlan &p, int precision) {
+  if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_cluster;
   return (precision == QD_PRECISION_MIXED && p.cluster) ? p.cluster : p.n2 / p.rows_per_cta;
 }
 
@@ -636,6 +1017,11 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
   const double scale = 1.0 / ((double)g.n1 * g.n2);
   const bool pow2 = ((g.n1 * g.n2) & (g.n1 * g.n2 - 1)) == 0;
   const float fscale = pow2 ? (float)scale : 0.0f;
+  if (std::is_same<R, float>::value && p.sep >= 0 && lf && lf->kinR) {
+    sep_dispatch_launch(p.sep, s, g, p, psi_j, slabs, n_slabs, *lf, ke_part, re_part, fscale, scale, status);
+    prof_mark(s, "fft_slab");
+    return;
+  }
   if (std::is_same<R, float>::value && p.cluster && lf && lf->kinR) {
     const int C = p.cluster;
     cudaLaunchConfig_t cfg{};

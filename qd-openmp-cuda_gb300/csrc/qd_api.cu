@@ -551,7 +551,7 @@ static void enqueue_tail(qd_session *s) {
 }
 
 static int count_launches_per_step(qd_session *s) {
-  const bool slab = s->precision == QD_PRECISION_MIXED && s->fft.cluster;
+  const bool slab = s->precision == QD_PRECISION_MIXED && (s->fft.cluster || s->fft.sep >= 0);
   int n = 1 + (slab ? 1 : 3) + 1 + 1;   // fwd, fft, bwd, finalize (+ step counter)
   if (s->any_coupled) n += 3;           // coriolis x2, rot energy
   if (s->flux.enabled) n += 1;          // surface extraction

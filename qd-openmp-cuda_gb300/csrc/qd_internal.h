@@ -118,6 +118,8 @@ struct FFTPlan {
   int rows_per_cta;
   int cols_per_cta;
   int cluster;   // CTAs per slab of the single-pass FP32 FFT (0: three-pass form)
+  int sep;           // shape index of the separable single-pass FP32 FFT, -1: none
+  int sep_cluster;   // its CTAs per slab
 };
 // FP32 three-shear phase tables of the mixed form (float2 (t, s) per entry,
 // see lift tables below); null entries are skipped.

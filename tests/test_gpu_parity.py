@@ -214,7 +214,9 @@ def test_mixed_precision_close_to_fp64(qd, oracle, gpu):
 
 @pytest.mark.parametrize("case", [dict(J=0, n1=16, n2=8, n_theta=6, l_max=5),
                                   dict(J=2, parity=0, n1=32, n2=16, n_theta=24, l_max=23),
-                                  dict(J=3, parity=1, n1=24, n2=12, n_theta=40, l_max=37)])
+                                  dict(J=3, parity=1, n1=24, n2=12, n_theta=40, l_max=37),
+                                  dict(J=0, n1=64, n2=32, n_theta=8, l_max=7),
+                                  dict(J=1, parity=0, n1=256, n2=128, n_theta=8, l_max=7)])
 def test_mixed_stages_match_oracle(qd, oracle, gpu, case):
     """tcgen05 BF16x3 Legendre contractions and the FP32 FFT: FP32-level agreement (rel <= 3e-6)."""
     cfg, d, dref = make(qd, **case)
