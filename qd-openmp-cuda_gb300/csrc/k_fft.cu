@@ -632,7 +632,7 @@ __device__ __forceinline__ void tw_apply(float2 &v, const float2 *tab, int e, in
 // floats2 at Xr + q RS, used as the row transposition buffer and then as the
 // row the other CTAs gather from.  Column transposition buffer Sc[k1][j][col].
 template <int A, int B1, int B2, int THREADS>
-__global__ void __launch_bounds__(THREADS, 2) k_fft_slab_sep(double2 *__restrict__ psi, Grid g,
+__global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(double2 *__restrict__ psi, Grid g,
                                                              const SlabDesc *__restrict__ slabs,
                                                              const float2 *__restrict__ tw1,
                                                              const float2 *__restrict__ tw2, FFTLift lf,
@@ -796,9 +796,21 @@ __global__ void __launch_bounds__(THREADS, 2) k_fft_slab_sep(double2 *__restrict
     __stcs(P + (int64_t)rr * N1 + R,
            fscale != 0.0f ? make_double2(f2d(x), f2d(y)) : make_double2(f2d(x) * scale, f2d(y) * scale));
   }
-  const double ke = block_sum((double)N2 * (double)ke1 + (double)ke2 / (double)N1, red);
-  const double re = block_sum((double)ref, red);
+  // partial sums: FP32 within a warp, FP64 across warps in a fixed order
+  float kew = fmaf((float)N2, ke1, ke2 * (1.0f / (float)N1)), rew = ref;
+  for (int o = 16; o > 0; o >>= 1) {
+    kew += __shfl_down_sync(0xffffffffu, kew, o);
+    rew += __shfl_down_sync(0xffffffffu, rew, o);
+  }
+  float2 *red2 = reinterpret_cast<float2 *>(red);
+  if ((tid & 31) == 0) red2[tid >> 5] = make_float2(kew, rew);
+  __syncthreads();
   if (tid == 0) {
+    double ke = 0.0, re = 0.0;
+    for (int w = 0; w < THREADS / 32; w++) {
+      ke += (double)red2[w].x;
+      re += (double)red2[w].y;
+    }
     if (ke_part) ke_part[(int64_t)sl * C + c] = ke;
     if (re_part) re_part[(int64_t)sl * C + c] = re;
   }
