@@ -109,6 +109,8 @@ def algorithmic(kernel: str, d: dict, flux_chunk: int = 32):
         else:                              # psi_j in, psi_theta out, w V (FP32) in
             byts = sum(16.0 * npt * nl + 16.0 * npt * nth + 4.0 * npt * nth for nl in nls)
         return "hbm", byts, "GB/s"
+    if kernel == "fft_slab":   # one read and one write of every c128 point of every slab
+        return "hbm", 32.0 * npt * snl, "GB/s"
     if kernel == "fft_rows_forward" or kernel == "fft_cols_kinetic":
         return "hbm", 32.0 * npt * snl, "GB/s"
     if kernel == "fft_rows_inverse":
