@@ -63,57 +63,78 @@ __device__ inline void lift2f(float &x, float &y, float2 ts) {
   x = fmaf(ts.x, y, x);
 }
 
-__global__ void k_flux_extract_f32(Grid g, int n_grad, int n_ds, const double2 *__restrict__ psi_th,
-                                   const float2 *__restrict__ hv, const float *__restrict__ fd,
-                                   double2 *__restrict__ buf, int n_blocks, const int *slot_p, const int *status) {
+// One thread row y of FLUX_GY handles the stencil rows gg = y, y + FLUX_GY, ...
+// of FLUX_GX consecutive surface points (i fastest: coalesced loads); the
+// rows' partial derivatives are summed in a fixed order through shared memory.
+namespace {
+constexpr int FLUX_GX = 64, FLUX_GY = 4, FLUX_GMAX = 8;   // n_grad <= FLUX_GY * FLUX_GMAX
+}
+__global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, int n_grad, int n_ds,
+                                                                       const double2 *__restrict__ psi_th,
+                                                                       const float2 *__restrict__ hv,
+                                                                       const float *__restrict__ fd,
+                                                                       double2 *__restrict__ buf, int n_blocks,
+                                                                       const int *slot_p, const int *status) {
   if (status && *status) return;
+  __shared__ float2 sD[FLUX_GY][FLUX_GX];
+  __shared__ float2 sA[FLUX_GX];
   const int slot = *slot_p;
   const int b = blockIdx.y;
   const int h = (n_grad - 1) / 2;
   const int64_t ns = (int64_t)g.nth * g.n1;
   double2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
   const double2 *p = psi_th + (int64_t)b * g.nth * g.npt;
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= ns) return;
-  const int i = (int)(q % g.n1), k = (int)(q / g.n1);
-  float Ax = 0.0f, Ay = 0.0f, Dx = 0.0f, Dy = 0.0f;
-  constexpr int GB = 8;   // stencil rows loaded together
-  for (int g0 = 0; g0 < n_grad; g0 += GB) {
-    double2 a[GB];
-    float2 ts[GB];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t q = (int64_t)blockIdx.x * FLUX_GX + tx;
+  float Dx = 0.0f, Dy = 0.0f;
+  if (q < ns) {
+    const int i = (int)(q % g.n1), k = (int)(q / g.n1);
+    double2 a[FLUX_GMAX];
+    float2 ts[FLUX_GMAX];
 #pragma unroll
-    for (int u = 0; u < GB; u++) {
-      const int gg = g0 + u;
+    for (int u = 0; u < FLUX_GMAX; u++) {
+      const int gg = ty + FLUX_GY * u;
       if (gg < n_grad) {
         a[u] = p[((int64_t)k * g.n2 + (n_ds - h + gg)) * g.n1 + i];
         ts[u] = __ldg(hv + ((int64_t)k * n_grad + gg) * g.n1 + i);
       }
     }
 #pragma unroll
-    for (int u = 0; u < GB; u++) {
-      const int gg = g0 + u;
+    for (int u = 0; u < FLUX_GMAX; u++) {
+      const int gg = ty + FLUX_GY * u;
       if (gg < n_grad) {
         float x = d2f_rn(a[u].x), y = d2f_rn(a[u].y);
         lift2f(x, y, ts[u]);
         const float c = __ldg(fd + gg);
         Dx = fmaf(c, x, Dx);
         Dy = fmaf(c, y, Dy);
-        if (gg == h) {
-          Ax = x;
-          Ay = y;
-        }
+        if (gg == h) sA[tx] = make_float2(x, y);
       }
     }
   }
-  out[q] = make_double2(f2d(Ax), f2d(Ay));
-  out[ns + q] = make_double2(f2d(Dx), f2d(Dy));
+  sD[ty][tx] = make_float2(Dx, Dy);
+  __syncthreads();
+  if (ty == 0 && q < ns) {
+    float2 D = sD[0][tx];
+#pragma unroll
+    for (int y = 1; y < FLUX_GY; y++) {
+      D.x += sD[y][tx].x;
+      D.y += sD[y][tx].y;
+    }
+    const float2 A = sA[tx];
+    out[q] = make_double2(f2d(A.x), f2d(A.y));
+    out[ns + q] = make_double2(f2d(D.x), f2d(D.y));
+  }
 }
 
 void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const double2 *psi_th, int n_blocks,
                              const float2 *half_v, const float *fd, double2 *buf, const int *slot, const int *status) {
+  if (f.n_grad > FLUX_GY * FLUX_GMAX)
+    throw Error{QD_ERR_UNSUPPORTED, "mixed-form flux: more than 32 stencil points"};
   const int64_t ns = (int64_t)g.nth * g.n1;
-  dim3 grid((unsigned)((ns + 127) / 128), (unsigned)n_blocks);
-  k_flux_extract_f32<<<grid, 128, 0, s>>>(g, f.n_grad, f.n_ds, psi_th, half_v, fd, buf, n_blocks, slot, status);
+  dim3 grid((unsigned)((ns + FLUX_GX - 1) / FLUX_GX), (unsigned)n_blocks);
+  k_flux_extract_f32<<<grid, dim3(FLUX_GX, FLUX_GY), 0, s>>>(g, f.n_grad, f.n_ds, psi_th, half_v, fd, buf, n_blocks,
+                                                              slot, status);
 }
 
 // phase[n][E] = dt exp(i E (t0 + n dt))

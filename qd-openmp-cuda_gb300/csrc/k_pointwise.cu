@@ -259,100 +259,119 @@ void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, cons
 // 0 module + potential, 1 kinetic, 2 rotational, 3 Coriolis.  Coupling-energy
 // partials are laid out [group][ce_n][tiles]; a block collects them from every
 // group (one per l) of its problem that contains its Omega.
-__global__ void k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__restrict__ blocks,
+__global__ void __launch_bounds__(256) k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__restrict__ blocks,
                                   const int *__restrict__ pblock0, int n_problems,
                                   const CoriolisGroup *__restrict__ groups, const int *__restrict__ pgroup0,
                                   int ce_n, double *__restrict__ energies, double *__restrict__ rec,
                                   int *__restrict__ d_step, int rec_base, int rec_cap, int n_blocks, double norm_tol,
                                   int *status, int *status_step, StepTail tail, unsigned *done) {
-  if (*status) return;   // set before this launch: every CTA returns, the counter is untouched
-  __shared__ double red[32];
+  constexpr int NW = 256 / 32;
+  __shared__ double red[NW][5];
   __shared__ bool last;
-  const int qty = blockIdx.x, b = blockIdx.y;
+  const int b = blockIdx.x, tid = threadIdx.x;
+  // everything this launch reads is loaded up front: one round trip
+  const int st0 = *status;
+  const int step = *d_step;   // advanced only by the last CTA, after every CTA has read it
+  const int fcount = (tid == 0 && tail.flux_count) ? *tail.flux_count : 0;
   const BlockDesc bd = blocks[b];
-  const double dV = g.dr1 * g.dr2;
-  const bool have = (qty == 0 && ep.have_mod) || (qty == 1 && ep.have_ke) || (qty == 2 && ep.have_re) ||
-                    (qty == 3 && ep.have_ce);
-  if (have) {
-    if (qty == 0) {
-      double m = 0.0, pe = 0.0;
-      for (int t = threadIdx.x; t < ep.mod_pe_tiles; t += blockDim.x) {
-        m += ep.mod_pe[((int64_t)b * ep.mod_pe_tiles + t) * 2 + 0];
-        pe += ep.mod_pe[((int64_t)b * ep.mod_pe_tiles + t) * 2 + 1];
-      }
-      m = block_sum(m, red);
-      pe = block_sum(pe, red);
-      if (threadIdx.x == 0) {
-        energies[b * 6 + E_MODULE] = m * dV;
-        energies[b * 6 + E_POTENTIAL] = pe * dV;
-      }
-    } else if (qty == 1 || qty == 2) {
-      const double *part = qty == 1 ? ep.ke : ep.re;
-      const int tiles = qty == 1 ? ep.ke_tiles : ep.re_tiles;
-      double v = 0.0;
-      const int64_t n = (int64_t)bd.nl * tiles;
-      for (int64_t t = threadIdx.x; t < n; t += blockDim.x) v += part[(int64_t)bd.slab0 * tiles + t];
-      v = block_sum(v, red);
-      if (threadIdx.x == 0)
-        energies[b * 6 + (qty == 1 ? E_KINETIC : E_ROTATIONAL)] = qty == 1 ? v * dV / ((double)g.n1 * g.n2) : v * dV;
+  // the partials of this block as one index space: [module/potential pairs | kinetic | rotational | Coriolis]
+  const int n0 = ep.have_mod ? ep.mod_pe_tiles : 0;
+  const int n1 = ep.have_ke ? bd.nl * ep.ke_tiles : 0;
+  const int n2 = ep.have_re ? bd.nl * ep.re_tiles : 0;
+  // Coriolis: every group (one per l) of this problem, the tiles of this Omega where it is a member
+  const int g_lo = (ep.have_ce && groups) ? pgroup0[bd.problem] : 0;
+  const int n3 = (ep.have_ce && groups) ? (pgroup0[bd.problem + 1] - g_lo) * ep.ce_tiles : 0;
+  const double2 *mp = reinterpret_cast<const double2 *>(ep.mod_pe) + (int64_t)b * ep.mod_pe_tiles;
+  const double *kp = ep.ke + (int64_t)bd.slab0 * ep.ke_tiles;
+  const double *rp = ep.re + (int64_t)bd.slab0 * ep.re_tiles;
+  const int total = n0 + n1 + n2 + n3;
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll 8
+  for (int t = tid; t < total; t += 256) {
+    if (t < n0) {
+      const double2 v = mp[t];
+      acc[0] += v.x;
+      acc[1] += v.y;
+    } else if (t < n0 + n1) {
+      acc[2] += kp[t - n0];
+    } else if (t < n0 + n1 + n2) {
+      acc[3] += rp[t - n0 - n1];
     } else {
-      double c = 0.0;
-      if (groups) {
-        const int pr = bd.problem;
-        for (int gi = pgroup0[pr]; gi < pgroup0[pr + 1]; gi++) {
-          const CoriolisGroup gr = groups[gi];
-          const int o = bd.omega - gr.omega_lo;
-          if (o < 0 || o >= gr.n) continue;
-          for (int t = threadIdx.x; t < ep.ce_tiles; t += blockDim.x)
-            c += ep.ce[((int64_t)gi * ce_n + o) * ep.ce_tiles + t];
-        }
-      }
-      c = block_sum(c, red);
-      if (threadIdx.x == 0) energies[b * 6 + E_CORIOLIS] = c * dV;
+      const int q = t - n0 - n1 - n2;
+      const int gi = g_lo + q / ep.ce_tiles, tt = q - (q / ep.ce_tiles) * ep.ce_tiles;
+      const int o = bd.omega - groups[gi].omega_lo;
+      if (o >= 0 && o < groups[gi].n) acc[4] += ep.ce[((int64_t)gi * ce_n + o) * ep.ce_tiles + tt];
     }
   }
-  // ---- the last CTA: totals, records, norm guard, end-of-step bookkeeping
-  if (threadIdx.x == 0) {
-    __threadfence();
-    last = atomicAdd(done, 1u) == gridDim.x * gridDim.y - 1;
-  }
+  // fixed-order reduction: shuffle tree per warp, then the warps in order
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 5; q++) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+  if ((tid & 31) == 0)
+#pragma unroll
+    for (int q = 0; q < 5; q++) red[tid >> 5][q] = acc[q];
   __syncthreads();
-  if (!last) return;
-  __threadfence();
-  const int step = *d_step;
-  for (int bb = threadIdx.x; bb < n_blocks; bb += blockDim.x) {
-    double *e = energies + bb * 6;
-    e[E_TOTAL] = e[E_POTENTIAL] + e[E_KINETIC] + e[E_ROTATIONAL] + e[E_CORIOLIS];
+  if (st0) return;   // set before this launch: nothing is written, the counter is untouched
+  double mod = 0.0;
+  if (tid == 0) {
+    double tot[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < NW; w++)
+#pragma unroll
+      for (int q = 0; q < 5; q++) tot[q] += red[w][q];
+    const double dV = g.dr1 * g.dr2;
+    double *e = energies + b * 6;
+    double ev[6];
+    ev[E_MODULE] = ep.have_mod ? tot[0] * dV : e[E_MODULE];
+    ev[E_POTENTIAL] = ep.have_mod ? tot[1] * dV : e[E_POTENTIAL];
+    ev[E_KINETIC] = ep.have_ke ? tot[2] * dV / ((double)g.n1 * g.n2) : e[E_KINETIC];
+    ev[E_ROTATIONAL] = ep.have_re ? tot[3] * dV : e[E_ROTATIONAL];
+    ev[E_CORIOLIS] = ep.have_ce ? tot[4] * dV : e[E_CORIOLIS];
+    ev[E_TOTAL] = ev[E_POTENTIAL] + ev[E_KINETIC] + ev[E_ROTATIONAL] + ev[E_CORIOLIS];
+    for (int q = 0; q < 6; q++) e[q] = ev[q];
     const int slot = step - rec_base;
     if (rec && slot >= 0 && slot < rec_cap)
-      for (int q = 0; q < 6; q++) rec[((int64_t)slot * n_blocks + bb) * 6 + q] = e[q];
+      for (int q = 0; q < 6; q++) rec[((int64_t)slot * n_blocks + b) * 6 + q] = ev[q];
+    mod = ev[E_MODULE];
   }
-  if (ep.have_mod) {
-    for (int pr = 0; pr < n_problems; pr++) {
-      double m = 0.0;
-      for (int bb = pblock0[pr] + threadIdx.x; bb < pblock0[pr + 1]; bb += blockDim.x) m += energies[bb * 6 + E_MODULE];
-      m = block_sum(m, red);
-      if (threadIdx.x == 0 && m > 1.0 + norm_tol) {
-        if (atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
-      }
+  // ---- end of step: norm guard per problem, flux slot, step counter
+  bool bad = false;   // thread 0: this launch set the norm status
+  if (gridDim.x == 1) {
+    if (tid != 0) return;
+    if (ep.have_mod && mod > 1.0 + norm_tol) {
+      bad = true;
+      if (atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
     }
-  }
-  if (threadIdx.x == 0) {
+  } else {
+    if (tid == 0) {
+      __threadfence();
+      last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (ep.have_mod)
+      for (int pr = tid; pr < n_problems; pr += 256) {
+        double m = 0.0;
+        for (int bb = pblock0[pr]; bb < pblock0[pr + 1]; bb++) m += __ldcg(energies + bb * 6 + E_MODULE);
+        if (m > 1.0 + norm_tol && atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
+      }
+    __syncthreads();
+    if (tid != 0) return;
     *done = 0u;
-    if (tail.done && atomicAdd(status, 0) == 0) {
-      if (tail.flux_count) {
-        const int c = *tail.flux_count;
-        if (c >= tail.cap) {
-          atomicCAS(status, 0, QD_ERR_INVALID);
-          *tail.flux_slot = 0;
-        } else {
-          if (c == 0) *tail.flux_t0 = (step + 1) * tail.dt;
-          *tail.flux_slot = c;
-          *tail.flux_count = c + 1;
-        }
+    bad = atomicAdd(status, 0) != 0;
+  }
+  if (tail.done && !bad) {
+    if (tail.flux_count) {
+      if (fcount >= tail.cap) {
+        atomicCAS(status, 0, QD_ERR_INVALID);
+        *tail.flux_slot = 0;
+      } else {
+        if (fcount == 0) *tail.flux_t0 = (step + 1) * tail.dt;
+        *tail.flux_slot = fcount;
+        *tail.flux_count = fcount + 1;
       }
-      *d_step = step + 1;
     }
+    *d_step = step + 1;
   }
 }
 
@@ -363,7 +382,7 @@ void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &
                              const StepTail *tail) {
   StepTail t{};
   if (tail) t = *tail;
-  k_energy_finalize<<<dim3(4, n_blocks), 256, 0, st>>>(g, ep, blocks, pblock0, n_problems, groups, pgroup0, ce_n,
+  k_energy_finalize<<<n_blocks, 256, 0, st>>>(g, ep, blocks, pblock0, n_problems, groups, pgroup0, ce_n,
                                                         energies, rec, const_cast<int *>(d_step), rec_base, rec_cap,
                                                         n_blocks, norm_tol, status, status_step, t, done);
 }

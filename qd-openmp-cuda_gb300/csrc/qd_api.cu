@@ -821,6 +821,8 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   const qd_crp &c = d0->CRP;
   s->flux.enabled = c.calculate_CRP != 0;
   if (s->flux.enabled) {
+    if (s->precision == QD_PRECISION_MIXED && c.n_gradient_points > 32)
+      throw Error{QD_ERR_UNSUPPORTED, "mixed form: CRP.n_gradient_points above 32"};
     s->flux.n_energies = c.n_energies;
     s->flux.n_grad = c.n_gradient_points;
     s->flux.n_ds = c.n_dividing_surface;
