@@ -46,8 +46,8 @@ void launch_build_coriolis_phase(cudaStream_t s, const Grid &g, const CoriolisGr
   k_build_coriolis_phase<<<dim3(4, n_groups), 256, 0, s>>>(g, groups, e, dt, ph);
 }
 
-template <int MAXN>
-__global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, double2 *__restrict__ psi_j,
+template <int MAXN, typename S>
+__global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, S *__restrict__ psi_j,
                                                           const BlockDesc *__restrict__ blocks,
                                                           const CoriolisGroup *__restrict__ groups,
                                                           const double *__restrict__ Vp, const double2 *__restrict__ php,
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, double2 *__res
     if (o < n) {
       const BlockDesc bd = blocks[gr.block_lo + o];
       addr[o] = (int64_t)(bd.slab0 + (gr.l - bd.omega)) * g.npt + pt;
-      x[o] = active ? psi_j[addr[o]] : make_double2(0.0, 0.0);
+      x[o] = active ? load_c(psi_j + addr[o]) : make_double2(0.0, 0.0);
       if (tabP && active) x[o] = cmul(x[o], ldg2(tabP + (int64_t)gr.l * g.npt + pt));
     }
   }
@@ -122,19 +122,20 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, double2 *__res
           acc.y = fma(v, y[a].y, acc.y);
         }
       if (tabE) acc = cmul(acc, ldg2(tabE + (int64_t)gr.l * g.npt + pt));
-      psi_j[addr[o]] = acc;
+      store_c(psi_j + addr[o], acc);
     }
   }
 }
 
-void launch_coriolis(cudaStream_t s, const Grid &g, double2 *psi_j, const BlockDesc *blocks,
+template <typename S>
+void launch_coriolis(cudaStream_t s, const Grid &g, S *psi_j, const BlockDesc *blocks,
                      const CoriolisGroup *groups, int n_groups, int max_n, const double *V, const double2 *ph,
                      const double *H, double *ce_part, int ce_tiles, const double2 *tabE, const int *status,
                      const double2 *tabP) {
   if (n_groups == 0) return;
   dim3 grid((unsigned)coriolis_tiles(g), (unsigned)n_groups);
 #define QD_COR(M)                                                                                        \
-  k_coriolis<M><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, V, ph, H, ce_part, ce_tiles, max_n, \
+  k_coriolis<M, S><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, V, ph, H, ce_part, ce_tiles, max_n, \
                                              tabE, status, tabP)
   if (max_n <= 2) QD_COR(2);
   else if (max_n <= 4) QD_COR(4);
@@ -146,5 +147,11 @@ void launch_coriolis(cudaStream_t s, const Grid &g, double2 *psi_j, const BlockD
   else throw Error{QD_ERR_UNSUPPORTED, "more than 48 coupled Omega blocks"};
 #undef QD_COR
 }
+template void launch_coriolis<double2>(cudaStream_t, const Grid &, double2 *, const BlockDesc *,
+                                       const CoriolisGroup *, int, int, const double *, const double2 *,
+                                       const double *, double *, int, const double2 *, const int *, const double2 *);
+template void launch_coriolis<float2>(cudaStream_t, const Grid &, float2 *, const BlockDesc *, const CoriolisGroup *,
+                                      int, int, const double *, const double2 *, const double *, double *, int,
+                                      const double2 *, const int *, const double2 *);
 
 }  // namespace qd

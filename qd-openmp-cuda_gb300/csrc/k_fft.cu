@@ -200,12 +200,21 @@ template <typename R> __device__ inline typename CT<R>::T from_d(double2 v) {
 }
 __device__ inline double2 to_d(double2 v) { return v; }
 __device__ inline double2 to_d(float2 v) { return make_double2(f2d(v.x), f2d(v.y)); }
+// psi_j storage: c128 in the FP64 form, c64 in the mixed form (one rounding)
+__device__ inline void store_psi(double2 *p, double2 v) { *p = v; }
+__device__ inline void store_psi(float2 *p, double2 v) { *p = make_float2(d2f_rn(v.x), d2f_rn(v.y)); }
+// FP32 result (x, y) times the transform scale: exact power of two in FP32, else
+// the product formed in FP64 and rounded once
+__device__ inline float2 scaled_c64(float x, float y, float fscale, double scale) {
+  if (fscale != 0.0f) return make_float2(x * fscale, y * fscale);
+  return make_float2(d2f_rn(f2d(x) * scale), d2f_rn(f2d(y) * scale));
+}
 
 }  // namespace
 
 // ---------------------------------------------------------- rows forward
 template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2 : 1) k_fft_rows(double2 *__restrict__ psi, Radices rd, int nrows,
+__global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2 : 1) k_fft_rows(typename CT<R>::T *__restrict__ psi, Radices rd, int nrows,
                                                           int n_rows_total, const typename CT<R>::T *__restrict__ tw,
                                                           int inv, Grid g, double scale,
                                                           const SlabDesc *__restrict__ slabs,
@@ -227,12 +236,12 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
   const bool lift = std::is_same<R, float>::value && liftR != nullptr;
   {
     // all of this thread's loads are issued before any is used
-    double2 raw[MAXV];
+    C raw[MAXV];
 #pragma unroll
     for (int u = 0; u < MAXV; u++) {
       const int e = threadIdx.x + FFT_THREADS * u;
       const int grow = row0 + (int)fdiv(rd.fn, (uint32_t)e);
-      raw[u] = (e < n && grow < n_rows_total) ? psi[(int64_t)row0 * N + e] : make_double2(0.0, 0.0);
+      raw[u] = (e < n && grow < n_rows_total) ? psi[(int64_t)row0 * N + e] : CT<R>::make(0, 0);
     }
 #pragma unroll
     for (int u = 0; u < MAXV; u++) {
@@ -240,7 +249,7 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
       if (e >= n) break;
       const int rl = (int)fdiv(rd.fn, (uint32_t)e);
       const int grow = row0 + rl;
-      C v = from_d<R>(raw[u]);
+      C v = raw[u];
       if (lift && !inv && grow < n_rows_total) {
         const int sl = (int)fdiv(fn2, (uint32_t)grow);
         const int l = slabs[sl].l, i = e - rl * N, j = grow - sl * g.n2;
@@ -264,9 +273,9 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
     const int i = e - rl * N;
     const int sl = (int)fdiv(fn2, (uint32_t)grow);
     const int j = grow - sl * g.n2;
-    if (std::is_same<R, float>::value && inv) {
+    if constexpr (std::is_same<R, float>::value) {
+     if (inv) {
       float x = (float)buf[e].x, y = (float)buf[e].y;
-      double2 v;
       if (fscale != 0.0f) {   // exact FP32 scale (power of two)
         x *= fscale;
         y *= fscale;
@@ -276,19 +285,15 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
         lift2(x, y, __ldg(liftR + (int64_t)l * g.n1 + i));
         lift2(x, y, __ldg(liftr + (int64_t)l * g.n2 + j));
       }
-      if (fscale != 0.0f) {
-        v = make_double2(f2d(x), f2d(y));
-      } else {
-        v = make_double2(f2d(x) * scale, f2d(y) * scale);
-      }
       if (re_part) {
         const float Rr = (float)(g.left1 + i * g.dr1), rr = (float)(g.left2 + j * g.dr2);
         const float I = 1.0f / (2.0f * (float)g.m1 * Rr * Rr) + 1.0f / (2.0f * (float)g.m2 * rr * rr);
         const float s2 = fscale != 0.0f ? 1.0f : (float)(scale * scale);
         ref = fmaf((float)l * (float)(l + 1) * I * s2, x * x + y * y, ref);
       }
-      psi[(int64_t)grow * N + i] = v;
+      psi[(int64_t)grow * N + i] = fscale != 0.0f ? make_float2(x, y) : scaled_c64(x, y, 0.0f, scale);
       continue;
+     }
     }
     double2 v = to_d(buf[e]);
     if (scale != 1.0) { v.x *= scale; v.y *= scale; }
@@ -302,7 +307,7 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
       const double I = 1.0 / (2 * g.m1 * Rr * Rr) + 1.0 / (2 * g.m2 * rr * rr);
       re += (double)l * (l + 1) * I * (v.x * v.x + v.y * v.y);
     }
-    psi[(int64_t)grow * N + i] = v;
+    store_psi(psi + (int64_t)grow * N + i, v);
   }
   if (re_part) {
     re = block_sum(re + (double)ref, red);
@@ -316,7 +321,7 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
 
 // ------------------------------------- columns: forward, kinetic, inverse
 template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2 : 1) k_fft_cols(double2 *__restrict__ psi, Radices rd, int ncols, Grid g,
+__global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2 : 1) k_fft_cols(typename CT<R>::T *__restrict__ psi, Radices rd, int ncols, Grid g,
                                                           const typename CT<R>::T *__restrict__ tw,
                                                           const double2 *__restrict__ tab_kin,
                                                           const double *__restrict__ T1, const double *__restrict__ T2,
@@ -334,20 +339,20 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
   const int64_t sl = blockIdx.x / tiles;
   const int tile = blockIdx.x % tiles;
   const int i0 = tile * ncols;
-  double2 *p = psi + sl * g.npt + i0;
+  C *p = psi + sl * g.npt + i0;
   const int n = ncols * N;
   {
-    double2 raw[MAXV];
+    C raw[MAXV];
 #pragma unroll
     for (int u = 0; u < MAXV; u++) {
       const int e = threadIdx.x + FFT_THREADS * u;
       const int t = (int)fdiv(fncols, (uint32_t)e);
-      raw[u] = e < n ? p[(int64_t)t * g.n1 + (e - t * ncols)] : make_double2(0.0, 0.0);
+      raw[u] = e < n ? p[(int64_t)t * g.n1 + (e - t * ncols)] : CT<R>::make(0, 0);
     }
 #pragma unroll
     for (int u = 0; u < MAXV; u++) {
       const int e = threadIdx.x + FFT_THREADS * u;
-      if (e < n) buf[e] = from_d<R>(raw[u]);
+      if (e < n) buf[e] = raw[u];
     }
   }
   __syncthreads();
@@ -375,7 +380,7 @@ __global__ void __launch_bounds__(FFT_THREADS, std::is_same<R, float>::value ? 2
   fft_run<R, true>(buf, rd, ncols, 1, ncols, tw, true, fncols);
   for (int e = threadIdx.x; e < n; e += FFT_THREADS) {
     const int t = (int)fdiv(fncols, (uint32_t)e), c = e - t * ncols;
-    p[(int64_t)t * g.n1 + c] = to_d(buf[e]);
+    p[(int64_t)t * g.n1 + c] = buf[e];
   }
   if (ke_part) {
     ke = block_sum(ke, red);
@@ -393,7 +398,7 @@ constexpr int SLAB_THREADS = 512;
 constexpr int SLAB_MV = 8;   // values per thread per stage: n1 n2 / C <= 4096
 
 __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
-    double2 *__restrict__ psi, Radices r1d, Radices r2d, int C, Grid g, const SlabDesc *__restrict__ slabs,
+    float2 *__restrict__ psi, Radices r1d, Radices r2d, int C, Grid g, const SlabDesc *__restrict__ slabs,
     const float2 *__restrict__ tw1, const float2 *__restrict__ tw2, FFTLift lf, double *__restrict__ ke_part,
     double *__restrict__ re_part, float fscale, double scale, FastDiv fcols, const int *status) {
   if (status && *status) return;   // uniform over the cluster: every CTA reads the same flag
@@ -411,24 +416,24 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
   const int c = (int)cluster.block_rank();
   const int sl = blockIdx.x / C;
   const int l = slabs[sl].l;
-  double2 *P = psi + (int64_t)sl * g.npt;
+  float2 *P = psi + (int64_t)sl * g.npt;
   const int r0 = c * rows, k0 = c * cols;
   const int n = rows * n1;   // == n2 * cols
   const int tid = threadIdx.x;
 
   // 1. rows -> Xr (FP32), rotational phase before the forward transform
   {
-    double2 raw[SLAB_MV];
+    float2 raw[SLAB_MV];
 #pragma unroll
     for (int u = 0; u < SLAB_MV; u++) {
       const int e = tid + SLAB_THREADS * u;
-      raw[u] = e < n ? __ldcs(P + (int64_t)r0 * n1 + e) : make_double2(0.0, 0.0);
+      raw[u] = e < n ? __ldcs(P + (int64_t)r0 * n1 + e) : make_float2(0.0f, 0.0f);
     }
 #pragma unroll
     for (int u = 0; u < SLAB_MV; u++) {
       const int e = tid + SLAB_THREADS * u;
       if (e >= n) break;
-      float x = d2f_rn(raw[u].x), y = d2f_rn(raw[u].y);
+      float x = raw[u].x, y = raw[u].y;
       if (lf.proR) {
         const int rl = (int)fdiv(r1d.fn, (uint32_t)e);
         const int i = e - rl * n1;
@@ -502,8 +507,7 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
       const float I = __ldg(lf.I1f + i) + __ldg(lf.I2f + j);
       ref = fmaf(lls2 * I, x * x + y * y, ref);
     }
-    __stcs(P + (int64_t)r0 * n1 + e,
-           fscale != 0.0f ? make_double2(f2d(x), f2d(y)) : make_double2(f2d(x) * scale, f2d(y) * scale));
+    __stcs(P + (int64_t)r0 * n1 + e, fscale != 0.0f ? make_float2(x, y) : scaled_c64(x, y, 0.0f, scale));
   }
   const double ke = block_sum((double)kef, red);
   const double re = block_sum((double)ref, red);
@@ -632,7 +636,7 @@ __device__ __forceinline__ void tw_apply(float2 &v, const float2 *tab, int e, in
 // floats2 at Xr + q RS, used as the row transposition buffer and then as the
 // row the other CTAs gather from.  Column transposition buffer Sc[k1][j][col].
 template <int A, int B1, int B2, int THREADS>
-__global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(double2 *__restrict__ psi, Grid g,
+__global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(float2 *__restrict__ psi, Grid g,
                                                              const SlabDesc *__restrict__ slabs,
                                                              const float2 *__restrict__ tw1,
                                                              const float2 *__restrict__ tw2, FFTLift lf,
@@ -660,7 +664,7 @@ __global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(double2 *__restrict
   const int c = (int)cluster.block_rank();
   const int sl = blockIdx.x / C;
   const int l = slabs[sl].l;
-  double2 *P = psi + (int64_t)sl * g.npt;
+  float2 *P = psi + (int64_t)sl * g.npt;
   float ke1 = 0.0f, ke2 = 0.0f, ref = 0.0f;
   float2 v[A];
 
@@ -668,14 +672,9 @@ __global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(double2 *__restrict
   {
     const int q = tid / B1, j = tid % B1;
     const int r = c * RPC + q;
-    const double2 *src = P + (int64_t)r * N1 + j;
-    {
-      double2 raw[A];
+    const float2 *src = P + (int64_t)r * N1 + j;
 #pragma unroll
-      for (int m = 0; m < A; m++) raw[m] = __ldcs(src + B1 * m);
-#pragma unroll
-      for (int m = 0; m < A; m++) v[m] = make_float2(d2f_rn(raw[m].x), d2f_rn(raw[m].y));
-    }
+    for (int m = 0; m < A; m++) v[m] = __ldcs(src + B1 * m);
     if (lf.proR) {
       const float2 pr = __ldg(lf.pror + (int64_t)l * N2 + r);
 #pragma unroll
@@ -793,8 +792,7 @@ __global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(double2 *__restrict
       lift2(x, y, __ldg(lf.epir + (int64_t)l * N2 + rr));
     }
     if (re_part) ref = fmaf(lls2 * (I1 + __ldg(lf.I2f + rr)), x * x + y * y, ref);
-    __stcs(P + (int64_t)rr * N1 + R,
-           fscale != 0.0f ? make_double2(f2d(x), f2d(y)) : make_double2(f2d(x) * scale, f2d(y) * scale));
+    __stcs(P + (int64_t)rr * N1 + R, fscale != 0.0f ? make_float2(x, y) : scaled_c64(x, y, 0.0f, scale));
   }
   // partial sums: FP32 within a warp, FP64 across warps in a fixed order
   float kew = fmaf((float)N2, ke1, ke2 * (1.0f / (float)N1)), rew = ref;
@@ -848,7 +846,7 @@ void sep_set_attr() {
 }
 
 template <int A, int B1, int B2, int T>
-void sep_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j, const SlabDesc *slabs, int n_slabs,
+void sep_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, const SlabDesc *slabs, int n_slabs,
                 const FFTLift &lf, double *ke_part, double *re_part, float fscale, double scale, const int *status) {
   const int C = sep_cluster<A, B1, B2, T>();
   cudaLaunchConfig_t cfg{};
@@ -884,7 +882,7 @@ int sep_dispatch_cluster(int id) {
   }
   return 0;
 }
-void sep_dispatch_launch(int id, cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j,
+void sep_dispatch_launch(int id, cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j,
                          const SlabDesc *slabs, int n_slabs, const FFTLift &lf, double *ke_part, double *re_part,
                          float fscale, double scale, const int *status) {
   switch (id) {
@@ -999,7 +997,7 @@ int fft_row_tiles(const FFTPlan &p, int precision) {
 
 
 template <typename R>
-static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j,
+static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p, typename CT<R>::T *psi_j,
                                  const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1,
                                  const double *T2, double *ke_part, const double2 *tabE, double *re_part,
                                  const int *status, const FFTLift *lf) {
@@ -1029,12 +1027,13 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
   const double scale = 1.0 / ((double)g.n1 * g.n2);
   const bool pow2 = ((g.n1 * g.n2) & (g.n1 * g.n2 - 1)) == 0;
   const float fscale = pow2 ? (float)scale : 0.0f;
-  if (std::is_same<R, float>::value && p.sep >= 0 && lf && lf->kinR) {
+  if constexpr (std::is_same<R, float>::value) {
+  if (p.sep >= 0 && lf && lf->kinR) {
     sep_dispatch_launch(p.sep, s, g, p, psi_j, slabs, n_slabs, *lf, ke_part, re_part, fscale, scale, status);
     prof_mark(s, "fft_slab");
     return;
   }
-  if (std::is_same<R, float>::value && p.cluster && lf && lf->kinR) {
+  if (p.cluster && lf && lf->kinR) {
     const int C = p.cluster;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)(n_slabs * C));
@@ -1053,6 +1052,7 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
     prof_mark(s, "fft_slab");
     return;
   }
+  }
   k_fft_rows<R><<<nrow_ctas, FFT_THREADS, sm_rows, s>>>(psi_j, r1, p.rows_per_cta, rows, tw1, 0, g, 1.0, slabs,
                                                         nullptr, nullptr, 0, status, lf ? lf->proR : nullptr,
                                                         lf ? lf->pror : nullptr, 0.0f, fn2);
@@ -1069,16 +1069,19 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
   prof_mark(s, "fft_rows_inverse");
 }
 
-void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, int precision, double2 *psi_j,
-                        const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1, const double *T2,
-                        double *ke_part, const double2 *tabE, const double *, const double *, double *re_part,
-                        const int *status, const FFTLift *lift) {
+void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j, const SlabDesc *slabs,
+                        int n_slabs, const double2 *tab_kin, const double *T1, const double *T2, double *ke_part,
+                        const double2 *tabE, double *re_part, const int *status) {
   if (n_slabs == 0) return;
-  if (precision == QD_PRECISION_MIXED)
-    launch_fft_kinetic_t<float>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status, lift);
-  else
-    launch_fft_kinetic_t<double>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status,
-                                 nullptr);
+  launch_fft_kinetic_t<double>(s, g, p, psi_j, slabs, n_slabs, tab_kin, T1, T2, ke_part, tabE, re_part, status,
+                               nullptr);
+}
+
+void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, const SlabDesc *slabs,
+                        int n_slabs, double *ke_part, double *re_part, const int *status, const FFTLift *lift) {
+  if (n_slabs == 0) return;
+  launch_fft_kinetic_t<float>(s, g, p, psi_j, slabs, n_slabs, nullptr, nullptr, nullptr, ke_part, nullptr, re_part,
+                              status, lift);
 }
 
 }  // namespace qd

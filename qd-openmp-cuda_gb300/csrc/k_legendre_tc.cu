@@ -30,6 +30,8 @@
 // epilogue also reduces the module and potential energy.
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "qd_internal.h"
 #include "qd_device.cuh"
 
@@ -198,8 +200,8 @@ __global__ void k_build_tc_bimage(const BlockDesc *__restrict__ blocks, const do
 
 struct TcArgs {
   Grid g;
-  const double2 *A;          // fwd: psi_theta pool, bwd: psi_j pool
-  double2 *C;                // fwd: psi_j pool, bwd: psi_theta pool
+  const void *A;             // fwd: psi_theta pool (double2), bwd: psi_j pool (float2)
+  void *C;                   // fwd: psi_j pool (float2), bwd: psi_theta pool (double2)
   const BlockDesc *blocks;
   const uint16_t *bimg;      // B images
   const int64_t *bimg_off;   // per block byte offset
@@ -225,221 +227,6 @@ __device__ inline void rot_lift2(float &x, float &y, float2 ts) {
   x = fmaf(ts.x, y, x);
 }
 
-template <bool FWD>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_legendre_tc(TcArgs P) {
-  if (P.status && *P.status) return;
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t mbar;
-  __shared__ uint32_t tmem_base_s;
-  __shared__ double red[32];
-  __shared__ float srow_s[128];
-  const BlockDesc bd = P.blocks[blockIdx.y];
-  const Grid &g = P.g;
-  const int Kv = FWD ? g.nth : bd.nl, Nv = FWD ? bd.nl : g.nth;
-  const int Kp = round16(Kv), Np = round16(Nv);
-  const uint32_t SBO_A = (uint32_t)(Kp / 8 * 128), SBO_B = SBO_A;
-  const uint32_t A_TERM = 16u * SBO_A;                 // 128 rows
-  const uint32_t B_TERM = (uint32_t)(Np / 8) * SBO_B;
-  const int LDF = Kp + 1;                              // padded FP32 staging row
-  unsigned char *sA = smem;
-  unsigned char *sB = smem + 3 * A_TERM;
-  float *sF = reinterpret_cast<float *>(sB + 3 * B_TERM);
-  float *sWV = sF + 128 * LDF;   // backward: w_k V(k, p) of the tile, [k][64]
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t p0 = (int64_t)blockIdx.x * TC_POINTS;
-  const uint32_t ncols = tc_tmem_cols(Np);
-
-  if (warp == 0) tmem_alloc(smem_u32(&tmem_base_s), ncols);
-  if (tid == 0) {
-    mbar_init(smem_u32(&mbar), 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-
-  // ---- backward: w_k V(k, p) of the tile, needed by the epilogue
-  if (!FWD) {
-    for (int q = tid; q < Np * TC_POINTS; q += TC_THREADS) {
-      const int k = q / TC_POINTS, pl2 = q % TC_POINTS;
-      const int64_t p = p0 + pl2;
-      sWV[q] = (k < Nv && p < g.npt) ? __ldg(P.wv + (int64_t)k * g.npt + p) : 0.0f;
-    }
-  }
-  // ---- B image -> shared memory
-  {
-    const uint4 *src = reinterpret_cast<const uint4 *>(P.bimg + P.bimg_off[blockIdx.y] / 2);
-    uint4 *dst = reinterpret_cast<uint4 *>(sB);
-    const int n16 = (int)(tc_bimg_bytes(Np, Kp) / 16);
-    for (int q = tid; q < n16; q += TC_THREADS) dst[q] = __ldg(src + q);
-  }
-  // ---- phase 1: A tile as FP32 rows (row 2p = re, 2p+1 = im), phases applied.
-  // Eight independent loads per thread are in flight before any is used.
-  {
-    const double2 *A = FWD ? P.A + (int64_t)blockIdx.y * g.nth * g.npt : P.A + (int64_t)bd.slab0 * g.npt;
-    const int total = TC_POINTS * Kp;
-    constexpr int U = 8;
-    static_assert(TC_THREADS % TC_POINTS == 0, "a thread stages one point");
-    // every item of this thread has the same point (it % 64 == tid % 64)
-    const int64_t pme = p0 + (tid % TC_POINTS);
-    float msk = 1.0f;
-    if (FWD && P.d1 && pme < g.npt) {
-      const int ip = (int)(pme % g.n1);
-      msk = P.d1[ip] * P.d2[(int)(pme / g.n1)];
-    }
-    for (int base = tid; base < total; base += TC_THREADS * U) {
-      double2 v[U];
-      float2 ts[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int it = base + u * TC_THREADS;
-        const int pl = it % TC_POINTS, k = it / TC_POINTS;
-        const int64_t p = p0 + pl;
-        const bool in = it < total && k < Kv && p < g.npt;
-        v[u] = in ? A[(int64_t)k * g.npt + p] : make_double2(0.0, 0.0);
-        if (FWD) ts[u] = (in && P.vph) ? __ldg(P.vph + (int64_t)k * g.npt + p) : make_float2(0.0f, 0.0f);
-      }
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int it = base + u * TC_THREADS;
-        if (it >= total) break;
-        const int pl = it % TC_POINTS, k = it / TC_POINTS;
-        const int64_t p = p0 + pl;
-        float x = d2f_rn(v[u].x), y = d2f_rn(v[u].y);
-        if (FWD && p < g.npt) {
-          x *= msk;
-          y *= msk;
-          if (P.vph) rot_lift2(x, y, ts[u]);
-        }
-        sF[(2 * pl) * LDF + k] = x;
-        sF[(2 * pl + 1) * LDF + k] = y;
-      }
-    }
-  }
-  __syncthreads();
-  // ---- phase 2: threads 2m and 2m+1 scale and slice row m (halves of K)
-  {
-    const int m = tid >> 1, half = tid & 1;
-    const float *row = sF + m * LDF;
-    float mx = 0.0f;
-    for (int k = 0; k < Kp; k++) mx = fmaxf(mx, fabsf(row[k]));
-    // rows below 1e-30 (far below any value that reaches a norm or a flux)
-    // are set to zero so that the power-of-two scale stays a normal float
-    int e = 0;
-    if (mx >= 1e-30f) frexpf(mx, &e);
-    const float inv = mx >= 1e-30f ? ldexpf(1.0f, -e) * 256.0f : 0.0f;
-    if (half == 0) srow_s[m] = ldexpf(1.0f, e - 16);   // s_m 2^-16 (the two 2^-8 of i0 j0)
-    const uint32_t orow = (uint32_t)(m / 8) * SBO_A + (m % 8) * 16;
-    const int kgs = Kp / 8;
-    for (int kg = half; kg < kgs; kg += 2) {
-      uint32_t w[3][4];
-#pragma unroll
-      for (int e8 = 0; e8 < 8; e8++) {
-        const float a = row[kg * 8 + e8] * inv;      // exact power-of-two scaling
-        const float i0 = rintf(a);
-        const float r1 = (a - i0) * 256.0f;          // exact
-        const float i1 = rintf(r1);
-        const float i2 = rintf((r1 - i1) * 256.0f);
-        const uint16_t h0 = __bfloat16_as_ushort(__float2bfloat16_rn(i0));
-        const uint16_t h1 = __bfloat16_as_ushort(__float2bfloat16_rn(i1));
-        const uint16_t h2 = __bfloat16_as_ushort(__float2bfloat16_rn(i2));
-        if (e8 & 1) {
-          w[0][e8 >> 1] |= (uint32_t)h0 << 16;
-          w[1][e8 >> 1] |= (uint32_t)h1 << 16;
-          w[2][e8 >> 1] |= (uint32_t)h2 << 16;
-        } else {
-          w[0][e8 >> 1] = h0;
-          w[1][e8 >> 1] = h1;
-          w[2][e8 >> 1] = h2;
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < 3; t++)
-        *reinterpret_cast<uint4 *>(sA + t * A_TERM + orow + kg * 128) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
-    }
-  }
-  // make the generic-proxy shared stores visible to the tensor core (async proxy)
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = tmem_base_s;
-
-  if (tid == 0) {
-    const uint32_t idesc = make_idesc(128, Np);
-    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-    for (int s = 0; s < Kp / 16; s++) {
-#pragma unroll
-      for (int q = 0; q < 6; q++) {
-        const int d = c_pair_a[q] + c_pair_b[q];            // slice order -> accumulator
-        const uint64_t ad = make_desc(a0 + c_pair_a[q] * A_TERM + s * 256, 128, SBO_A);
-        const uint64_t bdsc = make_desc(b0 + c_pair_b[q] * B_TERM + s * 256, 128, SBO_B);
-        const bool first = s == 0 && (q == 0 || q == 1 || q == 3);
-        mma_bf16(tmem + (uint32_t)(d * Np), ad, bdsc, idesc, first ? 0u : 1u);
-      }
-    }
-    mma_commit(smem_u32(&mbar));
-  }
-  // ---- wait for the MMA chain (bounded in wall-clock time); on a timeout
-  // flag the error, wait once more (bounded) for the chain, free TMEM, return
-  bool ok = false;
-  {
-    const uint64_t t0 = globaltimer();
-    while (!(ok = mbar_try_wait(smem_u32(&mbar), 0)))
-      if (globaltimer() - t0 > WAIT_NS) break;
-  }
-  if (!ok) {
-    if (tid == 0 && P.status_w) atomicCAS(P.status_w, 0, QD_ERR_CUDA);
-    const uint64_t t0 = globaltimer();
-    while (!mbar_try_wait(smem_u32(&mbar), 0))
-      if (globaltimer() - t0 > WAIT_NS) break;
-  }
-  tc_fence_after();
-
-  // ---- epilogue: warp w reads TMEM lanes 32(w%4) .. +31 (rows), column chunks
-  // n0 = 16 (w/4) + 32 j; row m -> point m/2, component m%2
-  const int quarter = warp & 3, cgrp = warp >> 2;
-  const int m = 32 * quarter + lane;
-  const int pl = m >> 1, c = m & 1;
-  const int64_t p = p0 + pl;
-  const float srow = srow_s[m];
-  const float *tsc = P.bscale + (int64_t)blockIdx.y * 256;
-  float mod = 0.0f, pe = 0.0f;
-  double *Cd = reinterpret_cast<double *>(P.C);
-  const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
-  for (int n0 = 16 * cgrp; n0 < Np; n0 += 32) {
-    float d0[16], d1[16], d2[16];
-    tmem_ld16(trow + (uint32_t)n0, d0);
-    tmem_ld16(trow + (uint32_t)(Np + n0), d1);
-    tmem_ld16(trow + (uint32_t)(2 * Np + n0), d2);
-    if (!ok || p >= g.npt) continue;
-#pragma unroll
-    for (int q = 0; q < 16; q++) {
-      const int n = n0 + q;
-      if (n >= Nv) break;
-      const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc[n]);
-      if (FWD) {
-        Cd[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = f2d(v);
-      } else {
-        Cd[2 * (((int64_t)blockIdx.y * g.nth + n) * g.npt + p) + c] = f2d(v);
-        const float v2 = v * v;
-        mod = fmaf(__ldg(P.w + n), v2, mod);
-        pe = fmaf(sWV[n * TC_POINTS + pl], v2, pe);
-      }
-    }
-  }
-  if (!FWD && P.part) {
-    const double m2 = block_sum((double)mod, red);
-    const double p2 = block_sum((double)pe, red);
-    if (tid == 0) {
-      P.part[((int64_t)blockIdx.y * P.n_part_tiles + blockIdx.x) * 2 + 0] = m2;
-      P.part[((int64_t)blockIdx.y * P.n_part_tiles + blockIdx.x) * 2 + 1] = p2;
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0) {
-    tc_fence_after();
-    tmem_dealloc(tmem, ncols);
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Persistent, warp-specialised form.  Each CTA walks a contiguous range of
@@ -495,6 +282,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   __shared__ uint32_t tmem_base_s;
   __shared__ float srow_s[2][128];
   __shared__ float red_s[16];
+  __shared__ float tsc_s[256], w_s[256];   // consumers: column scales and (backward) weights of the block
   __shared__ int abort_p, abort_c, n_issued;
   const Grid &g = P.g;
   const uint32_t a_term_max = 16u * (uint32_t)(kp_max / 8 * 128);
@@ -530,17 +318,21 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       const BlockDesc bd = P.blocks[T.b];
       const int64_t p0 = (int64_t)T.mt * TC_POINTS;
       const int LDF = T.Kp + 1;
-      const double2 *A = FWD ? P.A + (int64_t)T.b * g.nth * g.npt : P.A + (int64_t)bd.slab0 * g.npt;
+      using AT = typename std::conditional<FWD, double2, float2>::type;   // psi_theta c128, psi_j c64
+      const AT *A = reinterpret_cast<const AT *>(P.A) + (FWD ? (int64_t)T.b * g.nth * g.npt : (int64_t)bd.slab0 * g.npt);
       // L2 prefetch of the next tile (128-byte lines of its k rows)
       if (tt + 1 < t_end) {
         const TcTile Tn = tc_tile<FWD>(P, tt + 1, mtiles);
         const BlockDesc bn = P.blocks[Tn.b];
-        const double2 *An = FWD ? P.A + (int64_t)Tn.b * g.nth * g.npt : P.A + (int64_t)bn.slab0 * g.npt;
+        const AT *An = reinterpret_cast<const AT *>(P.A) +
+                       (FWD ? (int64_t)Tn.b * g.nth * g.npt : (int64_t)bn.slab0 * g.npt);
         const int64_t pn = (int64_t)Tn.mt * TC_POINTS;
-        const int lines = Tn.Kv * 8;   // 64 points x 16 B = 8 lines per k row
+        constexpr int LPR = FWD ? 8 : 4;                // 128-byte lines per k row: 64 points x 16 or 8 B
+        constexpr int PPL = TC_POINTS / LPR;            // points per line
+        const int lines = Tn.Kv * LPR;
         for (int q = tid; q < lines; q += WS_PROD) {
-          const int k = q >> 3, ln = q & 7;
-          const int64_t pp = pn + ln * 8;
+          const int k = q / LPR, ln = q % LPR;
+          const int64_t pp = pn + ln * PPL;
           if (pp < g.npt) asm volatile("prefetch.global.L2 [%0];" ::"l"(An + (int64_t)k * g.npt + pp));
           if (FWD && P.vph && (ln & 1) == 0 && pp < g.npt)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(P.vph + (int64_t)k * g.npt + pp));
@@ -552,23 +344,33 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         const int64_t p = p0 + pl;
         float msk = 1.0f;
         if (FWD && P.d1 && p < g.npt) msk = P.d1[(int)(p % g.n1)] * P.d2[(int)(p / g.n1)];
-        constexpr int U = 12;
+        constexpr int U = FWD ? 12 : 24;
         const int nk = T.Kp / 4;   // this thread's k values: tid/64 + 4u
         for (int u0 = 0; u0 < nk; u0 += U) {
-          double2 v[U];
+          AT v[U];
           float2 ts[U];
 #pragma unroll
           for (int u = 0; u < U; u++) {
             const int k = tid / TC_POINTS + 4 * (u0 + u);
             const bool in = u0 + u < nk && k < T.Kv && p < g.npt;
-            v[u] = in ? A[(int64_t)k * g.npt + p] : make_double2(0.0, 0.0);
+            if (in)
+              v[u] = A[(int64_t)k * g.npt + p];
+            else
+              v[u].x = v[u].y = 0;
             if (FWD) ts[u] = (in && P.vph) ? __ldg(P.vph + (int64_t)k * g.npt + p) : make_float2(0.0f, 0.0f);
           }
 #pragma unroll
           for (int u = 0; u < U; u++) {
             if (u0 + u >= nk) break;
             const int k = tid / TC_POINTS + 4 * (u0 + u);
-            float x = d2f_rn(v[u].x), y = d2f_rn(v[u].y);
+            float x, y;
+            if constexpr (FWD) {
+              x = d2f_rn(v[u].x);
+              y = d2f_rn(v[u].y);
+            } else {
+              x = v[u].x;
+              y = v[u].y;
+            }
             if (FWD) {
               x *= msk;
               y *= msk;
@@ -644,9 +446,20 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
     const int quarter = warp & 3, chalf = cw >> 2;
     const int m = 32 * quarter + lane;
     const int pl = m >> 1, c = m & 1;
+    int cons_b = -1;
     for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
       const TcTile T = tc_tile<FWD>(P, tt, mtiles);
       const BlockDesc bd = P.blocks[T.b];
+      const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
+      // backward: this thread's first chunk of w V, requested before the MMA wait
+      float wv[16];
+      if (!FWD) {
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const int n = 16 * chalf + q;
+          wv[q] = (n < T.Nv && p < g.npt) ? __ldg(P.wv + (int64_t)n * g.npt + p) : 0.0f;
+        }
+      }
       if (ctid == 0) {
         bool ok = mbar_wait_bounded(smem_u32(&mb_ready), (uint32_t)(it & 1));
         if (ok && it > 0) ok = mbar_wait_bounded(smem_u32(&mb_free), (uint32_t)((it - 1) & 1));
@@ -680,37 +493,54 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       __syncwarp();
       named_bar(2, WS_THREADS - WS_PROD);
       if (abort_c) break;
+      if (T.b != cons_b) {
+        for (int n = ctid; n < 256; n += WS_THREADS - WS_PROD) {
+          tsc_s[n] = n < T.Np ? __ldg(P.bscale + (int64_t)T.b * 256 + n) : 0.0f;
+          if (!FWD) w_s[n] = n < T.Nv ? __ldg(P.w + n) : 0.0f;
+        }
+        cons_b = T.b;
+        named_bar(2, WS_THREADS - WS_PROD);
+      }
       tc_fence_after();
-      const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
       const float srow = srow_s[it & 1][m];
-      const float *tsc = P.bscale + (int64_t)T.b * 256;
       float mod = 0.0f, pe = 0.0f;
-      double *Cd = reinterpret_cast<double *>(P.C);
+      double *Cd = reinterpret_cast<double *>(P.C);   // backward: psi_theta, c128
+      float *Cf = reinterpret_cast<float *>(P.C);     // forward: psi_j, c64
       const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
       for (int n0 = 16 * chalf; n0 < T.Np; n0 += 32) {
-        float d0[16], d1[16], d2[16], wv[16];
+        // the next chunk's w V values are requested before this chunk is used
+        float wv_nxt[16];
         if (!FWD) {
 #pragma unroll
-          for (int q = 0; q < 16; q++)
-            wv[q] = (n0 + q < T.Nv && p < g.npt) ? __ldg(P.wv + (int64_t)(n0 + q) * g.npt + p) : 0.0f;
+          for (int q = 0; q < 16; q++) {
+            const int n = n0 + 32 + q;
+            wv_nxt[q] = (n < T.Nv && p < g.npt) ? __ldg(P.wv + (int64_t)n * g.npt + p) : 0.0f;
+          }
         }
+        float d0[16], d1[16], d2[16];
         tmem_ld16(trow + (uint32_t)n0, d0);
         tmem_ld16(trow + (uint32_t)(T.Np + n0), d1);
         tmem_ld16(trow + (uint32_t)(2 * T.Np + n0), d2);
-        if (p >= g.npt) continue;
+        if (p < g.npt) {
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const int n = n0 + q;
-          if (n >= T.Nv) break;
-          const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc[n]);
-          if (FWD) {
-            Cd[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = f2d(v);
-          } else {
-            Cd[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = f2d(v);
-            const float v2 = v * v;
-            mod = fmaf(__ldg(P.w + n), v2, mod);
-            pe = fmaf(wv[q], v2, pe);
+          for (int q = 0; q < 16; q++) {
+            const int n = n0 + q;
+            const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc_s[n]);
+            if (n < T.Nv) {
+              if (FWD) {
+                Cf[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = v;
+              } else {
+                Cd[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = f2d(v);
+                const float v2 = v * v;
+                mod = fmaf(w_s[n], v2, mod);
+                pe = fmaf(wv[q], v2, pe);
+              }
+            }
           }
+        }
+        if (!FWD) {
+#pragma unroll
+          for (int q = 0; q < 16; q++) wv[q] = wv_nxt[q];
         }
       }
       tc_fence_before();
@@ -789,7 +619,7 @@ void launch_legendre_tc_ws(cudaStream_t s, bool fwd, const TcArgs &a, int n_bloc
 }
 
 
-void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, double2 *psi_j,
+void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, float2 *psi_j,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
                             int *status_w, const float *bscale, int max_nl) {
@@ -810,7 +640,7 @@ void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th
   launch_legendre_tc_ws(s, true, a, n_blocks, round16(g.nth), round16(max_nl));
 }
 
-void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j, double2 *psi_th,
+void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, double2 *psi_th,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
                             const int *status, int *status_w, const float *bscale, int max_nl) {
@@ -833,8 +663,7 @@ void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j,
 }
 
 void tc_set_smem_limit(size_t bytes) {
-  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  (void)bytes;
   QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
 }

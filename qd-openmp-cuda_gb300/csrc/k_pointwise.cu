@@ -27,23 +27,29 @@ void launch_theta_phase(cudaStream_t s, double2 *psi, const double2 *tab, int n_
   k_theta_phase<<<grid_for(n, 256), 256, 0, s>>>(psi, tab, n, n_per_block, status);
 }
 
-__global__ void k_slab_phase(double2 *__restrict__ psi_j, const double2 *__restrict__ tab,
+template <typename S>
+__global__ void k_slab_phase(S *__restrict__ psi_j, const double2 *__restrict__ tab,
                              const SlabDesc *__restrict__ slabs, int64_t npt, const int *status) {
   if (status && *status) return;
   const int sl = blockIdx.y;
   const int l = slabs[sl].l;
-  double2 *p = psi_j + (int64_t)sl * npt;
+  S *p = psi_j + (int64_t)sl * npt;
   const double2 *t = tab + (int64_t)l * npt;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npt; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = cmul(p[i], ldg2(t + i));
+    store_c(p + i, cmul(load_c(p + i), ldg2(t + i)));
 }
 
-void launch_slab_phase(cudaStream_t s, double2 *psi_j, const double2 *tab, const SlabDesc *slabs, int n_slabs,
+template <typename S>
+void launch_slab_phase(cudaStream_t s, S *psi_j, const double2 *tab, const SlabDesc *slabs, int n_slabs,
                        int64_t npt, const int *status) {
   if (n_slabs == 0) return;
   dim3 grid((unsigned)std::min<int64_t>((npt + 255) / 256, 64), n_slabs);
-  k_slab_phase<<<grid, 256, 0, s>>>(psi_j, tab, slabs, npt, status);
+  k_slab_phase<S><<<grid, 256, 0, s>>>(psi_j, tab, slabs, npt, status);
 }
+template void launch_slab_phase<double2>(cudaStream_t, double2 *, const double2 *, const SlabDesc *, int, int64_t,
+                                         const int *);
+template void launch_slab_phase<float2>(cudaStream_t, float2 *, const double2 *, const SlabDesc *, int, int64_t,
+                                        const int *);
 
 // ------------------------------------------------------------------ tables
 __global__ void k_build_theta_table(const double *__restrict__ pot, const double *__restrict__ d1,
@@ -226,39 +232,45 @@ void launch_build_float_tables(cudaStream_t s, const Grid &g, const double *w, c
 
 // ------------------------------------------------------------ energies
 // rotational energy partials: sum l(l+1) (I1_i + I2_j) |psi|^2 per (slab, tile)
-__global__ void k_rot_energy(Grid g, const double2 *__restrict__ psi_j, const SlabDesc *__restrict__ slabs,
+template <typename S>
+__global__ void k_rot_energy(Grid g, const S *__restrict__ psi_j, const SlabDesc *__restrict__ slabs,
                              double *__restrict__ re_part, int tiles, const int *status) {
   if (status && *status) return;
   __shared__ double red[32];
   const int sl = blockIdx.y;
   const double ll = (double)slabs[sl].l * (slabs[sl].l + 1);
-  const double2 *p = psi_j + (int64_t)sl * g.npt;
+  const S *p = psi_j + (int64_t)sl * g.npt;
   double acc = 0.0;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < g.npt; q += (int64_t)tiles * blockDim.x) {
     const int i = (int)(q % g.n1), j = (int)(q / g.n1);
     const double R = g.left1 + i * g.dr1, r = g.left2 + j * g.dr2;
     const double I = 1.0 / (2 * g.m1 * R * R) + 1.0 / (2 * g.m2 * r * r);
-    const double2 v = p[q];
+    const double2 v = load_c(p + q);
     acc += ll * I * (v.x * v.x + v.y * v.y);
   }
   acc = block_sum(acc, red);
   if (threadIdx.x == 0) re_part[(int64_t)sl * tiles + blockIdx.x] = acc;
 }
 
-void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, const SlabDesc *slabs, int n_slabs,
-                       const double *, const double *, double *re_part, int tiles, const int *status) {
+template <typename S>
+void launch_rot_energy(cudaStream_t s, const Grid &g, const S *psi_j, const SlabDesc *slabs, int n_slabs,
+                       double *re_part, int tiles, const int *status) {
   if (n_slabs == 0) return;
-  k_rot_energy<<<dim3(tiles, n_slabs), 256, 0, s>>>(g, psi_j, slabs, re_part, tiles, status);
+  k_rot_energy<S><<<dim3(tiles, n_slabs), 256, 0, s>>>(g, psi_j, slabs, re_part, tiles, status);
 }
+template void launch_rot_energy<double2>(cudaStream_t, const Grid &, const double2 *, const SlabDesc *, int,
+                                         double *, int, const int *);
+template void launch_rot_energy<float2>(cudaStream_t, const Grid &, const float2 *, const SlabDesc *, int, double *,
+                                        int, const int *);
 
-// Energy finalisation.  One CTA per (quantity, block) sums that block's
-// partial array in a fixed order (deterministic) and writes energies[b][q];
-// the last CTA to finish then forms the totals, the step record and the norm
-// guard of print_energies (cudaOpenMP2.cu:425-445), and, at the end of a full
-// step, books the flux slot and advances the step counter.  Quantities:
-// 0 module + potential, 1 kinetic, 2 rotational, 3 Coriolis.  Coupling-energy
-// partials are laid out [group][ce_n][tiles]; a block collects them from every
-// group (one per l) of its problem that contains its Omega.
+// Energy finalisation.  One CTA per Omega block loads all of that block's
+// partials (module, potential, kinetic, rotational, Coriolis) in one pass,
+// sums them in a fixed order (deterministic) and writes energies[b] and the
+// step record; the last CTA to finish then applies the norm guard of
+// print_energies (cudaOpenMP2.cu:425-445) per problem and, at the end of a
+// full step, books the flux slot and advances the step counter.
+// Coupling-energy partials are laid out [group][ce_n][tiles]; a block collects
+// them from every group (one per l) of its problem that contains its Omega.
 __global__ void __launch_bounds__(256) k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__restrict__ blocks,
                                   const int *__restrict__ pblock0, int n_problems,
                                   const CoriolisGroup *__restrict__ groups, const int *__restrict__ pgroup0,

@@ -256,7 +256,8 @@ struct qd_session {
   SlabDesc *d_slabs = nullptr;
   int *d_pblock0 = nullptr;
   // coupled / uncoupled slab lists (epilogue tables differ)
-  double2 *psi_th = nullptr, *psi_j = nullptr;
+  double2 *psi_th = nullptr, *psi_j = nullptr;   // psi_j: FP64 form only (c128)
+  float2 *psi_jf = nullptr;                        // mixed form: psi_j pool in c64
   double *pot = nullptr, *w = nullptr, *T1 = nullptr, *T2 = nullptr, *I1 = nullptr, *I2 = nullptr;
   double *d1 = nullptr, *d2 = nullptr;
   double2 *tab_v = nullptr, *tab_v0 = nullptr, *tab_rot2 = nullptr, *tab_rot4 = nullptr, *tab_kin = nullptr;
@@ -382,7 +383,7 @@ __global__ void k_flux_reset(int *count) { *count = 0; }
 
 qd_session::~qd_session() {
   if (graph_chunk) cudaGraphExecDestroy(graph_chunk);
-  void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
+  void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, psi_jf, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
                   tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, d_pgroup0,
                   part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
                   flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
@@ -445,11 +446,11 @@ static void enqueue_tail(qd_session *s);
 static void enqueue_step_mixed(qd_session *s, bool first) {
   cudaStream_t st = s->stream;
   const Grid &g = s->g;
-  launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_j, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f,
+  launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_jf, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f,
                          first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status, s->bscale_f, s->max_nl);
   prof_mark(st, "legendre_forward");
   if (s->any_coupled) {
-    launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
+    launch_coriolis(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
                     s->cor_H, nullptr, s->t_ce, s->tab_rot4, s->status, s->tab_rot4);
     prof_mark(st, "coriolis");
   }
@@ -464,16 +465,16 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
   lf.T2f = s->T2f;
   lf.I1f = s->I1f;
   lf.I2f = s->I2f;
-  launch_fft_kinetic(st, g, s->fft, QD_PRECISION_MIXED, s->psi_j, s->d_slabs, s->n_slabs, nullptr, s->T1, s->T2,
-                     s->part_ke, nullptr, s->I1, s->I2, s->any_coupled ? nullptr : s->part_re, s->status, &lf);
+  launch_fft_kinetic(st, g, s->fft, s->psi_jf, s->d_slabs, s->n_slabs, s->part_ke,
+                     s->any_coupled ? nullptr : s->part_re, s->status, &lf);
   if (s->any_coupled) {
-    launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
+    launch_coriolis(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
                     s->cor_H, s->part_ce, s->t_ce, s->tab_rot4, s->status);
     prof_mark(st, "coriolis_energy");
-    launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->I1, s->I2, s->part_re, s->t_re, s->status);
+    launch_rot_energy(st, g, s->psi_jf, s->d_slabs, s->n_slabs, s->part_re, s->t_re, s->status);
     prof_mark(st, "rotational_energy");
   }
-  launch_legendre_tc_bwd(st, g, s->psi_j, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf, s->wvf,
+  launch_legendre_tc_bwd(st, g, s->psi_jf, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf, s->wvf,
                          s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b, s->max_nl);
   prof_mark(st, "legendre_backward");
   enqueue_tail(s);
@@ -500,15 +501,14 @@ static void enqueue_step(qd_session *s, bool first) {
     prof_mark(st, "coriolis");
   }
   // forward FFT, kinetic(dt), kinetic energy, backward FFT + scale, rotational(dt/4)
-  launch_fft_kinetic(st, g, s->fft, s->precision, s->psi_j, s->d_slabs, s->n_slabs, s->tab_kin, s->T1, s->T2,
-                     s->part_ke, s->any_coupled ? s->tab_rot4 : s->tab_rot2, s->I1, s->I2,
-                     s->any_coupled ? nullptr : s->part_re, s->status);
+  launch_fft_kinetic(st, g, s->fft, s->psi_j, s->d_slabs, s->n_slabs, s->tab_kin, s->T1, s->T2, s->part_ke,
+                     s->any_coupled ? s->tab_rot4 : s->tab_rot2, s->any_coupled ? nullptr : s->part_re, s->status);
   if (s->any_coupled) {
     // evolution_with_coriolis(dt/2, energy) + rotational(dt/4), then the rotational energy
     launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
                     s->cor_H, s->part_ce, s->t_ce, s->tab_rot4, s->status);
     prof_mark(st, "coriolis_energy");
-    launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->I1, s->I2, s->part_re, s->t_re, s->status);
+    launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->part_re, s->t_re, s->status);
     prof_mark(st, "rotational_energy");
   }
   // backward_legendre_transform + potential energy + module
@@ -620,7 +620,12 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   // wave packets
   const int64_t nth_pt = g.npt * g.nth;
   s->psi_th = dalloc<double2>((size_t)s->n_blocks * nth_pt);
-  s->psi_j = dalloc<double2>((size_t)s->n_slabs * g.npt);
+  // the mixed form keeps the Legendre-space pool in c64: every value written
+  // there (tensor-core epilogue, FP32 FFT) is an FP32 number
+  if (s->precision == QD_PRECISION_MIXED)
+    s->psi_jf = dalloc<float2>((size_t)s->n_slabs * g.npt);
+  else
+    s->psi_j = dalloc<double2>((size_t)s->n_slabs * g.npt);
   for (int p = 0; p < n_problems; p++)
     QD_CUDA(cudaMemcpyAsync(s->psi_th + (int64_t)s->h_pblock0[p] * nth_pt, problems[p]->OmegaStates.wave_packets,
                             (size_t)s->probs[p].n_omegas * nth_pt * sizeof(double2), cudaMemcpyHostToDevice, st));
@@ -1154,7 +1159,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         break;
       case QD_STAGE_FORWARD_LEGENDRE:
         if (s->precision == QD_PRECISION_MIXED)
-          launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_j, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f, nullptr,
+          launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_jf, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f, nullptr,
                                  nullptr, nullptr, s->smem_f, s->status, s->status, s->bscale_f, s->max_nl);
         else
           launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, nullptr,
@@ -1162,7 +1167,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         break;
       case QD_STAGE_BACKWARD_LEGENDRE:
         if (s->precision == QD_PRECISION_MIXED)
-          launch_legendre_tc_bwd(st, g, s->psi_j, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf,
+          launch_legendre_tc_bwd(st, g, s->psi_jf, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf,
                                  s->wvf, s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b, s->max_nl);
         else
           launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
@@ -1171,7 +1176,10 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       case QD_STAGE_ROTATIONAL:
         tab = scratch_tab(g.npt * (g.l_max + 1));
         launch_build_rot_table(st, g, dt, tab);
-        launch_slab_phase(st, s->psi_j, tab, s->d_slabs, s->n_slabs, g.npt, s->status);
+        if (s->psi_jf)
+          launch_slab_phase(st, s->psi_jf, tab, s->d_slabs, s->n_slabs, g.npt, s->status);
+        else
+          launch_slab_phase(st, s->psi_j, tab, s->d_slabs, s->n_slabs, g.npt, s->status);
         break;
       case QD_STAGE_CORIOLIS:
       case QD_STAGE_CORIOLIS_ENERGY: {
@@ -1179,8 +1187,12 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         double2 *ph = dalloc<double2>((size_t)s->h_groups.back().ph0 + (size_t)s->h_groups.back().n * g.n1);
         launch_build_coriolis_phase(st, g, s->d_groups, s->n_groups, s->max_group_n, s->cor_e, dt, ph);
         const bool en = stage == QD_STAGE_CORIOLIS_ENERGY;
-        launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, ph,
-                        s->cor_H, en ? s->part_ce : nullptr, s->t_ce, nullptr, s->status);
+        if (s->psi_jf)
+          launch_coriolis(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, ph,
+                          s->cor_H, en ? s->part_ce : nullptr, s->t_ce, nullptr, s->status);
+        else
+          launch_coriolis(st, g, s->psi_j, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, ph,
+                          s->cor_H, en ? s->part_ce : nullptr, s->t_ce, nullptr, s->status);
         if (en) {
           EnergyParts ep = energy_parts(s, false, false, false, true);
           launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
@@ -1208,8 +1220,11 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
           lf.I1f = s->I1f;
           lf.I2f = s->I2f;
         }
-        launch_fft_kinetic(st, g, s->fft, s->precision, s->psi_j, s->d_slabs, s->n_slabs, tab, s->T1, s->T2,
-                           s->part_ke, nullptr, s->I1, s->I2, nullptr, s->status, &lf);
+        if (s->psi_jf)
+          launch_fft_kinetic(st, g, s->fft, s->psi_jf, s->d_slabs, s->n_slabs, s->part_ke, nullptr, s->status, &lf);
+        else
+          launch_fft_kinetic(st, g, s->fft, s->psi_j, s->d_slabs, s->n_slabs, tab, s->T1, s->T2, s->part_ke, nullptr,
+                             nullptr, s->status);
         QD_CUDA(cudaStreamSynchronize(st));
         if (kR) cudaFree(kR);
         if (kr) cudaFree(kr);
@@ -1221,7 +1236,10 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       }
       case QD_STAGE_ENERGIES: {
         const int t_re_saved = s->t_re;
-        launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->I1, s->I2, s->part_re, s->t_re, s->status);
+        if (s->psi_jf)
+          launch_rot_energy(st, g, s->psi_jf, s->d_slabs, s->n_slabs, s->part_re, s->t_re, s->status);
+        else
+          launch_rot_energy(st, g, s->psi_j, s->d_slabs, s->n_slabs, s->part_re, s->t_re, s->status);
         // module and potential energy come from a backward contraction into psi_theta
         EnergyParts ep = energy_parts(s, true, false, true, false);
         ep.re_tiles = t_re_saved;
@@ -1256,18 +1274,23 @@ int qd_session_get_psi(qd_session *s, int32_t which, int32_t block, double *host
   QD_GUARD({
     QD_REQUIRE(s && host_out && block >= 0 && block < s->n_blocks, "session, block");
     const BlockDesc &bd = s->h_blocks[block];
-    const double2 *src;
-    size_t n;
-    if (which == 0) {
-      n = (size_t)s->g.npt * s->g.nth;
-      src = s->psi_th + (int64_t)block * n;
-    } else {
-      n = (size_t)s->g.npt * bd.nl;
-      src = s->psi_j + (int64_t)bd.slab0 * s->g.npt;
-    }
+    const size_t n = which == 0 ? (size_t)s->g.npt * s->g.nth : (size_t)s->g.npt * bd.nl;
     QD_REQUIRE(n_doubles == 2 * n, "buffer size");
     QD_CUDA(cudaStreamSynchronize(s->stream));
-    QD_CUDA(cudaMemcpy(host_out, src, n * sizeof(double2), cudaMemcpyDeviceToHost));
+    if (which == 0) {
+      QD_CUDA(cudaMemcpy(host_out, s->psi_th + (int64_t)block * n, n * sizeof(double2), cudaMemcpyDeviceToHost));
+    } else if (s->psi_jf) {   // mixed form: c64 pool, widened exactly
+      std::vector<float2> tmp(n);
+      QD_CUDA(cudaMemcpy(tmp.data(), s->psi_jf + (int64_t)bd.slab0 * s->g.npt, n * sizeof(float2),
+                         cudaMemcpyDeviceToHost));
+      for (size_t q = 0; q < n; q++) {
+        host_out[2 * q] = tmp[q].x;
+        host_out[2 * q + 1] = tmp[q].y;
+      }
+    } else {
+      QD_CUDA(cudaMemcpy(host_out, s->psi_j + (int64_t)bd.slab0 * s->g.npt, n * sizeof(double2),
+                         cudaMemcpyDeviceToHost));
+    }
   })
 }
 
@@ -1275,18 +1298,20 @@ int qd_session_set_psi(qd_session *s, int32_t which, int32_t block, const double
   QD_GUARD({
     QD_REQUIRE(s && host_in && block >= 0 && block < s->n_blocks, "session, block");
     const BlockDesc &bd = s->h_blocks[block];
-    double2 *dst;
-    size_t n;
-    if (which == 0) {
-      n = (size_t)s->g.npt * s->g.nth;
-      dst = s->psi_th + (int64_t)block * n;
-    } else {
-      n = (size_t)s->g.npt * bd.nl;
-      dst = s->psi_j + (int64_t)bd.slab0 * s->g.npt;
-    }
+    const size_t n = which == 0 ? (size_t)s->g.npt * s->g.nth : (size_t)s->g.npt * bd.nl;
     QD_REQUIRE(n_doubles == 2 * n, "buffer size");
     QD_CUDA(cudaStreamSynchronize(s->stream));
-    QD_CUDA(cudaMemcpy(dst, host_in, n * sizeof(double2), cudaMemcpyHostToDevice));
+    if (which == 0) {
+      QD_CUDA(cudaMemcpy(s->psi_th + (int64_t)block * n, host_in, n * sizeof(double2), cudaMemcpyHostToDevice));
+    } else if (s->psi_jf) {   // mixed form: c64 pool, rounded to nearest
+      std::vector<float2> tmp(n);
+      for (size_t q = 0; q < n; q++) tmp[q] = make_float2((float)host_in[2 * q], (float)host_in[2 * q + 1]);
+      QD_CUDA(cudaMemcpy(s->psi_jf + (int64_t)bd.slab0 * s->g.npt, tmp.data(), n * sizeof(float2),
+                         cudaMemcpyHostToDevice));
+    } else {
+      QD_CUDA(cudaMemcpy(s->psi_j + (int64_t)bd.slab0 * s->g.npt, host_in, n * sizeof(double2),
+                         cudaMemcpyHostToDevice));
+    }
   })
 }
 

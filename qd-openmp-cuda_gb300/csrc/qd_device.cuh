@@ -71,6 +71,16 @@ __device__ inline double f2d(float f) {
   return __hiloint2double((int)(sign | ((e + 896u) << 20) | (m >> 3)), (int)(m << 29));
 }
 
+// psi_j element access for either storage: c128 (FP64 form) or c64 (mixed
+// form, one round-to-nearest on store)
+__device__ inline double2 load_c(const double2 *p) { return *p; }
+__device__ inline double2 load_c(const float2 *p) {
+  const float2 v = *p;
+  return make_double2(f2d(v.x), f2d(v.y));
+}
+__device__ inline void store_c(double2 *p, double2 v) { *p = v; }
+__device__ inline void store_c(float2 *p, double2 v) { *p = make_float2(d2f_rn(v.x), d2f_rn(v.y)); }
+
 // Deterministic block-wide sum (fixed shuffle tree then fixed smem tree);
 // every thread gets the result.  red must hold 32 doubles; all threads call.
 __device__ inline double block_sum(double v, double *red) {

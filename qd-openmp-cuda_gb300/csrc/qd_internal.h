@@ -89,9 +89,10 @@ struct Grid {
 void launch_theta_phase(cudaStream_t s, double2 *psi, const double2 *tab, int n_blocks,
                         int64_t n_per_block, const int *status);
 
-// j-space phase: slab s (l = slabs[s].l) *= tab[l][j][i]
-void launch_slab_phase(cudaStream_t s, double2 *psi_j, const double2 *tab, const SlabDesc *slabs,
-                       int n_slabs, int64_t npt, const int *status);
+// j-space phase: slab s (l = slabs[s].l) *= tab[l][j][i]; psi_j c128 or c64
+template <typename S>
+void launch_slab_phase(cudaStream_t s, S *psi_j, const double2 *tab, const SlabDesc *slabs, int n_slabs,
+                       int64_t npt, const int *status);
 
 // FP64 Legendre contractions (SIMT DFMA).
 // forward: psi_j(slab0_b+n) = sum_k wP_b[k][n] (tabA[k] * psi_th[b][k]);  tabA may be null;
@@ -133,25 +134,30 @@ struct FFTLift {
 bool fft_factor(int n, int *rad, int *nst);
 void fft_plan_init(FFTPlan &p, int n1, int n2);
 void fft_plan_free(FFTPlan &p);
-// forward rows -> cols (fwd, kinetic, KE partials, inv) -> rows inverse with
-// scale 1/(n1 n2) and the epilogue phase tabE (may be null) and rotational
-// energy partials (when re_part is non-null).
-void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, int precision, double2 *psi_j,
-                        const SlabDesc *slabs, int n_slabs, const double2 *tab_kin, const double *T1,
-                        const double *T2, double *ke_part, const double2 *tabE, const double *I1,
-                        const double *I2, double *re_part, const int *status, const FFTLift *lift = nullptr);
+// FP64 form: forward rows -> cols (fwd, kinetic, KE partials, inv) -> rows
+// inverse with scale 1/(n1 n2) and the epilogue phase tabE (may be null) and
+// rotational energy partials (when re_part is non-null).
+void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, double2 *psi_j, const SlabDesc *slabs,
+                        int n_slabs, const double2 *tab_kin, const double *T1, const double *T2, double *ke_part,
+                        const double2 *tabE, double *re_part, const int *status);
+// Mixed form: FP32 transforms on the c64 psi_j pool with the three-shear phases
+// of lift (kinetic, and the rotational phase before/after when set).
+void launch_fft_kinetic(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, const SlabDesc *slabs,
+                        int n_slabs, double *ke_part, double *re_part, const int *status, const FFTLift *lift);
 int fft_col_tiles(const FFTPlan &p, int precision);
 int fft_row_tiles(const FFTPlan &p, int precision);
 
 // rotational energy partials only (for stage-by-stage use)
-void launch_rot_energy(cudaStream_t s, const Grid &g, const double2 *psi_j, const SlabDesc *slabs,
-                       int n_slabs, const double *I1, const double *I2, double *re_part, int tiles,
-                       const int *status);
+template <typename S>
+void launch_rot_energy(cudaStream_t s, const Grid &g, const S *psi_j, const SlabDesc *slabs, int n_slabs,
+                       double *re_part, int tiles, const int *status);
 
 // Coriolis: in-place psi_l^Omega <- sum_Omega1 U_l[Omega][Omega1](R) psi_l^Omega1 per group,
 // optional coupling-energy partials per block (computed on the input psi),
 // optional epilogue phase tabE[l] (may be null).
-void launch_coriolis(cudaStream_t s, const Grid &g, double2 *psi_j, const BlockDesc *blocks,
+// psi_j is double2 (FP64 form) or float2 (mixed form; arithmetic stays FP64).
+template <typename S>
+void launch_coriolis(cudaStream_t s, const Grid &g, S *psi_j, const BlockDesc *blocks,
                      const CoriolisGroup *groups, int n_groups, int max_n, const double *V,
                      const double2 *ph, const double *H, double *ce_part, int ce_tiles,
                      const double2 *tabE, const int *status, const double2 *tabP = nullptr);
@@ -228,11 +234,11 @@ bool tc_shape_ok(int Kp, int Np);
 void tc_set_smem_limit(size_t bytes);
 void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,
                             bool fwd, const int64_t *img_off, uint16_t *img, float *bscale, int max_np);
-void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, double2 *psi_j,
+void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, float2 *psi_j,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
                             int *status_w, const float *bscale, int max_nl);
-void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const double2 *psi_j, double2 *psi_th,
+void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, double2 *psi_th,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
                             const int *status, int *status_w, const float *bscale, int max_nl);
