@@ -70,7 +70,7 @@ namespace {
 constexpr int FLUX_GX = 64, FLUX_GY = 4, FLUX_GMAX = 8;   // n_grad <= FLUX_GY * FLUX_GMAX
 }
 __global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, int n_grad, int n_ds,
-                                                                       const double2 *__restrict__ psi_th,
+                                                                       const float2 *__restrict__ psi_th,
                                                                        const float2 *__restrict__ hv,
                                                                        const float *__restrict__ fd,
                                                                        double2 *__restrict__ buf, int n_blocks,
@@ -83,13 +83,13 @@ __global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, i
   const int h = (n_grad - 1) / 2;
   const int64_t ns = (int64_t)g.nth * g.n1;
   double2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
-  const double2 *p = psi_th + (int64_t)b * g.nth * g.npt;
+  const float2 *p = psi_th + (int64_t)b * g.nth * g.npt;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t q = (int64_t)blockIdx.x * FLUX_GX + tx;
   float Dx = 0.0f, Dy = 0.0f;
   if (q < ns) {
     const int i = (int)(q % g.n1), k = (int)(q / g.n1);
-    double2 a[FLUX_GMAX];
+    float2 a[FLUX_GMAX];
     float2 ts[FLUX_GMAX];
 #pragma unroll
     for (int u = 0; u < FLUX_GMAX; u++) {
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, i
     for (int u = 0; u < FLUX_GMAX; u++) {
       const int gg = ty + FLUX_GY * u;
       if (gg < n_grad) {
-        float x = d2f_rn(a[u].x), y = d2f_rn(a[u].y);
+        float x = a[u].x, y = a[u].y;
         lift2f(x, y, ts[u]);
         const float c = __ldg(fd + gg);
         Dx = fmaf(c, x, Dx);
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, i
   }
 }
 
-void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const double2 *psi_th, int n_blocks,
+void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const float2 *psi_th, int n_blocks,
                              const float2 *half_v, const float *fd, double2 *buf, const int *slot, const int *status) {
   if (f.n_grad > FLUX_GY * FLUX_GMAX)
     throw Error{QD_ERR_UNSUPPORTED, "mixed-form flux: more than 32 stencil points"};

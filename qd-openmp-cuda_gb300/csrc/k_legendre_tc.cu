@@ -30,7 +30,6 @@
 // epilogue also reduces the module and potential energy.
 #include <cuda_bf16.h>
 
-#include <type_traits>
 
 #include "qd_internal.h"
 #include "qd_device.cuh"
@@ -200,8 +199,8 @@ __global__ void k_build_tc_bimage(const BlockDesc *__restrict__ blocks, const do
 
 struct TcArgs {
   Grid g;
-  const void *A;             // fwd: psi_theta pool (double2), bwd: psi_j pool (float2)
-  void *C;                   // fwd: psi_j pool (float2), bwd: psi_theta pool (double2)
+  const float2 *A;           // fwd: psi_theta pool, bwd: psi_j pool (both c64)
+  float2 *C;                 // fwd: psi_j pool, bwd: psi_theta pool
   const BlockDesc *blocks;
   const uint16_t *bimg;      // B images
   const int64_t *bimg_off;   // per block byte offset
@@ -318,23 +317,21 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       const BlockDesc bd = P.blocks[T.b];
       const int64_t p0 = (int64_t)T.mt * TC_POINTS;
       const int LDF = T.Kp + 1;
-      using AT = typename std::conditional<FWD, double2, float2>::type;   // psi_theta c128, psi_j c64
-      const AT *A = reinterpret_cast<const AT *>(P.A) + (FWD ? (int64_t)T.b * g.nth * g.npt : (int64_t)bd.slab0 * g.npt);
+      const float2 *A = P.A + (FWD ? (int64_t)T.b * g.nth * g.npt : (int64_t)bd.slab0 * g.npt);
       // L2 prefetch of the next tile (128-byte lines of its k rows)
       if (tt + 1 < t_end) {
         const TcTile Tn = tc_tile<FWD>(P, tt + 1, mtiles);
         const BlockDesc bn = P.blocks[Tn.b];
-        const AT *An = reinterpret_cast<const AT *>(P.A) +
-                       (FWD ? (int64_t)Tn.b * g.nth * g.npt : (int64_t)bn.slab0 * g.npt);
+        const float2 *An = P.A + (FWD ? (int64_t)Tn.b * g.nth * g.npt : (int64_t)bn.slab0 * g.npt);
         const int64_t pn = (int64_t)Tn.mt * TC_POINTS;
-        constexpr int LPR = FWD ? 8 : 4;                // 128-byte lines per k row: 64 points x 16 or 8 B
+        constexpr int LPR = 4;                          // 128-byte lines per k row: 64 points x 8 B
         constexpr int PPL = TC_POINTS / LPR;            // points per line
         const int lines = Tn.Kv * LPR;
         for (int q = tid; q < lines; q += WS_PROD) {
           const int k = q / LPR, ln = q % LPR;
           const int64_t pp = pn + ln * PPL;
           if (pp < g.npt) asm volatile("prefetch.global.L2 [%0];" ::"l"(An + (int64_t)k * g.npt + pp));
-          if (FWD && P.vph && (ln & 1) == 0 && pp < g.npt)
+          if (FWD && P.vph && pp < g.npt)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(P.vph + (int64_t)k * g.npt + pp));
         }
       }
@@ -344,33 +341,23 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         const int64_t p = p0 + pl;
         float msk = 1.0f;
         if (FWD && P.d1 && p < g.npt) msk = P.d1[(int)(p % g.n1)] * P.d2[(int)(p / g.n1)];
-        constexpr int U = FWD ? 12 : 24;
+        constexpr int U = FWD ? 16 : 24;
         const int nk = T.Kp / 4;   // this thread's k values: tid/64 + 4u
         for (int u0 = 0; u0 < nk; u0 += U) {
-          AT v[U];
+          float2 v[U];
           float2 ts[U];
 #pragma unroll
           for (int u = 0; u < U; u++) {
             const int k = tid / TC_POINTS + 4 * (u0 + u);
             const bool in = u0 + u < nk && k < T.Kv && p < g.npt;
-            if (in)
-              v[u] = A[(int64_t)k * g.npt + p];
-            else
-              v[u].x = v[u].y = 0;
+            v[u] = in ? A[(int64_t)k * g.npt + p] : make_float2(0.0f, 0.0f);
             if (FWD) ts[u] = (in && P.vph) ? __ldg(P.vph + (int64_t)k * g.npt + p) : make_float2(0.0f, 0.0f);
           }
 #pragma unroll
           for (int u = 0; u < U; u++) {
             if (u0 + u >= nk) break;
             const int k = tid / TC_POINTS + 4 * (u0 + u);
-            float x, y;
-            if constexpr (FWD) {
-              x = d2f_rn(v[u].x);
-              y = d2f_rn(v[u].y);
-            } else {
-              x = v[u].x;
-              y = v[u].y;
-            }
+            float x = v[u].x, y = v[u].y;
             if (FWD) {
               x *= msk;
               y *= msk;
@@ -504,8 +491,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       tc_fence_after();
       const float srow = srow_s[it & 1][m];
       float mod = 0.0f, pe = 0.0f;
-      double *Cd = reinterpret_cast<double *>(P.C);   // backward: psi_theta, c128
-      float *Cf = reinterpret_cast<float *>(P.C);     // forward: psi_j, c64
+      float *Cf = reinterpret_cast<float *>(P.C);
       const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
       for (int n0 = 16 * chalf; n0 < T.Np; n0 += 32) {
         // the next chunk's w V values are requested before this chunk is used
@@ -530,7 +516,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
               if (FWD) {
                 Cf[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = v;
               } else {
-                Cd[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = f2d(v);
+                Cf[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = v;
                 const float v2 = v * v;
                 mod = fmaf(w_s[n], v2, mod);
                 pe = fmaf(wv[q], v2, pe);
@@ -619,7 +605,7 @@ void launch_legendre_tc_ws(cudaStream_t s, bool fwd, const TcArgs &a, int n_bloc
 }
 
 
-void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, float2 *psi_j,
+void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const float2 *psi_th, float2 *psi_j,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
                             int *status_w, const float *bscale, int max_nl) {
@@ -640,7 +626,7 @@ void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th
   launch_legendre_tc_ws(s, true, a, n_blocks, round16(g.nth), round16(max_nl));
 }
 
-void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, double2 *psi_th,
+void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, float2 *psi_th,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
                             const int *status, int *status_w, const float *bscale, int max_nl) {

@@ -11,20 +11,45 @@
 
 namespace qd {
 
-__global__ void k_theta_phase(double2 *__restrict__ psi, const double2 *__restrict__ tab, int64_t n_total,
+template <typename S>
+__global__ void k_theta_phase(S *__restrict__ psi, const double2 *__restrict__ tab, int64_t n_total,
                               int64_t n_per_block, const int *status) {
   if (status && *status) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_total; i += stride) {
     const int64_t t = i % n_per_block;
-    psi[i] = cmul(psi[i], ldg2(tab + t));
+    store_c(psi + i, cmul(load_c(psi + i), ldg2(tab + t)));
   }
 }
 
-void launch_theta_phase(cudaStream_t s, double2 *psi, const double2 *tab, int n_blocks, int64_t n_per_block,
+template <typename S>
+void launch_theta_phase(cudaStream_t s, S *psi, const double2 *tab, int n_blocks, int64_t n_per_block,
                         const int *status) {
   const int64_t n = (int64_t)n_blocks * n_per_block;
-  k_theta_phase<<<grid_for(n, 256), 256, 0, s>>>(psi, tab, n, n_per_block, status);
+  k_theta_phase<S><<<grid_for(n, 256), 256, 0, s>>>(psi, tab, n, n_per_block, status);
+}
+template void launch_theta_phase<double2>(cudaStream_t, double2 *, const double2 *, int, int64_t, const int *);
+template void launch_theta_phase<float2>(cudaStream_t, float2 *, const double2 *, int, int64_t, const int *);
+
+// c64 <-> c128 copies for the mixed form's host transfers (widening is exact,
+// narrowing rounds to nearest)
+__global__ void k_widen(const float2 *__restrict__ src, double2 *__restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = src[i];
+    dst[i] = make_double2(f2d(v.x), f2d(v.y));
+  }
+}
+__global__ void k_narrow(const double2 *__restrict__ src, float2 *__restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = src[i];
+    dst[i] = make_float2(d2f_rn(v.x), d2f_rn(v.y));
+  }
+}
+void launch_widen(cudaStream_t s, const float2 *src, double2 *dst, int64_t n) {
+  if (n > 0) k_widen<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n);
+}
+void launch_narrow(cudaStream_t s, const double2 *src, float2 *dst, int64_t n) {
+  if (n > 0) k_narrow<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n);
 }
 
 template <typename S>

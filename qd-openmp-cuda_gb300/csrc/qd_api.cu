@@ -7,6 +7,7 @@
 // of every problem resident in HBM; each stage is one launch over all blocks,
 // and steps are replayed from CUDA graphs.
 #include "qd_internal.h"
+#include "qd_device.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -256,8 +257,12 @@ struct qd_session {
   SlabDesc *d_slabs = nullptr;
   int *d_pblock0 = nullptr;
   // coupled / uncoupled slab lists (epilogue tables differ)
-  double2 *psi_th = nullptr, *psi_j = nullptr;   // psi_j: FP64 form only (c128)
-  float2 *psi_jf = nullptr;                        // mixed form: psi_j pool in c64
+  double2 *psi_th = nullptr, *psi_j = nullptr;   // FP64 form: both pools in c128
+  // mixed form: both pools in c64 (every value the mixed step writes is an
+  // FP32 number); host transfers widen/narrow through xfer (c128)
+  float2 *psi_thf = nullptr, *psi_jf = nullptr;
+  double2 *xfer = nullptr;
+  int64_t xfer_elems = 0;
   double *pot = nullptr, *w = nullptr, *T1 = nullptr, *T2 = nullptr, *I1 = nullptr, *I2 = nullptr;
   double *d1 = nullptr, *d2 = nullptr;
   double2 *tab_v = nullptr, *tab_v0 = nullptr, *tab_rot2 = nullptr, *tab_rot4 = nullptr, *tab_kin = nullptr;
@@ -327,7 +332,8 @@ __global__ void k_flux_begin(const int *step, int *flux_count, double *flux_t0, 
 }
 
 // flux extract with a device-side slot
-__global__ void k_flux_extract_dev(Grid g, int n_grad, int n_ds, const double2 *__restrict__ psi_th,
+template <typename S>
+__global__ void k_flux_extract_dev(Grid g, int n_grad, int n_ds, const S *__restrict__ psi_th,
                                    const double2 *__restrict__ hv, const double *__restrict__ fd,
                                    double2 *__restrict__ buf, int n_blocks, const int *slot_p, const int *status) {
   if (status && *status) return;
@@ -336,7 +342,7 @@ __global__ void k_flux_extract_dev(Grid g, int n_grad, int n_ds, const double2 *
   const int h = (n_grad - 1) / 2;
   const int64_t ns = (int64_t)g.nth * g.n1;
   double2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
-  const double2 *p = psi_th + (int64_t)b * g.nth * g.npt;
+  const S *p = psi_th + (int64_t)b * g.nth * g.npt;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(q % g.n1), k = (int)(q / g.n1);
     double2 A = make_double2(0.0, 0.0), D = make_double2(0.0, 0.0);
@@ -346,7 +352,7 @@ __global__ void k_flux_extract_dev(Grid g, int n_grad, int n_ds, const double2 *
 #pragma unroll
       for (int u = 0; u < GB; u++)
         if (g0 + u < n_grad) {
-          av[u] = p[((int64_t)k * g.n2 + (n_ds - h + g0 + u)) * g.n1 + i];
+          av[u] = load_c(p + ((int64_t)k * g.n2 + (n_ds - h + g0 + u)) * g.n1 + i);
           mv[u] = hv[((int64_t)k * n_grad + g0 + u) * g.n1 + i];
         }
 #pragma unroll
@@ -383,7 +389,7 @@ __global__ void k_flux_reset(int *count) { *count = 0; }
 
 qd_session::~qd_session() {
   if (graph_chunk) cudaGraphExecDestroy(graph_chunk);
-  void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, psi_jf, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
+  void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, psi_thf, psi_jf, xfer, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
                   tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, d_pgroup0,
                   part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
                   flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
@@ -446,7 +452,7 @@ static void enqueue_tail(qd_session *s);
 static void enqueue_step_mixed(qd_session *s, bool first) {
   cudaStream_t st = s->stream;
   const Grid &g = s->g;
-  launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_jf, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f,
+  launch_legendre_tc_fwd(st, g, s->psi_thf, s->psi_jf, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f,
                          first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status, s->bscale_f, s->max_nl);
   prof_mark(st, "legendre_forward");
   if (s->any_coupled) {
@@ -474,7 +480,7 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
     launch_rot_energy(st, g, s->psi_jf, s->d_slabs, s->n_slabs, s->part_re, s->t_re, s->status);
     prof_mark(st, "rotational_energy");
   }
-  launch_legendre_tc_bwd(st, g, s->psi_jf, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf, s->wvf,
+  launch_legendre_tc_bwd(st, g, s->psi_jf, s->psi_thf, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf, s->wvf,
                          s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b, s->max_nl);
   prof_mark(st, "legendre_backward");
   enqueue_tail(s);
@@ -538,7 +544,7 @@ static void enqueue_tail(qd_session *s) {
   prof_mark(st, "energy_finalize");
   if (s->flux.enabled) {
     if (s->precision == QD_PRECISION_MIXED) {
-      launch_flux_extract_f32(st, g, s->flux, s->psi_th, s->n_blocks, s->half_v_lift, s->fdf, s->flux_buf,
+      launch_flux_extract_f32(st, g, s->flux, s->psi_thf, s->n_blocks, s->half_v_lift, s->fdf, s->flux_buf,
                               s->flux_slot, s->status);
     } else {
       const int64_t ns = (int64_t)g.nth * g.n1;
@@ -559,6 +565,34 @@ static int count_launches_per_step(qd_session *s) {
 }
 
 }  // namespace qd
+
+// theta-space pool <-> host memory in c128.  The FP64 form copies directly;
+// the mixed form narrows (round to nearest) or widens (exact) through the
+// c128 staging buffer, chunk by chunk in stream order.
+static void theta_from_host(qd_session *s, int64_t off, int64_t n, const double *host) {
+  cudaStream_t st = s->stream;
+  if (!s->psi_thf) {
+    QD_CUDA(cudaMemcpyAsync(s->psi_th + off, host, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    return;
+  }
+  for (int64_t q = 0; q < n; q += s->xfer_elems) {
+    const int64_t m = std::min(s->xfer_elems, n - q);
+    QD_CUDA(cudaMemcpyAsync(s->xfer, host + 2 * q, m * sizeof(double2), cudaMemcpyHostToDevice, st));
+    launch_narrow(st, s->xfer, s->psi_thf + off + q, m);
+  }
+}
+static void theta_to_host(qd_session *s, int64_t off, int64_t n, double *host) {
+  cudaStream_t st = s->stream;
+  if (!s->psi_thf) {
+    QD_CUDA(cudaMemcpyAsync(host, s->psi_th + off, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    return;
+  }
+  for (int64_t q = 0; q < n; q += s->xfer_elems) {
+    const int64_t m = std::min(s->xfer_elems, n - q);
+    launch_widen(st, s->psi_thf + off + q, s->xfer, m);
+    QD_CUDA(cudaMemcpyAsync(host + 2 * q, s->xfer, m * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  }
+}
 
 // ------------------------------------------------------------ create
 static void session_build(qd_session *s, qd_fh2data *const *problems, int n_problems) {
@@ -619,16 +653,20 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
 
   // wave packets
   const int64_t nth_pt = g.npt * g.nth;
-  s->psi_th = dalloc<double2>((size_t)s->n_blocks * nth_pt);
-  // the mixed form keeps the Legendre-space pool in c64: every value written
-  // there (tensor-core epilogue, FP32 FFT) is an FP32 number
-  if (s->precision == QD_PRECISION_MIXED)
+  // the mixed form keeps both pools in c64: every value its step writes there
+  // (tensor-core epilogues, FP32 FFT) is an FP32 number
+  if (s->precision == QD_PRECISION_MIXED) {
+    s->psi_thf = dalloc<float2>((size_t)s->n_blocks * nth_pt);
     s->psi_jf = dalloc<float2>((size_t)s->n_slabs * g.npt);
-  else
+    s->xfer_elems = std::min<int64_t>((int64_t)s->n_blocks * nth_pt, (int64_t)1 << 25);
+    s->xfer = dalloc<double2>((size_t)s->xfer_elems);
+  } else {
+    s->psi_th = dalloc<double2>((size_t)s->n_blocks * nth_pt);
     s->psi_j = dalloc<double2>((size_t)s->n_slabs * g.npt);
+  }
   for (int p = 0; p < n_problems; p++)
-    QD_CUDA(cudaMemcpyAsync(s->psi_th + (int64_t)s->h_pblock0[p] * nth_pt, problems[p]->OmegaStates.wave_packets,
-                            (size_t)s->probs[p].n_omegas * nth_pt * sizeof(double2), cudaMemcpyHostToDevice, st));
+    theta_from_host(s, (int64_t)s->h_pblock0[p] * nth_pt, (int64_t)s->probs[p].n_omegas * nth_pt,
+                    problems[p]->OmegaStates.wave_packets);
 
   // grid tables
   std::vector<double> T1(g.n1), T2(g.n2);
@@ -940,9 +978,8 @@ static void run_steps(qd_session *s, int n) {
 static void download_psi(qd_session *s, qd_fh2data *const *problems, int n) {
   const int64_t nth_pt = s->g.npt * s->g.nth;
   for (int p = 0; p < n; p++)
-    QD_CUDA(cudaMemcpyAsync(problems[p]->OmegaStates.wave_packets, s->psi_th + (int64_t)s->h_pblock0[p] * nth_pt,
-                            (size_t)s->probs[p].n_omegas * nth_pt * sizeof(double2), cudaMemcpyDeviceToHost,
-                            s->stream));
+    theta_to_host(s, (int64_t)s->h_pblock0[p] * nth_pt, (int64_t)s->probs[p].n_omegas * nth_pt,
+                  problems[p]->OmegaStates.wave_packets);
   QD_CUDA(cudaStreamSynchronize(s->stream));
 }
 
@@ -1114,9 +1151,8 @@ int qd_session_upload(qd_session *s, qd_fh2data *const *problems, int32_t n_prob
     QD_REQUIRE(s && problems && n_problems == s->n_problems, "session upload: same problem count");
     const int64_t nth_pt = s->g.npt * s->g.nth;
     for (int p = 0; p < n_problems; p++)
-      QD_CUDA(cudaMemcpyAsync(s->psi_th + (int64_t)s->h_pblock0[p] * nth_pt, problems[p]->OmegaStates.wave_packets,
-                              (size_t)s->probs[p].n_omegas * nth_pt * sizeof(double2), cudaMemcpyHostToDevice,
-                              s->stream));
+      theta_from_host(s, (int64_t)s->h_pblock0[p] * nth_pt, (int64_t)s->probs[p].n_omegas * nth_pt,
+                      problems[p]->OmegaStates.wave_packets);
   })
 }
 
@@ -1147,7 +1183,10 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         std::vector<double> zero((size_t)g.npt * g.nth, 0.0);
         double *z = dupload(zero.data(), zero.size(), st);
         launch_build_theta_table(st, g, z, s->d1, s->d2, 0.0, tab);
-        launch_theta_phase(st, s->psi_th, tab, s->n_blocks, g.npt * g.nth, s->status);
+        if (s->psi_thf)
+          launch_theta_phase(st, s->psi_thf, tab, s->n_blocks, g.npt * g.nth, s->status);
+        else
+          launch_theta_phase(st, s->psi_th, tab, s->n_blocks, g.npt * g.nth, s->status);
         QD_CUDA(cudaStreamSynchronize(st));
         cudaFree(z);
         break;
@@ -1155,11 +1194,14 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
       case QD_STAGE_POTENTIAL:
         tab = scratch_tab(g.npt * g.nth);
         launch_build_theta_table(st, g, s->pot, nullptr, nullptr, dt, tab);
-        launch_theta_phase(st, s->psi_th, tab, s->n_blocks, g.npt * g.nth, s->status);
+        if (s->psi_thf)
+          launch_theta_phase(st, s->psi_thf, tab, s->n_blocks, g.npt * g.nth, s->status);
+        else
+          launch_theta_phase(st, s->psi_th, tab, s->n_blocks, g.npt * g.nth, s->status);
         break;
       case QD_STAGE_FORWARD_LEGENDRE:
         if (s->precision == QD_PRECISION_MIXED)
-          launch_legendre_tc_fwd(st, g, s->psi_th, s->psi_jf, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f, nullptr,
+          launch_legendre_tc_fwd(st, g, s->psi_thf, s->psi_jf, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f, nullptr,
                                  nullptr, nullptr, s->smem_f, s->status, s->status, s->bscale_f, s->max_nl);
         else
           launch_legendre_fwd_f64(st, g, s->psi_th, s->psi_j, s->Bf, s->d_blocks, s->n_blocks, s->max_nl, nullptr,
@@ -1167,7 +1209,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         break;
       case QD_STAGE_BACKWARD_LEGENDRE:
         if (s->precision == QD_PRECISION_MIXED)
-          launch_legendre_tc_bwd(st, g, s->psi_jf, s->psi_th, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf,
+          launch_legendre_tc_bwd(st, g, s->psi_jf, s->psi_thf, s->d_blocks, s->n_blocks, s->img_b, s->imgoff_b, s->wf,
                                  s->wvf, s->part_modpe, s->t_modpe, s->smem_b, s->status, s->status, s->bscale_b, s->max_nl);
         else
           launch_legendre_bwd_f64(st, g, s->psi_j, s->psi_th, s->Bb, s->d_blocks, s->n_blocks, nullptr, s->w, s->pot,
@@ -1254,8 +1296,12 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
                                   s->status);
         const int64_t ns = (int64_t)g.nth * g.n1;
         dim3 grid((unsigned)std::min<int64_t>((ns + 255) / 256, 64), (unsigned)s->n_blocks);
-        k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
-                                                 s->flux_buf, s->n_blocks, s->flux_slot, s->status);
+        if (s->psi_thf)
+          k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_thf, s->half_v, s->fd,
+                                                   s->flux_buf, s->n_blocks, s->flux_slot, s->status);
+        else
+          k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
+                                                   s->flux_buf, s->n_blocks, s->flux_slot, s->status);
         k_step_end<<<1, 1, 0, st>>>(s->d_step, s->status, nullptr, nullptr, 0.0, 0);
         s->steps++;
         if (++s->flux_pending == s->flux.chunk) flush_flux(s);
@@ -1278,7 +1324,8 @@ int qd_session_get_psi(qd_session *s, int32_t which, int32_t block, double *host
     QD_REQUIRE(n_doubles == 2 * n, "buffer size");
     QD_CUDA(cudaStreamSynchronize(s->stream));
     if (which == 0) {
-      QD_CUDA(cudaMemcpy(host_out, s->psi_th + (int64_t)block * n, n * sizeof(double2), cudaMemcpyDeviceToHost));
+      theta_to_host(s, (int64_t)block * n, (int64_t)n, host_out);
+      QD_CUDA(cudaStreamSynchronize(s->stream));
     } else if (s->psi_jf) {   // mixed form: c64 pool, widened exactly
       std::vector<float2> tmp(n);
       QD_CUDA(cudaMemcpy(tmp.data(), s->psi_jf + (int64_t)bd.slab0 * s->g.npt, n * sizeof(float2),
@@ -1302,7 +1349,8 @@ int qd_session_set_psi(qd_session *s, int32_t which, int32_t block, const double
     QD_REQUIRE(n_doubles == 2 * n, "buffer size");
     QD_CUDA(cudaStreamSynchronize(s->stream));
     if (which == 0) {
-      QD_CUDA(cudaMemcpy(s->psi_th + (int64_t)block * n, host_in, n * sizeof(double2), cudaMemcpyHostToDevice));
+      theta_from_host(s, (int64_t)block * n, (int64_t)n, host_in);
+      QD_CUDA(cudaStreamSynchronize(s->stream));
     } else if (s->psi_jf) {   // mixed form: c64 pool, rounded to nearest
       std::vector<float2> tmp(n);
       for (size_t q = 0; q < n; q++) tmp[q] = make_float2((float)host_in[2 * q], (float)host_in[2 * q + 1]);

@@ -85,9 +85,13 @@ struct Grid {
   double dr1, dr2, m1, m2, left1, left2;
 };
 
-// theta-space phase: psi[b][k][j][i] *= tab[k][j][i] for every block
-void launch_theta_phase(cudaStream_t s, double2 *psi, const double2 *tab, int n_blocks,
-                        int64_t n_per_block, const int *status);
+// theta-space phase: psi[b][k][j][i] *= tab[k][j][i] for every block; psi c128 or c64
+template <typename S>
+void launch_theta_phase(cudaStream_t s, S *psi, const double2 *tab, int n_blocks, int64_t n_per_block,
+                        const int *status);
+// c64 -> c128 (exact) and c128 -> c64 (round to nearest) element copies
+void launch_widen(cudaStream_t s, const float2 *src, double2 *dst, int64_t n);
+void launch_narrow(cudaStream_t s, const double2 *src, float2 *dst, int64_t n);
 
 // j-space phase: slab s (l = slabs[s].l) *= tab[l][j][i]; psi_j c128 or c64
 template <typename S>
@@ -190,7 +194,7 @@ void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &
                              const StepTail *tail = nullptr);
 void launch_build_half_v_lift(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
                               float2 *half_v);
-void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const double2 *psi_th,
+void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const float2 *psi_th,
                              int n_blocks, const float2 *half_v, const float *fd, double2 *buf, const int *slot,
                              const int *status);
 
@@ -234,11 +238,11 @@ bool tc_shape_ok(int Kp, int Np);
 void tc_set_smem_limit(size_t bytes);
 void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,
                             bool fwd, const int64_t *img_off, uint16_t *img, float *bscale, int max_np);
-void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const double2 *psi_th, float2 *psi_j,
+void launch_legendre_tc_fwd(cudaStream_t s, const Grid &g, const float2 *psi_th, float2 *psi_j,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float2 *vph, const float *d1f, const float *d2f, size_t smem, const int *status,
                             int *status_w, const float *bscale, int max_nl);
-void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, double2 *psi_th,
+void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, float2 *psi_th,
                             const BlockDesc *blocks, int n_blocks, const uint16_t *img, const int64_t *img_off,
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
                             const int *status, int *status_w, const float *bscale, int max_nl);
