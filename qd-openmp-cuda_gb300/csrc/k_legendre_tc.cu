@@ -289,6 +289,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   unsigned char *sA = smem;
   unsigned char *sB = smem + 3 * a_term_max;
   float *sF = reinterpret_cast<float *>(sB + 3 * b_term_max);
+  float *sWV = sF + 128 * (kp_max + 1);   // backward: w V of the tile, [n][64 points]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t ncols = 512;
   const int t_begin = (int)((int64_t)blockIdx.x * n_tiles / gridDim.x);
@@ -389,33 +390,34 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         const int m = tid >> 1, half = tid & 1;
         const float *row = sF + m * LDF;
         float mx = 0.0f;
-        for (int k = 0; k < T.Kp; k++) mx = fmaxf(mx, fabsf(row[k]));
-        int e = 0;
-        if (mx >= 1e-30f) frexpf(mx, &e);
-        const float inv = mx >= 1e-30f ? ldexpf(1.0f, -e) * 256.0f : 0.0f;
-        if (half == 0) srow_s[it & 1][m] = ldexpf(1.0f, e - 16);
+        for (int k = half; k < T.Kp; k += 2) mx = fmaxf(mx, fabsf(row[k]));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+        // mx = f 2^e, f in [0.5, 1): row scale 2^e, slices of a = 256 x / 2^e
+        const int e = mx >= 1e-30f ? (int)((__float_as_uint(mx) >> 23) & 0xffu) - 126 : 0;
+        const float inv = mx >= 1e-30f ? __uint_as_float((uint32_t)(127 + 8 - e) << 23) : 0.0f;
+        if (half == 0) srow_s[it & 1][m] = __uint_as_float((uint32_t)(127 + e - 16) << 23);
         const uint32_t orow = (uint32_t)(m / 8) * T.SBO + (m % 8) * 16;
+        // round to nearest even integer for |x| <= 2^22: (x + 1.5 2^23) - 1.5 2^23
+        auto rne = [](float x) { return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f); };
         for (int kg = half; kg < T.Kp / 8; kg += 2) {
           uint32_t w[3][4];
 #pragma unroll
-          for (int e8 = 0; e8 < 8; e8++) {
-            const float a = row[kg * 8 + e8] * inv;
-            const float i0 = rintf(a);
-            const float r1 = (a - i0) * 256.0f;
-            const float i1 = rintf(r1);
-            const float i2 = rintf((r1 - i1) * 256.0f);
-            const uint16_t h0 = __bfloat16_as_ushort(__float2bfloat16_rn(i0));
-            const uint16_t h1 = __bfloat16_as_ushort(__float2bfloat16_rn(i1));
-            const uint16_t h2 = __bfloat16_as_ushort(__float2bfloat16_rn(i2));
-            if (e8 & 1) {
-              w[0][e8 >> 1] |= (uint32_t)h0 << 16;
-              w[1][e8 >> 1] |= (uint32_t)h1 << 16;
-              w[2][e8 >> 1] |= (uint32_t)h2 << 16;
-            } else {
-              w[0][e8 >> 1] = h0;
-              w[1][e8 >> 1] = h1;
-              w[2][e8 >> 1] = h2;
+          for (int e2 = 0; e2 < 4; e2++) {
+            uint32_t b[3][2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+              const float a = __fmul_rn(row[kg * 8 + 2 * e2 + h], inv);
+              const float i0 = rne(a);
+              const float r1 = __fmul_rn(__fsub_rn(a, i0), 256.0f);
+              const float i1 = rne(r1);
+              const float i2 = rne(__fmul_rn(__fsub_rn(r1, i1), 256.0f));
+              // |i| <= 256 integers: the BF16 encoding is the upper half of the FP32 one
+              b[0][h] = __float_as_uint(i0);
+              b[1][h] = __float_as_uint(i1);
+              b[2][h] = __float_as_uint(i2);
             }
+#pragma unroll
+            for (int t = 0; t < 3; t++) w[t][e2] = __byte_perm(b[t][0], b[t][1], 0x7632);
           }
 #pragma unroll
           for (int t = 0; t < 3; t++)
@@ -438,15 +440,21 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       const TcTile T = tc_tile<FWD>(P, tt, mtiles);
       const BlockDesc bd = P.blocks[T.b];
       const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
-      // backward: this thread's first chunk of w V, requested before the MMA wait
-      float wv[16];
-      if (!FWD) {
+      // backward: the w V values of this thread's columns, copied asynchronously
+      // into shared memory before the MMA wait (the re/im pair shares them: the
+      // even lane copies, both read after the warp synchronises)
+      if (!FWD && c == 0 && p < g.npt) {
+        for (int n0 = 16 * chalf; n0 < T.Nv; n0 += 32)
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const int n = 16 * chalf + q;
-          wv[q] = (n < T.Nv && p < g.npt) ? __ldg(P.wv + (int64_t)n * g.npt + p) : 0.0f;
-        }
+          for (int q = 0; q < 16; q++) {
+            const int n = n0 + q;
+            if (n < T.Nv)
+              asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(sWV + n * TC_POINTS + pl)),
+                           "l"(P.wv + (int64_t)n * g.npt + p)
+                           : "memory");
+          }
       }
+      if (!FWD) asm volatile("cp.async.commit_group;" ::: "memory");
       if (ctid == 0) {
         bool ok = mbar_wait_bounded(smem_u32(&mb_ready), (uint32_t)(it & 1));
         if (ok && it > 0) ok = mbar_wait_bounded(smem_u32(&mb_free), (uint32_t)((it - 1) & 1));
@@ -493,16 +501,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       float mod = 0.0f, pe = 0.0f;
       float *Cf = reinterpret_cast<float *>(P.C);
       const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
+      if (!FWD) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncwarp();
+      }
       for (int n0 = 16 * chalf; n0 < T.Np; n0 += 32) {
-        // the next chunk's w V values are requested before this chunk is used
-        float wv_nxt[16];
-        if (!FWD) {
-#pragma unroll
-          for (int q = 0; q < 16; q++) {
-            const int n = n0 + 32 + q;
-            wv_nxt[q] = (n < T.Nv && p < g.npt) ? __ldg(P.wv + (int64_t)n * g.npt + p) : 0.0f;
-          }
-        }
         float d0[16], d1[16], d2[16];
         tmem_ld16(trow + (uint32_t)n0, d0);
         tmem_ld16(trow + (uint32_t)(T.Np + n0), d1);
@@ -519,18 +522,15 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
                 Cf[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = v;
                 const float v2 = v * v;
                 mod = fmaf(w_s[n], v2, mod);
-                pe = fmaf(wv[q], v2, pe);
+                pe = fmaf(sWV[n * TC_POINTS + pl], v2, pe);
               }
             }
           }
         }
-        if (!FWD) {
-#pragma unroll
-          for (int q = 0; q < 16; q++) wv[q] = wv_nxt[q];
-        }
       }
       tc_fence_before();
       mbar_arrive(smem_u32(&mb_free));
+      __syncwarp();   // both lanes of a re/im pair are done with the w V tile
       if (!FWD && P.part) {
         // fixed-order reduction over the 256 consumer threads
         for (int o = 16; o > 0; o >>= 1) {
@@ -567,28 +567,21 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   }
 }
 
-// Dynamic shared memory of one launch: the BF16 slices of A and B and the
-// FP32 staging rows, and at least enough that no more than 512/ncols CTAs fit
-// on an SM (233472 bytes of shared memory), so the TMEM columns that their
-// allocations need never exceed the SM's 512.
-size_t tc_smem_bytes(int Kp, int Np) {
-  const size_t need = (size_t)3 * 16 * (Kp / 8 * 128) + (size_t)tc_bimg_bytes(Np, Kp) + (size_t)128 * (Kp + 1) * 4 +
-                      (size_t)Np * TC_POINTS * 4;
-  const size_t ctas = 512 / tc_tmem_cols(Np);
-  return std::max(need, (size_t)233472 / (ctas + 1) + 1024);
+// Dynamic shared memory of the persistent kernel: the BF16 slices of A and B,
+// the FP32 staging rows and (backward) the w V tile, and at least 120 KB so
+// that one CTA (holding all 512 TMEM columns) runs per SM.
+size_t tc_ws_smem_bytes(bool fwd, int kp_max, int np_max) {
+  const size_t need = (size_t)3 * 16 * (kp_max / 8 * 128) + (size_t)tc_bimg_bytes(np_max, kp_max) +
+                      (size_t)128 * (kp_max + 1) * 4 + (fwd ? 0 : (size_t)np_max * TC_POINTS * 4);
+  return std::max(need, (size_t)120 * 1024);
 }
 
-bool tc_shape_ok(int Kp, int Np) { return Kp <= 192 && Np <= 160 && tc_smem_bytes(Kp, Np) <= 200 * 1024; }
+bool tc_shape_ok(bool fwd, int Kp, int Np) {
+  return Kp <= 192 && Np <= 160 && tc_ws_smem_bytes(fwd, Kp, Np) <= 220 * 1024;
+}
 
 int legendre_tc_part_tiles(const Grid &g) { return (int)((g.npt + TC_POINTS - 1) / TC_POINTS); }
 
-// persistent launch: A/B slices for the largest tile and the FP32 staging rows,
-// and at least 120 KB so that one CTA (holding all 512 TMEM columns) runs per SM
-size_t tc_ws_smem_bytes(int kp_max, int np_max) {
-  const size_t need =
-      (size_t)3 * 16 * (kp_max / 8 * 128) + (size_t)tc_bimg_bytes(np_max, kp_max) + (size_t)128 * (kp_max + 1) * 4;
-  return std::max(need, (size_t)120 * 1024);
-}
 
 void launch_legendre_tc_ws(cudaStream_t s, bool fwd, const TcArgs &a, int n_blocks, int kp_max, int np_max) {
   const int mtiles = legendre_tc_part_tiles(a.g);
@@ -597,7 +590,7 @@ void launch_legendre_tc_ws(cudaStream_t s, bool fwd, const TcArgs &a, int n_bloc
   QD_CUDA(cudaGetDevice(&dev));
   QD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int grid = std::min(n_tiles, sms);
-  const size_t smem = tc_ws_smem_bytes(kp_max, np_max);
+  const size_t smem = tc_ws_smem_bytes(fwd, kp_max, np_max);
   if (fwd)
     k_legendre_tc_ws<true><<<grid, WS_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
   else
@@ -649,9 +642,8 @@ void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, 
 }
 
 void tc_set_smem_limit(size_t bytes) {
-  (void)bytes;
-  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
 }
 
 void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,

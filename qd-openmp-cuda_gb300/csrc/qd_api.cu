@@ -758,14 +758,14 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     for (const BlockDesc &bd : s->h_blocks) {
       of.push_back(tf);
       tf += 3LL * r16(bd.nl) * r16(g.nth) * 2;
-      s->smem_f = std::max(s->smem_f, tc_smem_bytes(r16(g.nth), r16(bd.nl)));
+      s->smem_f = std::max(s->smem_f, tc_ws_smem_bytes(true, r16(g.nth), r16(bd.nl)));
       ob.push_back(tb);
       tb += 3LL * r16(g.nth) * r16(bd.nl) * 2;
-      s->smem_b = std::max(s->smem_b, tc_smem_bytes(r16(bd.nl), r16(g.nth)));
+      s->smem_b = std::max(s->smem_b, tc_ws_smem_bytes(false, r16(bd.nl), r16(g.nth)));
     }
     bool ok = true;
     for (const BlockDesc &bd : s->h_blocks)
-      ok = ok && tc_shape_ok(r16(g.nth), r16(bd.nl)) && tc_shape_ok(r16(bd.nl), r16(g.nth));
+      ok = ok && tc_shape_ok(true, r16(g.nth), r16(bd.nl)) && tc_shape_ok(false, r16(bd.nl), r16(g.nth));
     if (!ok) {
       if (s->precision == QD_PRECISION_MIXED)
         throw Error{QD_ERR_UNSUPPORTED, "mixed form: n_theta and l_max+1 above the tensor-core tile limit "

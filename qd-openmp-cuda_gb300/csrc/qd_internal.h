@@ -233,8 +233,8 @@ void launch_build_float_tables(cudaStream_t s, const Grid &g, const double *w, c
 
 // tcgen05 BF16x3 Legendre contraction
 struct TcArgs;
-size_t tc_smem_bytes(int Kp, int Np);
-bool tc_shape_ok(int Kp, int Np);
+size_t tc_ws_smem_bytes(bool fwd, int kp_max, int np_max);
+bool tc_shape_ok(bool fwd, int Kp, int Np);
 void tc_set_smem_limit(size_t bytes);
 void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,
                             bool fwd, const int64_t *img_off, uint16_t *img, float *bscale, int max_np);
