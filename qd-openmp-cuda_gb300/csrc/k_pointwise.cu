@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(256) k_energy_finalize(Grid g, EnergyParts ep,
   const int step = *d_step;   // advanced only by the last CTA, after every CTA has read it
   const int fcount = (tid == 0 && tail.flux_count) ? *tail.flux_count : 0;
   const BlockDesc bd = blocks[b];
-  // the partials of this block as one index space: [module/potential pairs | kinetic | rotational | Coriolis]
+  // partial counts of this block: module/potential pairs, kinetic, rotational, Coriolis
   const int n0 = ep.have_mod ? ep.mod_pe_tiles : 0;
   const int n1 = ep.have_ke ? bd.nl * ep.ke_tiles : 0;
   const int n2 = ep.have_re ? bd.nl * ep.re_tiles : 0;
@@ -321,20 +321,26 @@ __global__ void __launch_bounds__(256) k_energy_finalize(Grid g, EnergyParts ep,
   const double2 *mp = reinterpret_cast<const double2 *>(ep.mod_pe) + (int64_t)b * ep.mod_pe_tiles;
   const double *kp = ep.ke + (int64_t)bd.slab0 * ep.ke_tiles;
   const double *rp = ep.re + (int64_t)bd.slab0 * ep.re_tiles;
-  const int total = n0 + n1 + n2 + n3;
+  // two warps per quantity (warp-uniform branch, no divergence inside a loop),
+  // so that each lane's loads are independent and issue together
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  const int wq = tid >> 6, l64 = tid & 63;
+  if (wq == 0) {
 #pragma unroll 8
-  for (int t = tid; t < total; t += 256) {
-    if (t < n0) {
+    for (int t = l64; t < n0; t += 64) {
       const double2 v = mp[t];
       acc[0] += v.x;
       acc[1] += v.y;
-    } else if (t < n0 + n1) {
-      acc[2] += kp[t - n0];
-    } else if (t < n0 + n1 + n2) {
-      acc[3] += rp[t - n0 - n1];
-    } else {
-      const int q = t - n0 - n1 - n2;
+    }
+  } else if (wq == 1) {
+#pragma unroll 8
+    for (int t = l64; t < n1; t += 64) acc[2] += kp[t];
+  } else if (wq == 2) {
+#pragma unroll 8
+    for (int t = l64; t < n2; t += 64) acc[3] += rp[t];
+  } else {
+#pragma unroll 4
+    for (int q = l64; q < n3; q += 64) {
       const int gi = g_lo + q / ep.ce_tiles, tt = q - (q / ep.ce_tiles) * ep.ce_tiles;
       const int o = bd.omega - groups[gi].omega_lo;
       if (o >= 0 && o < groups[gi].n) acc[4] += ep.ce[((int64_t)gi * ce_n + o) * ep.ce_tiles + tt];
