@@ -183,6 +183,49 @@ def run_form(qd, precision: int, steps: int, warmup: int, sampler=None):
                 "clocks": clocks, "psi": psi, "d": d}
 
 
+OTHER_WORKLOADS = ("fh2_j12_256x128x96", "fh2_batched_j0-40_192x96x80")
+
+
+def workload_problems(qd, name: str, precision: int):
+    """FH2Data list of a named workload: one problem, or the batched J=0..40 partial waves."""
+    if name.startswith("fh2_batched"):
+        ds = [qd.inputs.build_fh2data(c) for c in qd.inputs.batched_partial_waves()]
+    else:
+        ds = [qd.inputs.build_fh2data(qd.inputs.CONFIGS[name])]
+    for d in ds:
+        d["options"]["precision"] = precision
+    return ds
+
+
+def workload_mode(qd, name: str, precision: int, steps: int, warmup: int):
+    """Device-timed steps of any named workload (the secondary configurations)."""
+    import torch
+
+    ds = workload_problems(qd, name, precision)
+    with qd.Session(ds) as s:
+        stream = torch.cuda.ExternalStream(s.stream())
+        s.run(warmup)
+        s.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        s.run(steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        prof = s.profile(max(1, min(steps, 4)))
+        e = s.energies()
+        nb = s.n_blocks
+    tot = sum(v["ms"] * v["per_step"] for v in prof.values())
+    return {"mode": "workload", "workload": name, "precision": "mixed" if precision else "fp64",
+            "problems": len(ds), "omega_blocks": nb, "steps": steps, "warmup": warmup,
+            "value": steps * nb / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+            "module_min": float(e[:, 0].min()), "module_max": float(e[:, 0].max()),
+            "kernels": {k: {"ms": round(v["ms"], 5), "per_step": v["per_step"],
+                            "share": round(v["ms"] * v["per_step"] / tot, 4)} for k, v in prof.items()}}
+
+
 def e2e(qd, precision: int, steps: int):
     """K steps through cudaOpenMPEvolution with pinned host buffers."""
     import torch
@@ -305,6 +348,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only build the workload and run this many steps of --precision (for ncu captures)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--workload", default="", choices=("",) + OTHER_WORKLOADS,
+                    help="time a secondary configuration (--precision) instead of the headline benchmark")
     ap.add_argument("--accuracy", type=int, default=0,
                     help="run the mixed-vs-FP64 accuracy study for this many steps instead of the benchmark")
     args = ap.parse_args()
@@ -322,6 +367,11 @@ def main():
     qd.load_library()
     if args.accuracy:
         print(json.dumps({"accuracy": accuracy(qd, args.accuracy)}), flush=True)
+        return
+    if args.workload:
+        line = workload_mode(qd, args.workload, 1 if args.precision == "mixed" else 0, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
         return
     if args.profile_steps:
         d = qd.inputs.build_fh2data(qd.inputs.CONFIGS[WORKLOAD])

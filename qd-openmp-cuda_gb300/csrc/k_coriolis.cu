@@ -46,6 +46,227 @@ void launch_build_coriolis_phase(cudaStream_t s, const Grid &g, const CoriolisGr
   k_build_coriolis_phase<<<dim3(4, n_groups), 256, 0, s>>>(g, groups, e, dt, ph);
 }
 
+// ------------------------------------------------------------ mixed form
+// Same operator in FP32 arithmetic on the c64 pool, for up to 24 coupled
+// Omega blocks.  The eigenvectors are held as FP32 pairs V = Vh + Vl (the
+// pair carries V to ~2^-48), so the applied U stays unitary to FP64 level and
+// the per-step rounding is random rather than a fixed bias; the phases
+// exp(-i dt e_a/(2 m1 R^2)) and the rotational phases before/after are
+// three-shear rotations of determinant exactly 1.  Each CTA walks a strided
+// 1/tiles of the points of one group (one l), so the coupling and rotational
+// energy partials are [group][omega][tiles] and [slab][tiles].
+namespace {
+__device__ inline void lift2c(float2 &v, float2 ts) {
+  float x = v.x, y = v.y;
+  x = fmaf(ts.x, y, x);
+  y = fmaf(ts.y, x, y);
+  x = fmaf(ts.x, y, x);
+  x = fmaf(ts.x, y, x);
+  y = fmaf(ts.y, x, y);
+  x = fmaf(ts.x, y, x);
+  v.x = x;
+  v.y = y;
+}
+}  // namespace
+
+template <int MAXN, bool EN>
+__global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__restrict__ psi_j,
+                                                              const BlockDesc *__restrict__ blocks,
+                                                              const CoriolisGroup *__restrict__ groups,
+                                                              const float *__restrict__ Vh, const float *__restrict__ Vl,
+                                                              const float2 *__restrict__ phl, const double *__restrict__ Hp,
+                                                              const float2 *__restrict__ rotR, const float2 *__restrict__ rotr,
+                                                              int pro, int epi, const float *__restrict__ I1f,
+                                                              const float *__restrict__ I2f, double *__restrict__ ce_part,
+                                                              double *__restrict__ re_part, int tiles, int ce_n,
+                                                              const int *status) {
+  if (status && *status) return;
+  __shared__ float sVh[MAXN * MAXN], sVl[MAXN * MAXN];
+  __shared__ float Hd[MAXN], Ho[MAXN];
+  __shared__ float red[COR_THREADS / 32][2 * MAXN];
+  const CoriolisGroup gr = groups[blockIdx.y];
+  const int n = gr.n, l = gr.l;
+  // row stride MAXN: every (o, a) offset below is a compile-time constant
+  for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
+    sVh[(q / n) * MAXN + q % n] = Vh[gr.v0 + q];
+    sVl[(q / n) * MAXN + q % n] = Vl[gr.v0 + q];
+  }
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    Hd[q] = (float)Hp[gr.h0 + q * n + q];
+    Ho[q] = q + 1 < n ? (float)Hp[gr.h0 + q * n + q + 1] : 0.0f;
+  }
+  __shared__ int64_t base[MAXN];   // slab offset of each member block
+  for (int o = threadIdx.x; o < n; o += blockDim.x) {
+    const BlockDesc bd = blocks[gr.block_lo + o];
+    base[o] = (int64_t)(bd.slab0 + (l - bd.omega)) * g.npt;
+  }
+  __syncthreads();
+  const float ll = (float)l * (float)(l + 1);
+  constexpr int NE = EN ? MAXN : 1;   // energy accumulators only in the energy variant
+  float ce[NE], re[NE];
+#pragma unroll
+  for (int o = 0; o < NE; o++) ce[o] = re[o] = 0.0f;
+  for (int64_t pt = (int64_t)blockIdx.x * COR_THREADS + threadIdx.x; pt < g.npt; pt += (int64_t)tiles * COR_THREADS) {
+    const int i = (int)(pt % g.n1), j = (int)(pt / g.n1);
+    float2 x[MAXN];
+#pragma unroll
+    for (int o = 0; o < MAXN; o++) x[o] = o < n ? psi_j[base[o] + pt] : make_float2(0.0f, 0.0f);
+    float2 tR = make_float2(0.0f, 0.0f), tr = make_float2(0.0f, 0.0f);
+    if (pro || epi) {
+      tR = __ldg(rotR + (int64_t)l * g.n1 + i);
+      tr = __ldg(rotr + (int64_t)l * g.n2 + j);
+    }
+    if (pro) {
+#pragma unroll
+      for (int o = 0; o < MAXN; o++)
+        if (o < n) {
+          lift2c(x[o], tR);
+          lift2c(x[o], tr);
+        }
+    }
+    const float inv1 = __ldg(I1f + i);
+    if (EN) {   // coupling energy of the incoming state
+#pragma unroll
+      for (int o = 0; o < NE; o++)
+        if (o < n) {
+          float c = Hd[o] * (x[o].x * x[o].x + x[o].y * x[o].y);
+          if (o + 1 < n) c = fmaf(2.0f * Ho[o], x[o].x * x[o + 1].x + x[o].y * x[o + 1].y, c);
+          ce[o] = fmaf(inv1, c, ce[o]);
+        }
+    }
+    // y = V^T x: one pass over the members o, every a accumulating independently.
+    // V is re-read from shared memory per point (volatile): held in registers
+    // across the point loop it would leave room for only a few warps
+    const volatile float *vVh = sVh, *vVl = sVl;
+    float2 y[MAXN];
+#pragma unroll
+    for (int a = 0; a < MAXN; a++) y[a] = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int o = 0; o < MAXN; o++) {
+      if (o < n) {
+#pragma unroll
+        for (int a = 0; a < MAXN; a++)
+          if (a < n) {
+            const float vh = vVh[o * MAXN + a], vl = vVl[o * MAXN + a];
+            y[a].x = fmaf(vl, x[o].x, fmaf(vh, x[o].x, y[a].x));
+            y[a].y = fmaf(vl, x[o].y, fmaf(vh, x[o].y, y[a].y));
+          }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < MAXN; a++)
+      if (a < n) lift2c(y[a], __ldg(phl + gr.ph0 + (int64_t)a * g.n1 + i));
+    // x = V y
+#pragma unroll
+    for (int o = 0; o < MAXN; o++) x[o] = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int a = 0; a < MAXN; a++) {
+      if (a < n) {
+#pragma unroll
+        for (int o = 0; o < MAXN; o++)
+          if (o < n) {
+            const float vh = vVh[o * MAXN + a], vl = vVl[o * MAXN + a];
+            x[o].x = fmaf(vl, y[a].x, fmaf(vh, y[a].x, x[o].x));
+            x[o].y = fmaf(vl, y[a].y, fmaf(vh, y[a].y, x[o].y));
+          }
+      }
+    }
+    const float rI = ll * (inv1 + __ldg(I2f + j));
+#pragma unroll
+    for (int o = 0; o < MAXN; o++) {
+      if (o < n) {
+        float2 v = x[o];
+        if (epi) {
+          lift2c(v, tR);
+          lift2c(v, tr);
+        }
+        if constexpr (EN) re[o] = fmaf(rI, v.x * v.x + v.y * v.y, re[o]);
+        psi_j[base[o] + pt] = v;
+      }
+    }
+  }
+  if constexpr (!EN) return;
+  // per-Omega partials: shuffle tree per warp, then the warps in a fixed order
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 0; o < NE; o++) {
+    if (o < n) {
+      float c = ce[o], r = re[o];
+      for (int s = 16; s > 0; s >>= 1) {
+        c += __shfl_down_sync(0xffffffffu, c, s);
+        r += __shfl_down_sync(0xffffffffu, r, s);
+      }
+      if (lane == 0) {
+        red[warp][o] = c;
+        red[warp][MAXN + o] = r;
+      }
+    }
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < n; o += blockDim.x) {
+    double c = 0.0, r = 0.0;
+    for (int w = 0; w < COR_THREADS / 32; w++) {
+      c += (double)red[w][o];
+      r += (double)red[w][MAXN + o];
+    }
+    if (ce_part) ce_part[((int64_t)blockIdx.y * ce_n + o) * tiles + blockIdx.x] = c;
+    if (re_part) {
+      const BlockDesc bd = blocks[gr.block_lo + o];
+      re_part[(int64_t)(bd.slab0 + (l - bd.omega)) * tiles + blockIdx.x] = r;
+    }
+  }
+}
+
+void launch_coriolis_f32(cudaStream_t s, const Grid &g, float2 *psi_j, const BlockDesc *blocks,
+                         const CoriolisGroup *groups, int n_groups, int max_n, const float *Vh, const float *Vl,
+                         const float2 *phl, const double *H, const float2 *rotR, const float2 *rotr, bool pro,
+                         bool epi, const float *I1f, const float *I2f, double *ce_part, double *re_part, int tiles,
+                         const int *status) {
+  if (n_groups == 0) return;
+  dim3 grid((unsigned)tiles, (unsigned)n_groups);
+#define QD_COR32(M)                                                                                          \
+  do {                                                                                                       \
+    if (ce_part)                                                                                             \
+      k_coriolis_f32<M, true><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H, rotR, rotr, \
+                                                           pro ? 1 : 0, epi ? 1 : 0, I1f, I2f, ce_part, re_part, \
+                                                           tiles, max_n, status);                             \
+    else                                                                                                     \
+      k_coriolis_f32<M, false><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H, rotR,     \
+                                                            rotr, pro ? 1 : 0, epi ? 1 : 0, I1f, I2f, nullptr,   \
+                                                            nullptr, tiles, max_n, status);                  \
+  } while (0)
+  if (max_n <= 4) QD_COR32(4);
+  else if (max_n <= 8) QD_COR32(8);
+  else if (max_n <= 12) QD_COR32(12);
+  else if (max_n <= 16) QD_COR32(16);
+  else if (max_n <= 20) QD_COR32(20);
+  else if (max_n <= CORIOLIS_F32_MAXN) QD_COR32(24);
+  else throw Error{QD_ERR_UNSUPPORTED, "FP32 Coriolis: more than 24 coupled Omega blocks"};
+#undef QD_COR32
+}
+
+// half-step phase exp(-i dt e_a / (2 m1 R^2)) of every group as three-shear
+// coefficients (applied twice), [ph0 + a n1 + i]
+__global__ void k_build_coriolis_lift(Grid g, const CoriolisGroup *__restrict__ groups, const double *__restrict__ e,
+                                      double dt, float2 *__restrict__ phl) {
+  const CoriolisGroup gr = groups[blockIdx.y];
+  const int64_t n = (int64_t)gr.n * g.n1;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(q / g.n1), i = (int)(q % g.n1);
+    const double R = g.left1 + i * g.dr1;
+    const double ang = -dt * e[gr.e0 + a] / (2 * g.m1 * R * R);
+    const double r = remainder(ang, 2.0 * M_PI);
+    const double h = 0.5 * r;
+    phl[gr.ph0 + q] = make_float2((float)(-tan(0.5 * h)), (float)sin(h));
+  }
+}
+
+void launch_build_coriolis_lift(cudaStream_t s, const Grid &g, const CoriolisGroup *groups, int n_groups,
+                                const double *e, double dt, float2 *phl) {
+  if (n_groups == 0) return;
+  k_build_coriolis_lift<<<dim3(4, n_groups), 256, 0, s>>>(g, groups, e, dt, phl);
+}
+
 template <int MAXN, typename S>
 __global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, S *__restrict__ psi_j,
                                                           const BlockDesc *__restrict__ blocks,

@@ -273,6 +273,10 @@ struct qd_session {
   int n_groups = 0, max_group_n = 1;
   double *cor_V = nullptr, *cor_e = nullptr, *cor_H = nullptr;
   double2 *cor_ph = nullptr;
+  // mixed form with at most CORIOLIS_F32_MAXN coupled blocks: FP32 Coriolis
+  bool cor_f32 = false;
+  float *cor_Vh = nullptr, *cor_Vl = nullptr;
+  float2 *cor_phl = nullptr;
   std::vector<int> h_pgroup0;
   int *d_pgroup0 = nullptr;
   // energies
@@ -390,7 +394,8 @@ __global__ void k_flux_reset(int *count) { *count = 0; }
 qd_session::~qd_session() {
   if (graph_chunk) cudaGraphExecDestroy(graph_chunk);
   void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, psi_thf, psi_jf, xfer, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
-                  tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, d_pgroup0,
+                  tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, cor_Vh, cor_Vl, cor_phl,
+                  d_pgroup0,
                   part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
                   flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
                   img_f, img_b, bscale_f, bscale_b, imgoff_f, imgoff_b, vph, vph0, lrotR, lrotr, lkinR, lkinr, wf, wvf, d1f, d2f,
@@ -455,7 +460,12 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
   launch_legendre_tc_fwd(st, g, s->psi_thf, s->psi_jf, s->d_blocks, s->n_blocks, s->img_f, s->imgoff_f,
                          first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status, s->bscale_f, s->max_nl);
   prof_mark(st, "legendre_forward");
-  if (s->any_coupled) {
+  if (s->cor_f32) {
+    launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_Vh,
+                        s->cor_Vl, s->cor_phl, s->cor_H, s->lrotR, s->lrotr, true, true, s->I1f, s->I2f, nullptr,
+                        nullptr, s->t_ce, s->status);
+    prof_mark(st, "coriolis");
+  } else if (s->any_coupled) {
     launch_coriolis(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
                     s->cor_H, nullptr, s->t_ce, s->tab_rot4, s->status, s->tab_rot4);
     prof_mark(st, "coriolis");
@@ -473,7 +483,13 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
   lf.I2f = s->I2f;
   launch_fft_kinetic(st, g, s->fft, s->psi_jf, s->d_slabs, s->n_slabs, s->part_ke,
                      s->any_coupled ? nullptr : s->part_re, s->status, &lf);
-  if (s->any_coupled) {
+  if (s->cor_f32) {
+    // coupling energy of the incoming state, rotational energy of the outgoing one
+    launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_Vh,
+                        s->cor_Vl, s->cor_phl, s->cor_H, s->lrotR, s->lrotr, false, true, s->I1f, s->I2f,
+                        s->part_ce, s->part_re, s->t_ce, s->status);
+    prof_mark(st, "coriolis_energy");
+  } else if (s->any_coupled) {
     launch_coriolis(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, s->cor_ph,
                     s->cor_H, s->part_ce, s->t_ce, s->tab_rot4, s->status);
     prof_mark(st, "coriolis_energy");
@@ -559,7 +575,8 @@ static void enqueue_tail(qd_session *s) {
 static int count_launches_per_step(qd_session *s) {
   const bool slab = s->precision == QD_PRECISION_MIXED && (s->fft.cluster || s->fft.sep >= 0);
   int n = 1 + (slab ? 1 : 3) + 1 + 1;   // fwd, fft, bwd, finalize (+ step counter)
-  if (s->any_coupled) n += 3;           // coriolis x2, rot energy
+  if (s->cor_f32) n += 2;              // coriolis x2 (rotational energy fused)
+  else if (s->any_coupled) n += 3;     // coriolis x2, rot energy
   if (s->flux.enabled) n += 1;          // surface extraction
   return n;
 }
@@ -838,13 +855,27 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     s->cor_H = dupload(H.data(), H.size(), st);
     s->cor_ph = dalloc<double2>((size_t)ph0);
     launch_build_coriolis_phase(st, g, s->d_groups, s->n_groups, s->max_group_n, s->cor_e, 0.5 * s->dt, s->cor_ph);
+    if (s->precision == QD_PRECISION_MIXED && s->max_group_n <= CORIOLIS_F32_MAXN) {
+      // eigenvectors as FP32 pairs (hi + lo) and the phases as three-shear coefficients
+      std::vector<float> vh(V.size()), vl(V.size());
+      for (size_t q = 0; q < V.size(); q++) {
+        vh[q] = (float)V[q];
+        vl[q] = (float)(V[q] - (double)vh[q]);
+      }
+      s->cor_Vh = dupload(vh.data(), vh.size(), st);
+      s->cor_Vl = dupload(vl.data(), vl.size(), st);
+      s->cor_phl = dalloc<float2>((size_t)ph0);
+      launch_build_coriolis_lift(st, g, s->d_groups, s->n_groups, s->cor_e, 0.5 * s->dt, s->cor_phl);
+      s->cor_f32 = true;
+    }
   }
 
   // energies and partials
   s->t_modpe = s->precision == QD_PRECISION_MIXED ? legendre_tc_part_tiles(g) : legendre_bwd_part_tiles(g);
   s->t_ke = fft_col_tiles(s->fft, s->precision);
-  s->t_re = s->any_coupled ? 16 : fft_row_tiles(s->fft, s->precision);
-  s->t_ce = coriolis_tiles(g);
+  // coupled: partials of the rotational-energy pass (or of the fused FP32 Coriolis)
+  s->t_re = s->any_coupled ? CORIOLIS_F32_TILES : fft_row_tiles(s->fft, s->precision);
+  s->t_ce = s->cor_f32 ? CORIOLIS_F32_TILES : coriolis_tiles(g);
   s->part_modpe = dalloc<double>((size_t)s->n_blocks * s->t_modpe * 2);
   s->part_ke = dalloc<double>((size_t)s->n_slabs * s->t_ke);
   s->part_re = dalloc<double>((size_t)s->n_slabs * s->t_re);
@@ -1229,7 +1260,14 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         double2 *ph = dalloc<double2>((size_t)s->h_groups.back().ph0 + (size_t)s->h_groups.back().n * g.n1);
         launch_build_coriolis_phase(st, g, s->d_groups, s->n_groups, s->max_group_n, s->cor_e, dt, ph);
         const bool en = stage == QD_STAGE_CORIOLIS_ENERGY;
-        if (s->psi_jf)
+        float2 *phl = nullptr;
+        if (s->cor_f32) {
+          phl = dalloc<float2>((size_t)s->h_groups.back().ph0 + (size_t)s->h_groups.back().n * g.n1);
+          launch_build_coriolis_lift(st, g, s->d_groups, s->n_groups, s->cor_e, dt, phl);
+          launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_Vh,
+                              s->cor_Vl, phl, s->cor_H, nullptr, nullptr, false, false, s->I1f, s->I2f,
+                              en ? s->part_ce : nullptr, nullptr, s->t_ce, s->status);
+        } else if (s->psi_jf)
           launch_coriolis(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_V, ph,
                           s->cor_H, en ? s->part_ce : nullptr, s->t_ce, nullptr, s->status);
         else
@@ -1243,6 +1281,7 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         }
         QD_CUDA(cudaStreamSynchronize(st));
         cudaFree(ph);
+        if (phl) cudaFree(phl);
         break;
       }
       case QD_STAGE_FFT_KINETIC: {

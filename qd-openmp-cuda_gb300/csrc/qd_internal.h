@@ -168,6 +168,21 @@ void launch_coriolis(cudaStream_t s, const Grid &g, S *psi_j, const BlockDesc *b
 void launch_build_coriolis_phase(cudaStream_t s, const Grid &g, const CoriolisGroup *groups, int n_groups,
                                  int max_n, const double *e, double dt, double2 *ph);
 int coriolis_tiles(const Grid &g);
+// Mixed form (FP32 arithmetic, c64 pool, at most CORIOLIS_F32_MAXN coupled
+// blocks): V = Vh + Vl as FP32 pairs, phases as three-shear coefficients
+// (phl from launch_build_coriolis_lift; rotR/rotr the dt/4 rotational phase,
+// applied before when pro, after when epi); optional coupling-energy partials
+// [group][omega][tiles] and rotational-energy partials [slab][tiles] of the
+// outgoing state.
+constexpr int CORIOLIS_F32_MAXN = 24;
+constexpr int CORIOLIS_F32_TILES = 16;   // CTAs per group (its partial tiles)
+void launch_coriolis_f32(cudaStream_t s, const Grid &g, float2 *psi_j, const BlockDesc *blocks,
+                         const CoriolisGroup *groups, int n_groups, int max_n, const float *Vh, const float *Vl,
+                         const float2 *phl, const double *H, const float2 *rotR, const float2 *rotr, bool pro,
+                         bool epi, const float *I1f, const float *I2f, double *ce_part, double *re_part, int tiles,
+                         const int *status);
+void launch_build_coriolis_lift(cudaStream_t s, const Grid &g, const CoriolisGroup *groups, int n_groups,
+                                const double *e, double dt, float2 *phl);
 
 // Energy finalisation: sums partial arrays per block in a fixed order,
 // writes energies[b][6] (and rec if non-null), applies the norm guard.
