@@ -530,32 +530,40 @@ __global__ void __launch_bounds__(SLAB_THREADS, 2) k_fft_slab_cluster(
 // n2 sum T1 |F1 psi|^2 + (1/n1) sum T2 |F2 (n1 A1 psi)|^2, A1 the unitary row
 // propagator, so each pass accumulates its own term.
 namespace {
-// t = -tan(theta/2), s = sin(theta) of theta = u pi/8, u = 1..3
+// t = -tan(theta/2), s = sin(theta) of theta = u pi/24 (units of 7.5 degrees), u = 1..11
 __device__ __forceinline__ float rot_tan_half(int u) {
-  return u == 1 ? 0.198912367379658006911f : (u == 2 ? 0.414213562373095048802f : 0.668178637919298919998f);
+  constexpr float T[12] = {0.0f, 6.554346281523822093e-02f, 1.316524975873958336e-01f, 1.989123673796580061e-01f,
+                           2.679491924311226958e-01f, 3.394542588633758240e-01f, 4.142135623730950345e-01f,
+                           4.931454260313040683e-01f, 5.773502691896257311e-01f, 6.681786379192988790e-01f,
+                           7.673269879789603731e-01f, 8.769764629927567778e-01f};
+  return T[u];
 }
 __device__ __forceinline__ float rot_sin(int u) {
-  return u == 1 ? 0.382683432365089771728f : (u == 2 ? 0.707106781186547524401f : 0.923879532511286756128f);
+  constexpr float S[12] = {0.0f, 1.305261922200515734e-01f, 2.588190451025207395e-01f, 3.826834323650897818e-01f,
+                           0.5f, 6.087614290087206559e-01f, 7.071067811865474617e-01f, 7.933533402912351651e-01f,
+                           8.660254037844385966e-01f, 9.238795325112867385e-01f, 9.659258262890683122e-01f,
+                           9.914448613738103822e-01f};
+  return S[u];
 }
 
-// v *= exp(i u pi/8) for a compile-time-known integer u (after unrolling):
+// v *= exp(i u pi/24) for a compile-time-known integer u (after unrolling):
 // exact for multiples of pi/2, a three-shear rotation otherwise
-__device__ __forceinline__ void rot_pi8(float2 &v, int u) {
-  u = ((u % 16) + 16) % 16;
-  if (u > 8) u -= 16;   // (-8, 8]
-  if (u > 4 || u < -4) {
+__device__ __forceinline__ void rot48(float2 &v, int u) {
+  u = ((u % 48) + 48) % 48;
+  if (u > 24) u -= 48;   // (-24, 24]
+  if (u > 12 || u < -12) {
     v.x = -v.x;
     v.y = -v.y;
-    u += u > 0 ? -8 : 8;
+    u += u > 0 ? -24 : 24;
   }
   if (u == 0) return;
-  if (u == 4) {   // * i
+  if (u == 12) {   // * i
     const float x = v.x;
     v.x = -v.y;
     v.y = x;
     return;
   }
-  if (u == -4) {   // * -i
+  if (u == -12) {   // * -i
     const float x = v.x;
     v.x = v.y;
     v.y = -x;
@@ -572,20 +580,23 @@ __device__ __forceinline__ void rot_pi8(float2 &v, int u) {
   v.y = y;
 }
 
-// In-register DFT of N in {1, 2, 4, 8, 16} values in natural order; forward
-// exp(-2 pi i jk/N), inverse exp(+2 pi i jk/N), unnormalised.
+// In-register DFT of N values in natural order, N | 48 (products of 2, 3, 4);
+// forward exp(-2 pi i jk/N), inverse exp(+2 pi i jk/N), unnormalised.
+// N = P Q with P = 4 (or 3, 2): length-P DFTs over the stride-Q subsequences,
+// twiddles W_N^(q k1) as exact rotations, then length-Q DFTs.
 template <int N, bool INV> struct RegDFT {
   static __device__ __forceinline__ void run(float2 *v) {
-    static_assert(N == 8 || N == 16, "register DFT length");
-    constexpr int P = 4, Q = N / 4;
+    static_assert(48 % N == 0, "register DFT length divides 48");
+    constexpr int P = (N % 4 == 0) ? 4 : ((N % 3 == 0) ? 3 : 2);
+    constexpr int Q = N / P;
     float2 a[Q][P];
 #pragma unroll
     for (int q = 0; q < Q; q++) {
 #pragma unroll
       for (int p = 0; p < P; p++) a[q][p] = v[q + Q * p];
-      RegDFT<4, INV>::run(a[q]);
+      RegDFT<P, INV>::run(a[q]);
 #pragma unroll
-      for (int k1 = 1; k1 < P; k1++) rot_pi8(a[q][k1], (INV ? 16 : -16) * q * k1 / N);
+      for (int k1 = 1; k1 < P; k1++) rot48(a[q][k1], (INV ? 48 : -48) * q * k1 / N);
     }
 #pragma unroll
     for (int k1 = 0; k1 < P; k1++) {
@@ -606,6 +617,23 @@ template <bool INV> struct RegDFT<2, INV> {
     const float2 a = v[0], b = v[1];
     v[0] = make_float2(a.x + b.x, a.y + b.y);
     v[1] = make_float2(a.x - b.x, a.y - b.y);
+  }
+};
+template <bool INV> struct RegDFT<3, INV> {
+  // sqrt(3)/2 as an FP32 pair: h s is formed to ~2^-48, so the butterfly
+  // carries no fixed FP32 constant error (which would bias the norm)
+  static __device__ __forceinline__ void run(float2 *v) {
+    constexpr float H_HI = 0.8660253882408142f, H_LO = 1.5543625053737742e-08f;
+    const float2 t = make_float2(v[1].x + v[2].x, v[1].y + v[2].y);
+    const float2 d = make_float2(v[1].x - v[2].x, v[1].y - v[2].y);
+    const float2 x0 = v[0];
+    const float2 u = make_float2(fmaf(-0.5f, t.x, x0.x), fmaf(-0.5f, t.y, x0.y));
+    const float hx = fmaf(H_LO, d.x, H_HI * d.x), hy = fmaf(H_LO, d.y, H_HI * d.y);
+    // forward: w = -i h d ; inverse: +i h d
+    const float2 w = INV ? make_float2(-hy, hx) : make_float2(hy, -hx);
+    v[0] = make_float2(x0.x + t.x, x0.y + t.y);
+    v[1] = make_float2(u.x + w.x, u.y + w.y);
+    v[2] = make_float2(u.x - w.x, u.y - w.y);
   }
 };
 template <bool INV> struct RegDFT<4, INV> {
@@ -823,6 +851,7 @@ struct SepShape {
 };
 constexpr SepShape kSepShapes[] = {
     {256, 128, 16, 16, 8, 256},
+    {192, 96, 24, 8, 4, 96},
     {64, 32, 8, 8, 4, 128},
     {32, 16, 8, 4, 2, 32},
     {16, 8, 4, 4, 2, 32},
@@ -868,17 +897,19 @@ void sep_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, 
 void sep_dispatch_attr(int id) {
   switch (id) {
     case 0: sep_set_attr<16, 16, 8, 256>(); break;
-    case 1: sep_set_attr<8, 8, 4, 128>(); break;
-    case 2: sep_set_attr<8, 4, 2, 32>(); break;
-    case 3: sep_set_attr<4, 4, 2, 32>(); break;
+    case 1: sep_set_attr<24, 8, 4, 96>(); break;
+    case 2: sep_set_attr<8, 8, 4, 128>(); break;
+    case 3: sep_set_attr<8, 4, 2, 32>(); break;
+    case 4: sep_set_attr<4, 4, 2, 32>(); break;
   }
 }
 int sep_dispatch_cluster(int id) {
   switch (id) {
     case 0: return sep_cluster<16, 16, 8, 256>();
-    case 1: return sep_cluster<8, 8, 4, 128>();
-    case 2: return sep_cluster<8, 4, 2, 32>();
-    case 3: return sep_cluster<4, 4, 2, 32>();
+    case 1: return sep_cluster<24, 8, 4, 96>();
+    case 2: return sep_cluster<8, 8, 4, 128>();
+    case 3: return sep_cluster<8, 4, 2, 32>();
+    case 4: return sep_cluster<4, 4, 2, 32>();
   }
   return 0;
 }
@@ -887,9 +918,10 @@ void sep_dispatch_launch(int id, cudaStream_t s, const Grid &g, const FFTPlan &p
                          float fscale, double scale, const int *status) {
   switch (id) {
     case 0: sep_launch<16, 16, 8, 256>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
-    case 1: sep_launch<8, 8, 4, 128>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
-    case 2: sep_launch<8, 4, 2, 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
-    case 3: sep_launch<4, 4, 2, 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+    case 1: sep_launch<24, 8, 4, 96>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+    case 2: sep_launch<8, 8, 4, 128>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+    case 3: sep_launch<8, 4, 2, 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+    case 4: sep_launch<4, 4, 2, 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
   }
 }
 }  // namespace

@@ -216,7 +216,8 @@ def test_mixed_precision_close_to_fp64(qd, oracle, gpu):
                                   dict(J=2, parity=0, n1=32, n2=16, n_theta=24, l_max=23),
                                   dict(J=3, parity=1, n1=24, n2=12, n_theta=40, l_max=37),
                                   dict(J=0, n1=64, n2=32, n_theta=8, l_max=7),
-                                  dict(J=1, parity=0, n1=256, n2=128, n_theta=8, l_max=7)])
+                                  dict(J=1, parity=0, n1=256, n2=128, n_theta=8, l_max=7),
+                                  dict(J=2, parity=0, n1=192, n2=96, n_theta=8, l_max=7)])
 def test_mixed_stages_match_oracle(qd, oracle, gpu, case):
     """tcgen05 BF16x3 Legendre contractions and the FP32 FFT: FP32-level agreement (rel <= 3e-6)."""
     cfg, d, dref = make(qd, **case)
@@ -262,3 +263,21 @@ def test_mixed_production_grid_tracks_fp64(qd, gpu):
     assert rel(a, b) < 1e-5
     ma, mb = out[1]["options"]["energies"][:, 0, 0], out[0]["options"]["energies"][:, 0, 0]
     assert np.max(np.abs(ma - mb)) < 1e-6
+
+
+def test_mixed_coupled_norm_tracks_fp64(qd, gpu):
+    """J=4 (five coupled Omega blocks) on a 64x32x24 grid: 400 steps of the mixed form, whose
+    Coriolis step runs in FP32, keep the module within 2e-6 of the FP64 form at every step
+    (no systematic drift) and the wave packet within 1e-4."""
+    cfg = qd.inputs.small_config(J=4, parity=0, n1=64, n2=32, n_theta=24, l_max=23, steps=400, n_energies=16)
+    out = {}
+    for prec in (0, 1):
+        d = qd.inputs.build_fh2data(cfg)
+        d["options"]["precision"] = prec
+        d["options"]["energies"] = np.zeros((cfg.total_steps, len(np.ravel(d["OmegaStates"]["omegas"])), 6))
+        qd.cudaOpenMPEvolution(d)
+        out[prec] = d
+    m1 = out[1]["options"]["energies"][:, :, 0].sum(axis=1)
+    m0 = out[0]["options"]["energies"][:, :, 0].sum(axis=1)
+    assert np.max(np.abs(m1 - m0)) < 2e-6
+    assert rel(out[1]["OmegaStates"]["wave_packets"], out[0]["OmegaStates"]["wave_packets"]) < 1e-4
