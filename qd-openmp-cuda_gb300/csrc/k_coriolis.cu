@@ -70,7 +70,7 @@ __device__ inline void lift2c(float2 &v, float2 ts) {
 }  // namespace
 
 template <int MAXN, bool EN>
-__global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__restrict__ psi_j,
+__device__ __forceinline__ void coriolis_f32_body(const Grid &g, float2 *__restrict__ psi_j,
                                                               const BlockDesc *__restrict__ blocks,
                                                               const CoriolisGroup *__restrict__ groups,
                                                               const float *__restrict__ Vh, const float *__restrict__ Vl,
@@ -79,12 +79,9 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__
                                                               int pro, int epi, const float *__restrict__ I1f,
                                                               const float *__restrict__ I2f, double *__restrict__ ce_part,
                                                               double *__restrict__ re_part, int tiles, int ce_n,
-                                                              const int *status) {
-  if (status && *status) return;
-  __shared__ float sVh[MAXN * MAXN], sVl[MAXN * MAXN];
-  __shared__ float Hd[MAXN], Ho[MAXN];
-  __shared__ float red[COR_THREADS / 32][2 * MAXN];
-  const CoriolisGroup gr = groups[blockIdx.y];
+                                                              int gid, float *sVh, float *sVl, float *Hd, float *Ho,
+                                                              float (*red)[2 * CORIOLIS_F32_MAXN], int64_t *base) {
+  const CoriolisGroup gr = groups[gid];
   const int n = gr.n, l = gr.l;
   // row stride MAXN: every (o, a) offset below is a compile-time constant
   for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
@@ -95,8 +92,7 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__
     Hd[q] = (float)Hp[gr.h0 + q * n + q];
     Ho[q] = q + 1 < n ? (float)Hp[gr.h0 + q * n + q + 1] : 0.0f;
   }
-  __shared__ int64_t base[MAXN];   // slab offset of each member block
-  for (int o = threadIdx.x; o < n; o += blockDim.x) {
+  for (int o = threadIdx.x; o < n; o += blockDim.x) {   // slab offset of each member block
     const BlockDesc bd = blocks[gr.block_lo + o];
     base[o] = (int64_t)(bd.slab0 + (l - bd.omega)) * g.npt;
   }
@@ -198,7 +194,7 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__
       }
       if (lane == 0) {
         red[warp][o] = c;
-        red[warp][MAXN + o] = r;
+        red[warp][CORIOLIS_F32_MAXN + o] = r;
       }
     }
   }
@@ -207,9 +203,9 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__
     double c = 0.0, r = 0.0;
     for (int w = 0; w < COR_THREADS / 32; w++) {
       c += (double)red[w][o];
-      r += (double)red[w][MAXN + o];
+      r += (double)red[w][CORIOLIS_F32_MAXN + o];
     }
-    if (ce_part) ce_part[((int64_t)blockIdx.y * ce_n + o) * tiles + blockIdx.x] = c;
+    if (ce_part) ce_part[((int64_t)gid * ce_n + o) * tiles + blockIdx.x] = c;
     if (re_part) {
       const BlockDesc bd = blocks[gr.block_lo + o];
       re_part[(int64_t)(bd.slab0 + (l - bd.omega)) * tiles + blockIdx.x] = r;
@@ -217,31 +213,73 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__
   }
 }
 
+int coriolis_f32_class(int n) {
+  for (int c = 0; c < CORIOLIS_F32_CLASSES; c++)
+    if (n <= 4 * (c + 1)) return c;
+  return -1;
+}
+
+// One launch for every group: each CTA runs the body compiled for its
+// group's size class (at most 4, 8, ..., 4 (MAXC+1) blocks), so small groups
+// do not pay for the largest one's unrolled loops.
+template <int MAXC, bool EN>
+__global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__restrict__ psi_j,
+                                                              const BlockDesc *__restrict__ blocks,
+                                                              const CoriolisGroup *__restrict__ groups,
+                                                              const float *__restrict__ Vh, const float *__restrict__ Vl,
+                                                              const float2 *__restrict__ phl, const double *__restrict__ Hp,
+                                                              const float2 *__restrict__ rotR, const float2 *__restrict__ rotr,
+                                                              int pro, int epi, const float *__restrict__ I1f,
+                                                              const float *__restrict__ I2f, double *__restrict__ ce_part,
+                                                              double *__restrict__ re_part, int tiles, int ce_n,
+                                                              const int *__restrict__ order, const int *status) {
+  if (status && *status) return;
+  constexpr int MAXN = 4 * (MAXC + 1);
+  __shared__ float sVh[MAXN * MAXN], sVl[MAXN * MAXN];
+  __shared__ float Hd[MAXN], Ho[MAXN];
+  __shared__ float red[COR_THREADS / 32][2 * CORIOLIS_F32_MAXN];
+  __shared__ int64_t base[MAXN];
+  const int gid = order[blockIdx.y];
+  const int cls = (groups[gid].n + 3) / 4 - 1;
+#define QD_BODY(C)                                                                                                \
+  coriolis_f32_body<4 * ((C) + 1), EN>(g, psi_j, blocks, groups, Vh, Vl, phl, Hp, rotR, rotr, pro, epi, I1f, I2f, \
+                                        ce_part, re_part, tiles, ce_n, gid, sVh, sVl, Hd, Ho, red, base)
+  if (MAXC >= 5 && cls == 5) QD_BODY(MAXC >= 5 ? 5 : 0);
+  else if (MAXC >= 4 && cls == 4) QD_BODY(MAXC >= 4 ? 4 : 0);
+  else if (MAXC >= 3 && cls == 3) QD_BODY(MAXC >= 3 ? 3 : 0);
+  else if (MAXC >= 2 && cls == 2) QD_BODY(MAXC >= 2 ? 2 : 0);
+  else if (MAXC >= 1 && cls == 1) QD_BODY(MAXC >= 1 ? 1 : 0);
+  else QD_BODY(0);
+#undef QD_BODY
+}
+
 void launch_coriolis_f32(cudaStream_t s, const Grid &g, float2 *psi_j, const BlockDesc *blocks,
-                         const CoriolisGroup *groups, int n_groups, int max_n, const float *Vh, const float *Vl,
-                         const float2 *phl, const double *H, const float2 *rotR, const float2 *rotr, bool pro,
-                         bool epi, const float *I1f, const float *I2f, double *ce_part, double *re_part, int tiles,
-                         const int *status) {
+                         const CoriolisGroup *groups, const int *order, int n_groups, int max_n, const float *Vh,
+                         const float *Vl, const float2 *phl, const double *H, const float2 *rotR, const float2 *rotr,
+                         bool pro, bool epi, const float *I1f, const float *I2f, double *ce_part, double *re_part,
+                         int tiles, const int *status) {
   if (n_groups == 0) return;
-  dim3 grid((unsigned)tiles, (unsigned)n_groups);
-#define QD_COR32(M)                                                                                          \
-  do {                                                                                                       \
-    if (ce_part)                                                                                             \
-      k_coriolis_f32<M, true><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H, rotR, rotr, \
-                                                           pro ? 1 : 0, epi ? 1 : 0, I1f, I2f, ce_part, re_part, \
-                                                           tiles, max_n, status);                             \
-    else                                                                                                     \
-      k_coriolis_f32<M, false><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H, rotR,     \
-                                                            rotr, pro ? 1 : 0, epi ? 1 : 0, I1f, I2f, nullptr,   \
-                                                            nullptr, tiles, max_n, status);                  \
+  const dim3 grid((unsigned)tiles, (unsigned)n_groups);
+#define QD_COR32(C)                                                                                              \
+  do {                                                                                                           \
+    if (ce_part)                                                                                                 \
+      k_coriolis_f32<C, true><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H, rotR, rotr,    \
+                                                           pro ? 1 : 0, epi ? 1 : 0, I1f, I2f, ce_part, re_part,    \
+                                                           tiles, max_n, order, status);                          \
+    else                                                                                                         \
+      k_coriolis_f32<C, false><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H, rotR, rotr,   \
+                                                            pro ? 1 : 0, epi ? 1 : 0, I1f, I2f, nullptr, nullptr,   \
+                                                            tiles, max_n, order, status);                        \
   } while (0)
-  if (max_n <= 4) QD_COR32(4);
-  else if (max_n <= 8) QD_COR32(8);
-  else if (max_n <= 12) QD_COR32(12);
-  else if (max_n <= 16) QD_COR32(16);
-  else if (max_n <= 20) QD_COR32(20);
-  else if (max_n <= CORIOLIS_F32_MAXN) QD_COR32(24);
-  else throw Error{QD_ERR_UNSUPPORTED, "FP32 Coriolis: more than 24 coupled Omega blocks"};
+  switch (coriolis_f32_class(max_n)) {
+    case 0: QD_COR32(0); break;
+    case 1: QD_COR32(1); break;
+    case 2: QD_COR32(2); break;
+    case 3: QD_COR32(3); break;
+    case 4: QD_COR32(4); break;
+    case 5: QD_COR32(5); break;
+    default: throw Error{QD_ERR_UNSUPPORTED, "FP32 Coriolis: more than 24 coupled Omega blocks"};
+  }
 #undef QD_COR32
 }
 

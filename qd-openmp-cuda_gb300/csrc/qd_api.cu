@@ -277,6 +277,7 @@ struct qd_session {
   bool cor_f32 = false;
   float *cor_Vh = nullptr, *cor_Vl = nullptr;
   float2 *cor_phl = nullptr;
+  int *cor_order = nullptr;   // group indices, largest groups first
   std::vector<int> h_pgroup0;
   int *d_pgroup0 = nullptr;
   // energies
@@ -394,7 +395,7 @@ __global__ void k_flux_reset(int *count) { *count = 0; }
 qd_session::~qd_session() {
   if (graph_chunk) cudaGraphExecDestroy(graph_chunk);
   void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, psi_thf, psi_jf, xfer, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
-                  tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, cor_Vh, cor_Vl, cor_phl,
+                  tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, cor_Vh, cor_Vl, cor_phl, cor_order,
                   d_pgroup0,
                   part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
                   flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
@@ -461,7 +462,8 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
                          first ? s->vph0 : s->vph, s->d1f, s->d2f, s->smem_f, s->status, s->status, s->bscale_f, s->max_nl);
   prof_mark(st, "legendre_forward");
   if (s->cor_f32) {
-    launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_Vh,
+    launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->cor_order, s->n_groups,
+                        s->max_group_n, s->cor_Vh,
                         s->cor_Vl, s->cor_phl, s->cor_H, s->lrotR, s->lrotr, true, true, s->I1f, s->I2f, nullptr,
                         nullptr, s->t_ce, s->status);
     prof_mark(st, "coriolis");
@@ -485,7 +487,8 @@ static void enqueue_step_mixed(qd_session *s, bool first) {
                      s->any_coupled ? nullptr : s->part_re, s->status, &lf);
   if (s->cor_f32) {
     // coupling energy of the incoming state, rotational energy of the outgoing one
-    launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_Vh,
+    launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->cor_order, s->n_groups,
+                        s->max_group_n, s->cor_Vh,
                         s->cor_Vl, s->cor_phl, s->cor_H, s->lrotR, s->lrotr, false, true, s->I1f, s->I2f,
                         s->part_ce, s->part_re, s->t_ce, s->status);
     prof_mark(st, "coriolis_energy");
@@ -866,6 +869,11 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
       s->cor_Vl = dupload(vl.data(), vl.size(), st);
       s->cor_phl = dalloc<float2>((size_t)ph0);
       launch_build_coriolis_lift(st, g, s->d_groups, s->n_groups, s->cor_e, 0.5 * s->dt, s->cor_phl);
+      std::vector<int> order;
+      for (int c = CORIOLIS_F32_CLASSES - 1; c >= 0; c--)
+        for (int gi = 0; gi < s->n_groups; gi++)
+          if (coriolis_f32_class(s->h_groups[gi].n) == c) order.push_back(gi);
+      s->cor_order = dupload(order.data(), order.size(), st);
       s->cor_f32 = true;
     }
   }
@@ -1264,7 +1272,8 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         if (s->cor_f32) {
           phl = dalloc<float2>((size_t)s->h_groups.back().ph0 + (size_t)s->h_groups.back().n * g.n1);
           launch_build_coriolis_lift(st, g, s->d_groups, s->n_groups, s->cor_e, dt, phl);
-          launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->n_groups, s->max_group_n, s->cor_Vh,
+          launch_coriolis_f32(st, g, s->psi_jf, s->d_blocks, s->d_groups, s->cor_order, s->n_groups,
+                        s->max_group_n, s->cor_Vh,
                               s->cor_Vl, phl, s->cor_H, nullptr, nullptr, false, false, s->I1f, s->I2f,
                               en ? s->part_ce : nullptr, nullptr, s->t_ce, s->status);
         } else if (s->psi_jf)

@@ -175,12 +175,15 @@ int coriolis_tiles(const Grid &g);
 // [group][omega][tiles] and rotational-energy partials [slab][tiles] of the
 // outgoing state.
 constexpr int CORIOLIS_F32_MAXN = 24;
+constexpr int CORIOLIS_F32_CLASSES = 6;  // size classes of at most 4, 8, ..., 24 blocks (one body each)
 constexpr int CORIOLIS_F32_TILES = 16;   // CTAs per group (its partial tiles)
+int coriolis_f32_class(int n);           // size class of a group of n blocks, -1 above the limit
+// order: the group indices, largest groups first
 void launch_coriolis_f32(cudaStream_t s, const Grid &g, float2 *psi_j, const BlockDesc *blocks,
-                         const CoriolisGroup *groups, int n_groups, int max_n, const float *Vh, const float *Vl,
-                         const float2 *phl, const double *H, const float2 *rotR, const float2 *rotr, bool pro,
-                         bool epi, const float *I1f, const float *I2f, double *ce_part, double *re_part, int tiles,
-                         const int *status);
+                         const CoriolisGroup *groups, const int *order, int n_groups, int max_n, const float *Vh,
+                         const float *Vl, const float2 *phl, const double *H, const float2 *rotR, const float2 *rotr,
+                         bool pro, bool epi, const float *I1f, const float *I2f, double *ce_part, double *re_part,
+                         int tiles, const int *status);
 void launch_build_coriolis_lift(cudaStream_t s, const Grid &g, const CoriolisGroup *groups, int n_groups,
                                 const double *e, double dt, float2 *phl);
 
