@@ -44,6 +44,29 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(ms: float) -> float:
+    """Slowest rank's timed region (ms): every rank returns the same value.  The
+    tensor lives where the process group's backend works (CUDA for NCCL, host
+    memory for gloo)."""
+    import torch
+
+    if not torch.distributed.is_initialized():
+        return ms
+    dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(ms: float, steps: int, blocks_per_replica: int) -> float:
+    """Whole-job Omega-block steps/s of independent replicas: the units all ranks
+    processed over the slowest rank's time."""
+    import torch
+
+    world = torch.distributed.get_world_size() if torch.distributed.is_initialized() else 1
+    return world * steps * blocks_per_replica / (max_over_ranks(ms) / 1e3)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
 
@@ -173,10 +196,7 @@ def run_form(qd, precision: int, steps: int, warmup: int, sampler=None):
             clocks = None
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-        if torch.distributed.is_initialized():
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms)
         prof = s.profile(64)
         psi = s.get_psi("theta", 0)
         return {"ms": ms, "n_blocks": s.n_blocks, "launches_per_step": s.launches_per_step, "profile": prof,
@@ -390,8 +410,8 @@ def main():
     mixed = run_form(qd, 1, args.steps, args.warmup, ClockSampler(gpu_index))
     fp64 = run_form(qd, 0, args.steps, args.warmup)
     nb = mixed["n_blocks"]
-    value = world * args.steps * nb / (mixed["ms"] / 1e3)
-    fp64_value = world * args.steps * nb / (fp64["ms"] / 1e3)
+    value = replica_throughput(mixed["ms"], args.steps, nb)
+    fp64_value = replica_throughput(fp64["ms"], args.steps, nb)
     # same number of steps from the same state: accuracy of the mixed form
     steps_done = args.warmup + args.steps + 64
     dpsi = float(np.linalg.norm(mixed["psi"] - fp64["psi"]) / np.linalg.norm(fp64["psi"]))
