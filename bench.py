@@ -111,7 +111,7 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def algorithmic(kernel: str, d: dict, flux_chunk: int = 32):
+def algorithmic(kernel: str, d: dict, flux_chunk: int = 64):
     """Algorithmic flops or bytes of one launch of ``kernel`` on FH2Data ``d``:
     returns (bound, amount, unit_of_rate)."""
     n1, n2, nth = int(d["r1"]["n"]), int(d["r2"]["n"]), int(d["theta"]["n"])
@@ -126,14 +126,15 @@ def algorithmic(kernel: str, d: dict, flux_chunk: int = 32):
         if prec == 0:
             return "fp64", flops, "TFLOP/s"
         # BF16x3 on tensor cores: 6 products per real multiply-add keep the
-        # tensor pipe far below its peak at K <= 96; HBM bounds the kernel
-        if kernel == "legendre_forward":   # psi_theta + V shears in, psi_j out
-            byts = sum(16.0 * npt * nth + 8.0 * npt * nth + 16.0 * npt * nl for nl in nls)
+        # tensor pipe far below its peak at K <= 96; HBM bounds the kernel.
+        # The mixed form stores both pools as c64 (8 B per complex value).
+        if kernel == "legendre_forward":   # psi_theta + V shears (float2) in, psi_j out
+            byts = sum(8.0 * npt * nth + 8.0 * npt * nth + 8.0 * npt * nl for nl in nls)
         else:                              # psi_j in, psi_theta out, w V (FP32) in
-            byts = sum(16.0 * npt * nl + 16.0 * npt * nth + 4.0 * npt * nth for nl in nls)
+            byts = sum(8.0 * npt * nl + 8.0 * npt * nth + 4.0 * npt * nth for nl in nls)
         return "hbm", byts, "GB/s"
-    if kernel == "fft_slab":   # one read and one write of every c128 point of every slab
-        return "hbm", 32.0 * npt * snl, "GB/s"
+    if kernel == "fft_slab":   # one read and one write of every c64 point of every slab
+        return "hbm", 16.0 * npt * snl, "GB/s"
     if kernel == "fft_rows_forward" or kernel == "fft_cols_kinetic":
         return "hbm", 32.0 * npt * snl, "GB/s"
     if kernel == "fft_rows_inverse":
@@ -439,7 +440,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "c128 storage; bf16x3-split Legendre GEMM / fp32 FFT; fp64 phases, norms, flux",
+        "dtype": "c64 state (c128 at the API); bf16x3-split Legendre GEMM / fp32 FFT, Coriolis; fp64 tables, norms, flux",
         "data": "synthetic (LEPS F+H2, deterministic inputs built on the host)",
         "config": {"workload": WORKLOAD, "grid": [256, 128, 96], "l_max": 95, "J": 0, "omega_blocks": nb,
                    "dt": 10.0, "n_energies": 400, "flux": True, "parallelism": f"replicas x{world}",
@@ -453,7 +454,7 @@ def main():
                      "unit": unit, "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_per_launch": amount},
         "kernels": kernels,
-        "gpu_launches": mixed["launches_per_step"] * args.steps + 3 * (args.steps // 32),
+        "gpu_launches": mixed["launches_per_step"] * args.steps + 3 * (args.steps // 64),
         "clocks": mixed["clocks"],
         "measured_fma_tflops": {"fp64": fp64_peak, "fp32": fp32_peak},
     }

@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(256) k_energy_finalize(Grid g, EnergyParts ep,
                                   int *__restrict__ d_step, int rec_base, int rec_cap, int n_blocks, double norm_tol,
                                   int *status, int *status_step, StepTail tail, unsigned *done) {
   constexpr int NW = 256 / 32;
-  __shared__ double red[NW][5];
+  __shared__ double red[NW][2];
   __shared__ bool last;
   const int b = blockIdx.x, tid = threadIdx.x;
   // everything this launch reads is loaded up front: one round trip
@@ -346,27 +346,30 @@ __global__ void __launch_bounds__(256) k_energy_finalize(Grid g, EnergyParts ep,
       if (o >= 0 && o < groups[gi].n) acc[4] += ep.ce[((int64_t)gi * ce_n + o) * ep.ce_tiles + tt];
     }
   }
-  // fixed-order reduction: shuffle tree per warp, then the warps in order
-  for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-    for (int q = 0; q < 5; q++) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
-  if ((tid & 31) == 0)
-#pragma unroll
-    for (int q = 0; q < 5; q++) red[tid >> 5][q] = acc[q];
+  // fixed-order reduction: each warp reduces only its own quantity (the
+  // module/potential pair for the first pair of warps, one sum for the others),
+  // then thread 0 adds the two warps of each quantity
+  double v0 = wq == 0 ? acc[0] : acc[1 + wq], v1 = acc[1];
+  for (int o = 16; o > 0; o >>= 1) {
+    v0 += __shfl_down_sync(0xffffffffu, v0, o);
+    if (wq == 0) v1 += __shfl_down_sync(0xffffffffu, v1, o);
+  }
+  if ((tid & 31) == 0) {
+    red[tid >> 5][0] = v0;
+    red[tid >> 5][1] = v1;
+  }
   __syncthreads();
   if (st0) return;   // set before this launch: nothing is written, the counter is untouched
   double mod = 0.0;
   if (tid == 0) {
-    double tot[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int w = 0; w < NW; w++)
-#pragma unroll
-      for (int q = 0; q < 5; q++) tot[q] += red[w][q];
+    const double tot[5] = {red[0][0] + red[1][0], red[0][1] + red[1][1], red[2][0] + red[3][0],
+                           red[4][0] + red[5][0], red[6][0] + red[7][0]};
     const double dV = g.dr1 * g.dr2;
     double *e = energies + b * 6;
     double ev[6];
     ev[E_MODULE] = ep.have_mod ? tot[0] * dV : e[E_MODULE];
     ev[E_POTENTIAL] = ep.have_mod ? tot[1] * dV : e[E_POTENTIAL];
-    ev[E_KINETIC] = ep.have_ke ? tot[2] * dV / ((double)g.n1 * g.n2) : e[E_KINETIC];
+    ev[E_KINETIC] = ep.have_ke ? tot[2] * ep.ke_scale : e[E_KINETIC];
     ev[E_ROTATIONAL] = ep.have_re ? tot[3] * dV : e[E_ROTATIONAL];
     ev[E_CORIOLIS] = ep.have_ce ? tot[4] * dV : e[E_CORIOLIS];
     ev[E_TOTAL] = ev[E_POTENTIAL] + ev[E_KINETIC] + ev[E_ROTATIONAL] + ev[E_CORIOLIS];

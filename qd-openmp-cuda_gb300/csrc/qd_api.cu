@@ -448,6 +448,7 @@ static EnergyParts energy_parts(qd_session *s, bool mod, bool ke, bool re, bool 
   ep.have_ke = ke;
   ep.have_re = re;
   ep.have_ce = ce;
+  ep.ke_scale = s->g.dr1 * s->g.dr2 / ((double)s->g.n1 * s->g.n2);
   return ep;
 }
 
@@ -908,7 +909,7 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     s->flux.n_energies = c.n_energies;
     s->flux.n_grad = c.n_gradient_points;
     s->flux.n_ds = c.n_dividing_surface;
-    s->flux.chunk = 32;
+    s->flux.chunk = 64;   // steps per flux DFT flush (and per CUDA graph)
     const int64_t ns = (int64_t)g.nth * g.n1;
     s->flux_buf = dalloc<double2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
     s->flux_acc = dalloc<double2>((size_t)s->n_blocks * 2 * c.n_energies * ns);
@@ -997,7 +998,8 @@ static void run_steps(qd_session *s, int n) {
       enqueue_step(s, true);
       s->steps++;
       n--;
-      if (s->flux.enabled && ++s->flux_pending == s->flux.chunk) flush_flux(s);
+      // flush step 0's surface values at once, so that later steps align with whole graph chunks
+      if (s->flux.enabled && ++s->flux_pending > 0) flush_flux(s);
       continue;
     }
     if (n >= chunk && s->flux_pending == 0) {

@@ -195,6 +195,7 @@ struct EnergyParts {
   const double *re;      int re_tiles;        // [slab][tiles]
   const double *ce;      int ce_tiles;        // [b][tiles]
   int have_ke, have_re, have_ce, have_mod;
+  double ke_scale;   // dr1 dr2 / (n1 n2): kinetic partials are sums over the unnormalised spectrum
 };
 // End-of-step bookkeeping done by the last CTA of the energy finalisation:
 // flux slot and t0 of this step (when flux_count is set) and the step counter.
