@@ -270,6 +270,11 @@ __device__ inline TcTile tc_tile(const TcArgs &P, int tt, int mtiles) {
 }
 
 constexpr int WS_THREADS = 512;      // 8 producer warps + 8 consumer warps
+// FP32 staging of one A tile, k-major: element (k, point pl, re/im c) at
+// k * TC_LDM + pl + TC_IM * c.  With TC_LDM = 2 (mod 32) and TC_IM = 8 (mod 32)
+// the loader's stores (32 consecutive points) and the slicer's loads (8
+// points x re/im x two k-groups 8 apart) fall in 32 distinct banks.
+constexpr int TC_LDM = 162, TC_IM = 72;
 constexpr int WS_PROD = 256;
 
 template <bool FWD>
@@ -289,7 +294,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   unsigned char *sA = smem;
   unsigned char *sB = smem + 3 * a_term_max;
   float *sF = reinterpret_cast<float *>(sB + 3 * b_term_max);
-  float *sWV = sF + 128 * (kp_max + 1);   // backward: w V of the tile, [n][64 points]
+  float *sWV = sF + kp_max * TC_LDM;   // backward: w V of the tile, [n][64 points]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t ncols = 512;
   const int t_begin = (int)((int64_t)blockIdx.x * n_tiles / gridDim.x);
@@ -317,7 +322,6 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       const TcTile T = tc_tile<FWD>(P, tt, mtiles);
       const BlockDesc bd = P.blocks[T.b];
       const int64_t p0 = (int64_t)T.mt * TC_POINTS;
-      const int LDF = T.Kp + 1;
       const float2 *A = P.A + (FWD ? (int64_t)T.b * g.nth * g.npt : (int64_t)bd.slab0 * g.npt);
       // L2 prefetch of the next tile (128-byte lines of its k rows)
       if (tt + 1 < t_end) {
@@ -364,8 +368,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
               y *= msk;
               if (P.vph) rot_lift2(x, y, ts[u]);
             }
-            sF[(2 * pl) * LDF + k] = x;
-            sF[(2 * pl + 1) * LDF + k] = y;
+            sF[k * TC_LDM + pl] = x;
+            sF[k * TC_LDM + TC_IM + pl] = y;
           }
         }
       }
@@ -385,13 +389,16 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         for (int q = tid; q < n16; q += WS_PROD) dst[q] = __ldg(src + q);
         cur_b = T.b;
       }
-      // phase 2: threads 2m and 2m+1 scale row m and slice one half of its k groups each
+      // phase 2: lanes l and l+16 of warp w scale row m = 16 w + l and slice the even and
+      // the odd k groups; each group of 8 lanes then writes 128 contiguous image bytes
       {
-        const int m = tid >> 1, half = tid & 1;
-        const float *row = sF + m * LDF;
+        const int m = 16 * warp + (lane & 15), half = lane >> 4;
+        const float *row = sF + (m >> 1) + TC_IM * (m & 1);   // element k at row[k * TC_LDM]
         float mx = 0.0f;
-        for (int k = half; k < T.Kp; k += 2) mx = fmaxf(mx, fabsf(row[k]));
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+        for (int kg = half; kg < T.Kp / 8; kg += 2)
+#pragma unroll
+          for (int e8 = 0; e8 < 8; e8++) mx = fmaxf(mx, fabsf(row[(kg * 8 + e8) * TC_LDM]));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
         // mx = f 2^e, f in [0.5, 1): row scale 2^e, slices of a = 256 x / 2^e
         const int e = mx >= 1e-30f ? (int)((__float_as_uint(mx) >> 23) & 0xffu) - 126 : 0;
         const float inv = mx >= 1e-30f ? __uint_as_float((uint32_t)(127 + 8 - e) << 23) : 0.0f;
@@ -406,7 +413,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
             uint32_t b[3][2];
 #pragma unroll
             for (int h = 0; h < 2; h++) {
-              const float a = __fmul_rn(row[kg * 8 + 2 * e2 + h], inv);
+              const float a = __fmul_rn(row[(kg * 8 + 2 * e2 + h) * TC_LDM], inv);
               const float i0 = rne(a);
               const float r1 = __fmul_rn(__fsub_rn(a, i0), 256.0f);
               const float i1 = rne(r1);
@@ -572,7 +579,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
 // that one CTA (holding all 512 TMEM columns) runs per SM.
 size_t tc_ws_smem_bytes(bool fwd, int kp_max, int np_max) {
   const size_t need = (size_t)3 * 16 * (kp_max / 8 * 128) + (size_t)tc_bimg_bytes(np_max, kp_max) +
-                      (size_t)128 * (kp_max + 1) * 4 + (fwd ? 0 : (size_t)np_max * TC_POINTS * 4);
+                      (size_t)kp_max * TC_LDM * 4 + (fwd ? 0 : (size_t)np_max * TC_POINTS * 4);
   return std::max(need, (size_t)120 * 1024);
 }
 
