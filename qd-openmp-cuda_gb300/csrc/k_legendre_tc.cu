@@ -275,6 +275,9 @@ constexpr int WS_THREADS = 512;      // 8 producer warps + 8 consumer warps
 // the loader's stores (32 consecutive points) and the slicer's loads (8
 // points x re/im x two k-groups 8 apart) fall in 32 distinct banks.
 constexpr int TC_LDM = 162, TC_IM = 72;
+// consumer thread that issues the MMA chain: not thread 0, which forms the
+// backward kernel's per-tile module/potential sums after each epilogue
+constexpr int MMA_ISSUER = 32;
 constexpr int WS_PROD = 256;
 
 template <bool FWD>
@@ -447,22 +450,25 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       const TcTile T = tc_tile<FWD>(P, tt, mtiles);
       const BlockDesc bd = P.blocks[T.b];
       const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
-      // backward: the w V values of this thread's columns, copied asynchronously
-      // into shared memory before the MMA wait (the re/im pair shares them: the
-      // even lane copies, both read after the warp synchronises)
-      if (!FWD && c == 0 && p < g.npt) {
-        for (int n0 = 16 * chalf; n0 < T.Nv; n0 += 32)
-#pragma unroll
-          for (int q = 0; q < 16; q++) {
-            const int n = n0 + q;
-            if (n < T.Nv)
-              asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(sWV + n * TC_POINTS + pl)),
-                           "l"(P.wv + (int64_t)n * g.npt + p)
-                           : "memory");
+      // backward: the tile's w V values [n][64 points], copied asynchronously into
+      // shared memory before the MMA wait, 16 bytes (4 points) per copy spread over
+      // all consumer threads (a 4-byte copy per point where the tile ends early)
+      if (!FWD) {
+        const int64_t p0 = (int64_t)T.mt * TC_POINTS;
+        for (int q = ctid; q < T.Nv * (TC_POINTS / 4); q += WS_THREADS - WS_PROD) {
+          const int n = q / (TC_POINTS / 4), c4 = 4 * (q % (TC_POINTS / 4));
+          const float *src = P.wv + (int64_t)n * g.npt + p0 + c4;
+          const uint32_t dst = smem_u32(sWV + n * TC_POINTS + c4);
+          if (p0 + c4 + 4 <= g.npt) {
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+          } else {
+            for (int e = 0; e < 4 && p0 + c4 + e < g.npt; e++)
+              asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst + 4 * e), "l"(src + e) : "memory");
           }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
       }
-      if (!FWD) asm volatile("cp.async.commit_group;" ::: "memory");
-      if (ctid == 0) {
+      if (ctid == MMA_ISSUER) {
         bool ok = mbar_wait_bounded(smem_u32(&mb_ready), (uint32_t)(it & 1));
         if (ok && it > 0) ok = mbar_wait_bounded(smem_u32(&mb_free), (uint32_t)((it - 1) & 1));
         if (!ok) {
@@ -472,14 +478,31 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
           tc_fence_after();
           const uint32_t idesc = make_idesc(128, T.Np);
           const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-          for (int s = 0; s < T.Kp / 16; s++) {
+          if (2 * T.Np <= 256) {
+            // B0 and B1 are adjacent in shared memory and D0, D1, D2 in TMEM, so
+            // A0 [B0 B1] -> [D0 D1] and A1 [B0 B1] -> [D1 D2] are single N = 2 Np
+            // MMAs: four per k step instead of six, same sums
+            const uint32_t idesc2 = make_idesc(128, 2 * T.Np);
+            for (int s = 0; s < T.Kp / 16; s++) {
+              const uint32_t acc = s > 0 ? 1u : 0u;
+              const uint64_t bd0 = make_desc(b0 + s * 256, 128, T.SBO);
+              mma_bf16(tmem, make_desc(a0 + s * 256, 128, T.SBO), bd0, idesc2, acc);
+              mma_bf16(tmem + (uint32_t)(2 * T.Np), make_desc(a0 + s * 256, 128, T.SBO),
+                       make_desc(b0 + 2 * T.B_TERM + s * 256, 128, T.SBO), idesc, acc);
+              mma_bf16(tmem + (uint32_t)T.Np, make_desc(a0 + T.A_TERM + s * 256, 128, T.SBO), bd0, idesc2, 1u);
+              mma_bf16(tmem + (uint32_t)(2 * T.Np), make_desc(a0 + 2 * T.A_TERM + s * 256, 128, T.SBO), bd0, idesc,
+                       1u);
+            }
+          } else {
+            for (int s = 0; s < T.Kp / 16; s++) {
 #pragma unroll
-            for (int q = 0; q < 6; q++) {
-              const int d = c_pair_a[q] + c_pair_b[q];
-              const uint64_t ad = make_desc(a0 + c_pair_a[q] * T.A_TERM + s * 256, 128, T.SBO);
-              const uint64_t bdsc = make_desc(b0 + c_pair_b[q] * T.B_TERM + s * 256, 128, T.SBO);
-              const bool first = s == 0 && (q == 0 || q == 1 || q == 3);
-              mma_bf16(tmem + (uint32_t)(d * T.Np), ad, bdsc, idesc, first ? 0u : 1u);
+              for (int q = 0; q < 6; q++) {
+                const int d = c_pair_a[q] + c_pair_b[q];
+                const uint64_t ad = make_desc(a0 + c_pair_a[q] * T.A_TERM + s * 256, 128, T.SBO);
+                const uint64_t bdsc = make_desc(b0 + c_pair_b[q] * T.B_TERM + s * 256, 128, T.SBO);
+                const bool first = s == 0 && (q == 0 || q == 1 || q == 3);
+                mma_bf16(tmem + (uint32_t)(d * T.Np), ad, bdsc, idesc, first ? 0u : 1u);
+              }
             }
           }
           mma_commit(smem_u32(&mb_done));
@@ -493,7 +516,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         tc_fence_before();
       }
       __syncwarp();
-      named_bar(2, WS_THREADS - WS_PROD);
+      if (!FWD) asm volatile("cp.async.wait_all;" ::: "memory");   // this thread's w V copies have landed
+      named_bar(2, WS_THREADS - WS_PROD);                          // ... and so have everyone's
       if (abort_c) break;
       if (T.b != cons_b) {
         for (int n = ctid; n < 256; n += WS_THREADS - WS_PROD) {
@@ -508,10 +532,6 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       float mod = 0.0f, pe = 0.0f;
       float *Cf = reinterpret_cast<float *>(P.C);
       const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
-      if (!FWD) {
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        __syncwarp();
-      }
       for (int n0 = 16 * chalf; n0 < T.Np; n0 += 32) {
         float d0[16], d1[16], d2[16];
         tmem_ld16(trow + (uint32_t)n0, d0);
@@ -537,7 +557,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       }
       tc_fence_before();
       mbar_arrive(smem_u32(&mb_free));
-      __syncwarp();   // both lanes of a re/im pair are done with the w V tile
+      __syncwarp();
       if (!FWD && P.part) {
         // fixed-order reduction over the 256 consumer threads
         for (int o = 16; o > 0; o >>= 1) {
@@ -548,23 +568,24 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
           red_s[cw] = mod;
           red_s[8 + cw] = pe;
         }
-        named_bar(2, WS_THREADS - WS_PROD);
-        if (ctid == 0) {
-          double ms = 0.0, ps = 0.0;
+        named_bar(2, WS_THREADS - WS_PROD);   // also: every consumer is done with the w V tile
+        if (ctid == 0) {   // red_s is next written after the next tile's MMA barrier
+          float ms = 0.0f, ps = 0.0f;
           for (int q = 0; q < 8; q++) {
             ms += red_s[q];
             ps += red_s[8 + q];
           }
-          P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 0] = ms;
-          P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 1] = ps;
+          P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 0] = (double)ms;
+          P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 1] = (double)ps;
         }
-        named_bar(2, WS_THREADS - WS_PROD);
+      } else if (!FWD) {
+        named_bar(2, WS_THREADS - WS_PROD);   // every consumer is done with the w V tile
       }
     }
   }
   // ---- drain: after a timeout, wait (bounded) for the last MMA chain issued
   __syncthreads();
-  if (tid == WS_PROD && (abort_p || abort_c) && n_issued > 0)
+  if (tid == WS_PROD + MMA_ISSUER && (abort_p || abort_c) && n_issued > 0)
     mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((n_issued - 1) & 1));
   tc_fence_before();
   __syncthreads();
