@@ -41,9 +41,12 @@ typedef enum qd_status {
 
 typedef enum qd_precision {
   QD_PRECISION_FP64 = 0,  /* every stage in FP64 */
-  QD_PRECISION_MIXED = 1  /* Legendre contraction as a 3-term BF16 split on tensor
-                             cores (FP32 accumulate), FFT butterflies in FP32;
-                             phases, norms, Coriolis and flux in FP64 */
+  QD_PRECISION_MIXED = 1  /* Legendre contraction as an exact 3-term BF16 split on
+                             tensor cores, FFT, phases and Coriolis in FP32 (phases
+                             as determinant-1 rotations), wave packets held as
+                             complex64 on the device; tables, norms, energies and
+                             flux accumulators in FP64.  Inputs and outputs stay
+                             complex128. */
 } qd_precision;
 
 /* r1 (R) and r2 (r): matlabStructures.C:17-23 */
