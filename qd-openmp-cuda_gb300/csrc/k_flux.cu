@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, i
                                                                        const float2 *__restrict__ psi_th,
                                                                        const float2 *__restrict__ hv,
                                                                        const float *__restrict__ fd,
-                                                                       double2 *__restrict__ buf, int n_blocks,
+                                                                       float2 *__restrict__ buf, int n_blocks,
                                                                        const int *slot_p, const int *status) {
   if (status && *status) return;
   __shared__ float2 sD[FLUX_GY][FLUX_GX];
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, i
   const int b = blockIdx.y;
   const int h = (n_grad - 1) / 2;
   const int64_t ns = (int64_t)g.nth * g.n1;
-  double2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
+  float2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
   const float2 *p = psi_th + (int64_t)b * g.nth * g.npt;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t q = (int64_t)blockIdx.x * FLUX_GX + tx;
@@ -121,14 +121,13 @@ __global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, i
       D.x += sD[y][tx].x;
       D.y += sD[y][tx].y;
     }
-    const float2 A = sA[tx];
-    out[q] = make_double2(f2d(A.x), f2d(A.y));
-    out[ns + q] = make_double2(f2d(D.x), f2d(D.y));
+    out[q] = sA[tx];
+    out[ns + q] = D;
   }
 }
 
 void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const float2 *psi_th, int n_blocks,
-                             const float2 *half_v, const float *fd, double2 *buf, const int *slot, const int *status) {
+                             const float2 *half_v, const float *fd, float2 *buf, const int *slot, const int *status) {
   if (f.n_grad > FLUX_GY * FLUX_GMAX)
     throw Error{QD_ERR_UNSUPPORTED, "mixed-form flux: more than 32 stencil points"};
   const int64_t ns = (int64_t)g.nth * g.n1;
@@ -259,11 +258,11 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_dev(int64_t ns2, int 
 // (phases computed in FP64 and rounded once, surface values converted with
 // integer instructions), each chunk's sum added into the FP64 accumulators.
 namespace {
-constexpr int FLUX_EB32 = 16;
+constexpr int FLUX_EB32 = 32;
 }
 
 __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_f32(int64_t ns2, int nE, int n_blocks, const int *count_p,
-                                                               int cap, const double2 *__restrict__ buf,
+                                                               int cap, const float2 *__restrict__ buf,
                                                                const double2 *__restrict__ phase,
                                                                double2 *__restrict__ acc, const int *status) {
   if (status && *status) return;
@@ -284,8 +283,8 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_f32(int64_t ns2, int 
 #pragma unroll
   for (int e = 0; e < FLUX_EB32; e++) a[e] = make_float2(0.0f, 0.0f);
   for (int n = 0; n < count; n++) {
-    const double2 vd = buf[((int64_t)n * n_blocks + b) * ns2 + s];
-    const float vx = d2f_rn(vd.x), vy = d2f_rn(vd.y);
+    const float2 vd = buf[((int64_t)n * n_blocks + b) * ns2 + s];
+    const float vx = vd.x, vy = vd.y;
 #pragma unroll
     for (int e = 0; e < FLUX_EB32; e++) {
       const float2 p = ph[n][e];
@@ -308,7 +307,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_f32(int64_t ns2, int 
 }
 
 void launch_flux_dft_f32(cudaStream_t s, int64_t ns2, int nE, int n_blocks, const int *count_p, int cap,
-                         const double2 *buf, const double2 *phase, double2 *acc, const int *status) {
+                         const float2 *buf, const double2 *phase, double2 *acc, const int *status) {
   dim3 grid((unsigned)((ns2 + FLUX_THREADS - 1) / FLUX_THREADS), (unsigned)((nE + FLUX_EB32 - 1) / FLUX_EB32),
             (unsigned)n_blocks);
   k_flux_dft_f32<<<grid, FLUX_THREADS, 0, s>>>(ns2, nE, n_blocks, count_p, cap, buf, phase, acc, status);

@@ -290,6 +290,7 @@ struct qd_session {
   // flux
   FluxConfig flux{};
   double2 *flux_buf = nullptr, *flux_acc = nullptr, *flux_phase = nullptr, *half_v = nullptr;
+  float2 *flux_buf_f = nullptr;   // mixed form: surface buffer in c64 (FP32 values)
   double *fd = nullptr, *flux_E = nullptr, *flux_eta = nullptr, *crp = nullptr, *flux_t0 = nullptr;
   int *flux_count = nullptr, *flux_slot = nullptr;
   unsigned *step_done = nullptr;
@@ -397,7 +398,7 @@ qd_session::~qd_session() {
   void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, psi_thf, psi_jf, xfer, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
                   tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, cor_Vh, cor_Vl, cor_phl, cor_order,
                   d_pgroup0,
-                  part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf,
+                  part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf, flux_buf_f,
                   flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
                   img_f, img_b, bscale_f, bscale_b, imgoff_f, imgoff_b, vph, vph0, lrotR, lrotr, lkinR, lkinr, wf, wvf, d1f, d2f,
                   T1f, T2f, I1f, I2f, step_done, half_v_lift, fdf};
@@ -422,7 +423,7 @@ static void enqueue_flux_dft(qd_session *s) {
   prof_mark(s->stream, "flux_phase");
   const int64_t ns2 = 2LL * s->g.nth * s->g.n1;
   if (s->precision == QD_PRECISION_MIXED) {
-    launch_flux_dft_f32(s->stream, ns2, nE, s->n_blocks, s->flux_count, cap, s->flux_buf, s->flux_phase,
+    launch_flux_dft_f32(s->stream, ns2, nE, s->n_blocks, s->flux_count, cap, s->flux_buf_f, s->flux_phase,
                         s->flux_acc, s->status);
   } else {
     dim3 grid((unsigned)((ns2 + 127) / 128), (unsigned)((nE + 7) / 8), (unsigned)s->n_blocks);
@@ -564,7 +565,7 @@ static void enqueue_tail(qd_session *s) {
   prof_mark(st, "energy_finalize");
   if (s->flux.enabled) {
     if (s->precision == QD_PRECISION_MIXED) {
-      launch_flux_extract_f32(st, g, s->flux, s->psi_thf, s->n_blocks, s->half_v_lift, s->fdf, s->flux_buf,
+      launch_flux_extract_f32(st, g, s->flux, s->psi_thf, s->n_blocks, s->half_v_lift, s->fdf, s->flux_buf_f,
                               s->flux_slot, s->status);
     } else {
       const int64_t ns = (int64_t)g.nth * g.n1;
@@ -911,7 +912,10 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     s->flux.n_ds = c.n_dividing_surface;
     s->flux.chunk = 64;   // steps per flux DFT flush (and per CUDA graph)
     const int64_t ns = (int64_t)g.nth * g.n1;
-    s->flux_buf = dalloc<double2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
+    if (s->precision == QD_PRECISION_MIXED)
+      s->flux_buf_f = dalloc<float2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
+    else
+      s->flux_buf = dalloc<double2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
     s->flux_acc = dalloc<double2>((size_t)s->n_blocks * 2 * c.n_energies * ns);
     s->flux_phase = dalloc<double2>((size_t)s->flux.chunk * c.n_energies);
     s->half_v = dalloc<double2>((size_t)g.nth * c.n_gradient_points * g.n1);
@@ -1347,8 +1351,8 @@ int qd_session_apply(qd_session *s, int32_t stage, double dt) {
         const int64_t ns = (int64_t)g.nth * g.n1;
         dim3 grid((unsigned)std::min<int64_t>((ns + 255) / 256, 64), (unsigned)s->n_blocks);
         if (s->psi_thf)
-          k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_thf, s->half_v, s->fd,
-                                                   s->flux_buf, s->n_blocks, s->flux_slot, s->status);
+          launch_flux_extract_f32(st, g, s->flux, s->psi_thf, s->n_blocks, s->half_v_lift, s->fdf, s->flux_buf_f,
+                                  s->flux_slot, s->status);
         else
           k_flux_extract_dev<<<grid, 256, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
                                                    s->flux_buf, s->n_blocks, s->flux_slot, s->status);

@@ -214,7 +214,7 @@ void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &
 void launch_build_half_v_lift(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
                               float2 *half_v);
 void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const float2 *psi_th,
-                             int n_blocks, const float2 *half_v, const float *fd, double2 *buf, const int *slot,
+                             int n_blocks, const float2 *half_v, const float *fd, float2 *buf, const int *slot,
                              const int *status);
 
 // flux: extract surface values (A, dA/dr) into buf[slot], then DFT chunks
@@ -225,7 +225,7 @@ void launch_flux_dft(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_b
                      int count, const double *energies, double t0, double dt, double2 *phase_scratch,
                      double2 *acc, const int *status);
 void launch_flux_dft_f32(cudaStream_t s, int64_t ns2, int nE, int n_blocks, const int *count_p, int cap,
-                         const double2 *buf, const double2 *phase, double2 *acc, const int *status);
+                         const float2 *buf, const double2 *phase, double2 *acc, const int *status);
 void launch_flux_crp(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_problems,
                      const int *block0_of_problem, const double2 *acc, const double *w, const double *eta_sq,
                      double *crp);
