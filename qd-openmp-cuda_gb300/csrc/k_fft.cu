@@ -822,7 +822,7 @@ __global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(float2 *__restrict_
     if (re_part) ref = fmaf(lls2 * (I1 + __ldg(lf.I2f + rr)), x * x + y * y, ref);
     __stcs(P + (int64_t)rr * N1 + R, fscale != 0.0f ? make_float2(x, y) : scaled_c64(x, y, 0.0f, scale));
   }
-  // partial sums: FP32 within a warp, FP64 across warps in a fixed order
+  // partial sums: FP32 within a warp and across warps, in a fixed order
   float kew = fmaf((float)N2, ke1, ke2 * (1.0f / (float)N1)), rew = ref;
   for (int o = 16; o > 0; o >>= 1) {
     kew += __shfl_down_sync(0xffffffffu, kew, o);
@@ -831,14 +831,14 @@ __global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(float2 *__restrict_
   float2 *red2 = reinterpret_cast<float2 *>(red);
   if ((tid & 31) == 0) red2[tid >> 5] = make_float2(kew, rew);
   __syncthreads();
-  if (tid == 0) {
-    double ke = 0.0, re = 0.0;
+  if (tid == 0) {   // FP32 over the warps (FP64 conversions would queue on the slow FP64 pipe)
+    float ke = 0.0f, re = 0.0f;
     for (int w = 0; w < THREADS / 32; w++) {
-      ke += (double)red2[w].x;
-      re += (double)red2[w].y;
+      ke += red2[w].x;
+      re += red2[w].y;
     }
-    if (ke_part) ke_part[(int64_t)sl * C + c] = ke;
-    if (re_part) re_part[(int64_t)sl * C + c] = re;
+    if (ke_part) ke_part[(int64_t)sl * C + c] = (double)ke;
+    if (re_part) re_part[(int64_t)sl * C + c] = (double)re;
   }
   // no CTA leaves while another may still read its rows
   asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");

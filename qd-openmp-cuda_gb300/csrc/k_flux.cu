@@ -14,6 +14,7 @@
 // [n_E x chunk] x [chunk x surface] product accumulated in FP64.
 #include "qd_internal.h"
 #include "qd_device.cuh"
+#include "qd_tail.cuh"
 
 namespace qd {
 
@@ -51,79 +52,13 @@ void launch_flux_extract(cudaStream_t s, const Grid &g, const FluxConfig &f, con
   k_flux_extract<<<grid, 256, 0, s>>>(g, f.n_grad, f.n_ds, psi_th, half_v, fd, buf, n_blocks, slot, status);
 }
 
-// Mixed form of the surface extraction: FP32 arithmetic on the FP64 state
-// (exp(-i V dt/2) as three-shear rotations, FP32 stencil weights), values
-// stored in FP64 for the FP64 accumulation.
-__device__ inline void lift2f(float &x, float &y, float2 ts) {
-  x = fmaf(ts.x, y, x);
-  y = fmaf(ts.y, x, y);
-  x = fmaf(ts.x, y, x);
-  x = fmaf(ts.x, y, x);
-  y = fmaf(ts.y, x, y);
-  x = fmaf(ts.x, y, x);
-}
-
-// One thread row y of FLUX_GY handles the stencil rows gg = y, y + FLUX_GY, ...
-// of FLUX_GX consecutive surface points (i fastest: coalesced loads); the
-// rows' partial derivatives are summed in a fixed order through shared memory.
-namespace {
-constexpr int FLUX_GX = 64, FLUX_GY = 4, FLUX_GMAX = 8;   // n_grad <= FLUX_GY * FLUX_GMAX
-}
-__global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(Grid g, int n_grad, int n_ds,
-                                                                       const float2 *__restrict__ psi_th,
-                                                                       const float2 *__restrict__ hv,
-                                                                       const float *__restrict__ fd,
-                                                                       float2 *__restrict__ buf, int n_blocks,
-                                                                       const int *slot_p, const int *status) {
+// Mixed form of the surface extraction (FP32 on the c64 pool; qd_tail.cuh).
+__global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(FluxTileArgs f, const int *slot_p,
+                                                                       const int *status) {
   if (status && *status) return;
   __shared__ float2 sD[FLUX_GY][FLUX_GX];
   __shared__ float2 sA[FLUX_GX];
-  const int slot = *slot_p;
-  const int b = blockIdx.y;
-  const int h = (n_grad - 1) / 2;
-  const int64_t ns = (int64_t)g.nth * g.n1;
-  float2 *out = buf + ((int64_t)slot * n_blocks + b) * 2 * ns;
-  const float2 *p = psi_th + (int64_t)b * g.nth * g.npt;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int64_t q = (int64_t)blockIdx.x * FLUX_GX + tx;
-  float Dx = 0.0f, Dy = 0.0f;
-  if (q < ns) {
-    const int i = (int)(q % g.n1), k = (int)(q / g.n1);
-    float2 a[FLUX_GMAX];
-    float2 ts[FLUX_GMAX];
-#pragma unroll
-    for (int u = 0; u < FLUX_GMAX; u++) {
-      const int gg = ty + FLUX_GY * u;
-      if (gg < n_grad) {
-        a[u] = p[((int64_t)k * g.n2 + (n_ds - h + gg)) * g.n1 + i];
-        ts[u] = __ldg(hv + ((int64_t)k * n_grad + gg) * g.n1 + i);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < FLUX_GMAX; u++) {
-      const int gg = ty + FLUX_GY * u;
-      if (gg < n_grad) {
-        float x = a[u].x, y = a[u].y;
-        lift2f(x, y, ts[u]);
-        const float c = __ldg(fd + gg);
-        Dx = fmaf(c, x, Dx);
-        Dy = fmaf(c, y, Dy);
-        if (gg == h) sA[tx] = make_float2(x, y);
-      }
-    }
-  }
-  sD[ty][tx] = make_float2(Dx, Dy);
-  __syncthreads();
-  if (ty == 0 && q < ns) {
-    float2 D = sD[0][tx];
-#pragma unroll
-    for (int y = 1; y < FLUX_GY; y++) {
-      D.x += sD[y][tx].x;
-      D.y += sD[y][tx].y;
-    }
-    out[q] = sA[tx];
-    out[ns + q] = D;
-  }
+  flux_extract_tile(f, *slot_p, blockIdx.y, blockIdx.x, threadIdx.y * FLUX_GX + threadIdx.x, sD, sA);
 }
 
 void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const float2 *psi_th, int n_blocks,
@@ -132,7 +67,7 @@ void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f,
     throw Error{QD_ERR_UNSUPPORTED, "mixed-form flux: more than 32 stencil points"};
   const int64_t ns = (int64_t)g.nth * g.n1;
   dim3 grid((unsigned)((ns + FLUX_GX - 1) / FLUX_GX), (unsigned)n_blocks);
-  k_flux_extract_f32<<<grid, dim3(FLUX_GX, FLUX_GY), 0, s>>>(g, f.n_grad, f.n_ds, psi_th, half_v, fd, buf, n_blocks,
+  k_flux_extract_f32<<<grid, dim3(FLUX_GX, FLUX_GY), 0, s>>>(flux_tile_args(g, f, psi_th, half_v, fd, buf, n_blocks),
                                                               slot, status);
 }
 

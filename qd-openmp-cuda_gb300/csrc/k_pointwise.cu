@@ -8,6 +8,7 @@
 // which matters on a part whose FP64 rate is a small fraction of its FP32 rate).
 #include "qd_internal.h"
 #include "qd_device.cuh"
+#include "qd_tail.cuh"
 
 namespace qd {
 
@@ -296,141 +297,88 @@ template void launch_rot_energy<float2>(cudaStream_t, const Grid &, const float2
 // full step, books the flux slot and advances the step counter.
 // Coupling-energy partials are laid out [group][ce_n][tiles]; a block collects
 // them from every group (one per l) of its problem that contains its Omega.
-__global__ void __launch_bounds__(256) k_energy_finalize(Grid g, EnergyParts ep, const BlockDesc *__restrict__ blocks,
-                                  const int *__restrict__ pblock0, int n_problems,
-                                  const CoriolisGroup *__restrict__ groups, const int *__restrict__ pgroup0,
-                                  int ce_n, double *__restrict__ energies, double *__restrict__ rec,
-                                  int *__restrict__ d_step, int rec_base, int rec_cap, int n_blocks, double norm_tol,
-                                  int *status, int *status_step, StepTail tail, unsigned *done) {
-  constexpr int NW = 256 / 32;
-  __shared__ double red[NW][2];
+__global__ void __launch_bounds__(256) k_energy_finalize(FinalizeArgs a) {
+  __shared__ double red[8][2];
   __shared__ bool last;
-  const int b = blockIdx.x, tid = threadIdx.x;
-  // everything this launch reads is loaded up front: one round trip
-  const int st0 = *status;
-  const int step = *d_step;   // advanced only by the last CTA, after every CTA has read it
-  const int fcount = (tid == 0 && tail.flux_count) ? *tail.flux_count : 0;
-  const BlockDesc bd = blocks[b];
-  // partial counts of this block: module/potential pairs, kinetic, rotational, Coriolis
-  const int n0 = ep.have_mod ? ep.mod_pe_tiles : 0;
-  const int n1 = ep.have_ke ? bd.nl * ep.ke_tiles : 0;
-  const int n2 = ep.have_re ? bd.nl * ep.re_tiles : 0;
-  // Coriolis: every group (one per l) of this problem, the tiles of this Omega where it is a member
-  const int g_lo = (ep.have_ce && groups) ? pgroup0[bd.problem] : 0;
-  const int n3 = (ep.have_ce && groups) ? (pgroup0[bd.problem + 1] - g_lo) * ep.ce_tiles : 0;
-  const double2 *mp = reinterpret_cast<const double2 *>(ep.mod_pe) + (int64_t)b * ep.mod_pe_tiles;
-  const double *kp = ep.ke + (int64_t)bd.slab0 * ep.ke_tiles;
-  const double *rp = ep.re + (int64_t)bd.slab0 * ep.re_tiles;
-  // two warps per quantity (warp-uniform branch, no divergence inside a loop),
-  // so that each lane's loads are independent and issue together
-  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  const int wq = tid >> 6, l64 = tid & 63;
-  if (wq == 0) {
-#pragma unroll 8
-    for (int t = l64; t < n0; t += 64) {
-      const double2 v = mp[t];
-      acc[0] += v.x;
-      acc[1] += v.y;
-    }
-  } else if (wq == 1) {
-#pragma unroll 8
-    for (int t = l64; t < n1; t += 64) acc[2] += kp[t];
-  } else if (wq == 2) {
-#pragma unroll 8
-    for (int t = l64; t < n2; t += 64) acc[3] += rp[t];
-  } else {
-#pragma unroll 4
-    for (int q = l64; q < n3; q += 64) {
-      const int gi = g_lo + q / ep.ce_tiles, tt = q - (q / ep.ce_tiles) * ep.ce_tiles;
-      const int o = bd.omega - groups[gi].omega_lo;
-      if (o >= 0 && o < groups[gi].n) acc[4] += ep.ce[((int64_t)gi * ce_n + o) * ep.ce_tiles + tt];
-    }
-  }
-  // fixed-order reduction: each warp reduces only its own quantity (the
-  // module/potential pair for the first pair of warps, one sum for the others),
-  // then thread 0 adds the two warps of each quantity
-  double v0 = wq == 0 ? acc[0] : acc[1 + wq], v1 = acc[1];
-  for (int o = 16; o > 0; o >>= 1) {
-    v0 += __shfl_down_sync(0xffffffffu, v0, o);
-    if (wq == 0) v1 += __shfl_down_sync(0xffffffffu, v1, o);
-  }
-  if ((tid & 31) == 0) {
-    red[tid >> 5][0] = v0;
-    red[tid >> 5][1] = v1;
-  }
-  __syncthreads();
+  const int tid = threadIdx.x;
+  // everything this launch reads is loaded up front
+  const int st0 = *a.status;
+  const int step = *a.d_step;   // advanced only at the very end, after every CTA has read it
+  const int fcount = (tid == 0 && a.tail.flux_count) ? *a.tail.flux_count : 0;
+  finalize_reduce(a, blockIdx.x, red);
   if (st0) return;   // set before this launch: nothing is written, the counter is untouched
   double mod = 0.0;
-  if (tid == 0) {
-    const double tot[5] = {red[0][0] + red[1][0], red[0][1] + red[1][1], red[2][0] + red[3][0],
-                           red[4][0] + red[5][0], red[6][0] + red[7][0]};
-    const double dV = g.dr1 * g.dr2;
-    double *e = energies + b * 6;
-    double ev[6];
-    ev[E_MODULE] = ep.have_mod ? tot[0] * dV : e[E_MODULE];
-    ev[E_POTENTIAL] = ep.have_mod ? tot[1] * dV : e[E_POTENTIAL];
-    ev[E_KINETIC] = ep.have_ke ? tot[2] * ep.ke_scale : e[E_KINETIC];
-    ev[E_ROTATIONAL] = ep.have_re ? tot[3] * dV : e[E_ROTATIONAL];
-    ev[E_CORIOLIS] = ep.have_ce ? tot[4] * dV : e[E_CORIOLIS];
-    ev[E_TOTAL] = ev[E_POTENTIAL] + ev[E_KINETIC] + ev[E_ROTATIONAL] + ev[E_CORIOLIS];
-    for (int q = 0; q < 6; q++) e[q] = ev[q];
-    const int slot = step - rec_base;
-    if (rec && slot >= 0 && slot < rec_cap)
-      for (int q = 0; q < 6; q++) rec[((int64_t)slot * n_blocks + b) * 6 + q] = ev[q];
-    mod = ev[E_MODULE];
-  }
-  // ---- end of step: norm guard per problem, flux slot, step counter
-  bool bad = false;   // thread 0: this launch set the norm status
+  if (tid == 0) mod = finalize_write(a, blockIdx.x, step, red);
   if (gridDim.x == 1) {
     if (tid != 0) return;
-    if (ep.have_mod && mod > 1.0 + norm_tol) {
+    bool bad = false;
+    if (a.ep.have_mod && mod > 1.0 + a.norm_tol) {
       bad = true;
-      if (atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
+      if (atomicCAS(a.status, 0, QD_ERR_NORM) == 0) *a.status_step = step;
     }
+    finalize_step_end(a, step, fcount, bad);
   } else {
-    if (tid == 0) {
-      __threadfence();
-      last = atomicAdd(done, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (ep.have_mod)
-      for (int pr = tid; pr < n_problems; pr += 256) {
-        double m = 0.0;
-        for (int bb = pblock0[pr]; bb < pblock0[pr + 1]; bb++) m += __ldcg(energies + bb * 6 + E_MODULE);
-        if (m > 1.0 + norm_tol && atomicCAS(status, 0, QD_ERR_NORM) == 0) *status_step = step;
-      }
-    __syncthreads();
-    if (tid != 0) return;
-    *done = 0u;
-    bad = atomicAdd(status, 0) != 0;
+    finalize_last_cta(a, step, fcount, &last);
   }
-  if (tail.done && !bad) {
-    if (tail.flux_count) {
-      if (fcount >= tail.cap) {
-        atomicCAS(status, 0, QD_ERR_INVALID);
-        *tail.flux_slot = 0;
-      } else {
-        if (fcount == 0) *tail.flux_t0 = (step + 1) * tail.dt;
-        *tail.flux_slot = fcount;
-        *tail.flux_count = fcount + 1;
-      }
-    }
-    *d_step = step + 1;
+}
+
+// Mixed form, one launch for the end of a step: CTAs [0, nfx) extract the flux
+// surface values (slot = the flux count before this step ends), CTAs
+// [nfx, nfx + n_blocks) finalise one Omega block each, and the last CTA to
+// finish applies the norm guard and ends the step.
+__global__ void __launch_bounds__(256) k_step_tail_mixed(FinalizeArgs a, FluxTileArgs f, int nfx, int fx_tiles) {
+  __shared__ double red[8][2];
+  __shared__ float2 sD[FLUX_GY][FLUX_GX];
+  __shared__ float2 sA[FLUX_GX];
+  __shared__ bool last;
+  if (*a.status) return;   // set before this launch: uniform, the counter is untouched
+  const int tid = threadIdx.x;
+  const int step = *a.d_step;
+  const int fcount = a.tail.flux_count ? *a.tail.flux_count : 0;
+  if ((int)blockIdx.x < nfx) {
+    // a full buffer is reported by the step end (QD_ERR_INVALID); nothing is written
+    if (fcount < a.tail.cap)
+      flux_extract_tile(f, fcount, blockIdx.x / fx_tiles, blockIdx.x % fx_tiles, tid, sD, sA);
+  } else {
+    const int b = blockIdx.x - nfx;
+    finalize_reduce(a, b, red);
+    if (tid == 0) finalize_write(a, b, step, red);
   }
+  finalize_last_cta(a, step, fcount, &last);
 }
 
 void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &ep, const BlockDesc *blocks,
                              const int *pblock0, int n_problems, const CoriolisGroup *groups, const int *pgroup0,
                              int ce_n, double *energies, double *rec, const int *d_step, int rec_base, int rec_cap,
                              double norm_tol, int *status, int *status_step, int n_blocks, unsigned *done,
-                             const StepTail *tail) {
-  StepTail t{};
-  if (tail) t = *tail;
-  k_energy_finalize<<<n_blocks, 256, 0, st>>>(g, ep, blocks, pblock0, n_problems, groups, pgroup0, ce_n,
-                                                        energies, rec, const_cast<int *>(d_step), rec_base, rec_cap,
-                                                        n_blocks, norm_tol, status, status_step, t, done);
+                             const StepTail *tail, const FluxTileArgs *fx) {
+  FinalizeArgs a{};
+  a.g = g;
+  a.ep = ep;
+  a.blocks = blocks;
+  a.pblock0 = pblock0;
+  a.n_problems = n_problems;
+  a.groups = groups;
+  a.pgroup0 = pgroup0;
+  a.ce_n = ce_n;
+  a.energies = energies;
+  a.rec = rec;
+  a.d_step = const_cast<int *>(d_step);
+  a.rec_base = rec_base;
+  a.rec_cap = rec_cap;
+  a.n_blocks = n_blocks;
+  a.norm_tol = norm_tol;
+  a.status = status;
+  a.status_step = status_step;
+  if (tail) a.tail = *tail;
+  a.done = done;
+  if (fx) {
+    const int fx_tiles = (int)(((int64_t)g.nth * g.n1 + FLUX_GX - 1) / FLUX_GX);
+    const int nfx = fx_tiles * n_blocks;
+    k_step_tail_mixed<<<nfx + n_blocks, FLUX_GX * FLUX_GY, 0, st>>>(a, *fx, nfx, fx_tiles);
+  } else {
+    k_energy_finalize<<<n_blocks, 256, 0, st>>>(a);
+  }
 }
 
 }  // namespace qd

@@ -8,6 +8,7 @@
 // and steps are replayed from CUDA graphs.
 #include "qd_internal.h"
 #include "qd_device.cuh"
+#include "qd_tail.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -559,20 +560,24 @@ static void enqueue_tail(qd_session *s) {
     tail.cap = s->flux.chunk;
     tail.dt = s->dt;
   }
+  if (s->flux.enabled && s->precision == QD_PRECISION_MIXED) {
+    // mixed form: surface extraction and energy finalisation in one launch
+    const FluxTileArgs fx = flux_tile_args(g, s->flux, s->psi_thf, s->half_v_lift, s->fdf, s->flux_buf_f, s->n_blocks);
+    launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
+                            s->max_group_n, s->energies, s->rec, s->d_step, s->rec_base, s->rec_cap, s->norm_tol,
+                            s->status, s->status_step, s->n_blocks, s->step_done, &tail, &fx);
+    prof_mark(st, "step_tail");
+    return;
+  }
   launch_energy_finalize2(st, g, ep, s->d_blocks, s->d_pblock0, s->n_problems, s->d_groups, s->d_pgroup0,
                           s->max_group_n, s->energies, s->rec, s->d_step, s->rec_base, s->rec_cap, s->norm_tol,
                           s->status, s->status_step, s->n_blocks, s->step_done, &tail);
   prof_mark(st, "energy_finalize");
   if (s->flux.enabled) {
-    if (s->precision == QD_PRECISION_MIXED) {
-      launch_flux_extract_f32(st, g, s->flux, s->psi_thf, s->n_blocks, s->half_v_lift, s->fdf, s->flux_buf_f,
-                              s->flux_slot, s->status);
-    } else {
-      const int64_t ns = (int64_t)g.nth * g.n1;
-      dim3 grid((unsigned)((ns + 127) / 128), (unsigned)s->n_blocks);
-      k_flux_extract_dev<<<grid, 128, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
-                                               s->flux_buf, s->n_blocks, s->flux_slot, s->status);
-    }
+    const int64_t ns = (int64_t)g.nth * g.n1;
+    dim3 grid((unsigned)((ns + 127) / 128), (unsigned)s->n_blocks);
+    k_flux_extract_dev<<<grid, 128, 0, st>>>(g, s->flux.n_grad, s->flux.n_ds, s->psi_th, s->half_v, s->fd,
+                                             s->flux_buf, s->n_blocks, s->flux_slot, s->status);
     prof_mark(st, "flux_extract");
   }
 }
@@ -582,7 +587,7 @@ static int count_launches_per_step(qd_session *s) {
   int n = 1 + (slab ? 1 : 3) + 1 + 1;   // fwd, fft, bwd, finalize (+ step counter)
   if (s->cor_f32) n += 2;              // coriolis x2 (rotational energy fused)
   else if (s->any_coupled) n += 3;     // coriolis x2, rot energy
-  if (s->flux.enabled) n += 1;          // surface extraction
+  if (s->flux.enabled && s->precision != QD_PRECISION_MIXED) n += 1;   // surface extraction (fused in the mixed form)
   return n;
 }
 

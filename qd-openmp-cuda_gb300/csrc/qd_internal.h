@@ -206,11 +206,14 @@ struct StepTail {
   int cap;
   double dt;
 };
+// With fx (mixed form, end of a full step) the surface extraction runs in the
+// same launch (k_step_tail_mixed); fx is defined in qd_tail.cuh.
+struct FluxTileArgs;
 void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &ep, const BlockDesc *blocks,
                              const int *pblock0, int n_problems, const CoriolisGroup *groups, const int *pgroup0,
                              int ce_n, double *energies, double *rec, const int *d_step, int rec_base, int rec_cap,
                              double norm_tol, int *status, int *status_step, int n_blocks, unsigned *done,
-                             const StepTail *tail = nullptr);
+                             const StepTail *tail = nullptr, const FluxTileArgs *fx = nullptr);
 void launch_build_half_v_lift(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
                               float2 *half_v);
 void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const float2 *psi_th,
