@@ -21,6 +21,7 @@ from typing import Callable, List, Optional, Sequence
 import numpy as np
 
 from . import inputs  # noqa: F401  (FH2Data builders)
+from . import snapshots  # noqa: F401  (headless wave-packet snapshots for the callback)
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "libqd.so"

@@ -281,3 +281,17 @@ def test_mixed_coupled_norm_tracks_fp64(qd, gpu):
     m0 = out[0]["options"]["energies"][:, :, 0].sum(axis=1)
     assert np.max(np.abs(m1 - m0)) < 2e-6
     assert rel(out[1]["OmegaStates"]["wave_packets"], out[0]["OmegaStates"]["wave_packets"]) < 1e-4
+
+
+def test_snapshot_callback_writes_copied_packets(qd, gpu, tmp_path):
+    """The headless snapshot callback receives the copied wave packets (steps 0, 2 of 4)."""
+    cfg, d, _ = make(qd, J=0, n1=32, n2=16, n_theta=8, l_max=6, steps=4)
+    d["options"]["wave_to_matlab"] = "PlotPotWave.m"
+    d["options"]["steps_to_copy_psi_from_device_to_host"] = 2
+    d["options"]["precision"] = 1
+    qd.cudaOpenMPEvolution(d, callback=qd.snapshots.snapshot_callback(tmp_path))
+    names = sorted(p.name for p in tmp_path.iterdir())
+    assert names == ["density_000000.pgm", "density_000002.pgm", "psi_000000.npy", "psi_000002.npy"]
+    psi2 = np.load(tmp_path / "psi_000002.npy")
+    assert psi2.shape == d["OmegaStates"]["wave_packets"].shape and np.isfinite(psi2).all()
+    assert qd.snapshots.read_pgm(tmp_path / "density_000002.pgm").max() == 255
