@@ -20,14 +20,16 @@
 // products loses about 2e-6 of the norm per forward+backward pair to biased
 // accumulation rounding; the exact form has no such bias.)
 //
-// Per CTA: 64 points (M = 128 real rows) x all N columns.  Four warps stage
-// the A tile (FP64 load -> FP32; forward: absorbing mask and exp(-iV dt) as an
-// exactly area-preserving three-shear rotation) into an FP32 buffer; each
-// thread then scales and slices one row into the SWIZZLE_NONE K-major
-// canonical layout; one thread issues the tcgen05.mma chain; the commit
-// arrives on an mbarrier; each thread reads its own row (TMEM lane) back with
-// tcgen05.ld 32x32b, recombines, converts to FP64 and stores.  The backward
-// epilogue also reduces the module and potential energy.
+// The kernel (k_legendre_tc_ws) is persistent and warp-specialised: one CTA
+// per SM walks a contiguous range of (block, 64-point tile) pairs, M = 128
+// real rows each.  Eight producer warps load the tile from the c64 pool (with
+// an L2 prefetch of the next tile; forward: absorbing mask and exp(-iV dt) as
+// an exactly area-preserving three-shear rotation), stage it in FP32, scale
+// and slice every row into the SWIZZLE_NONE K-major canonical layout; one
+// consumer thread issues the tcgen05.mma chain (four MMAs per K = 16 step) and
+// commits to an mbarrier; eight consumer warps read their rows (TMEM lanes)
+// back with tcgen05.ld 32x32b, recombine, and store c64.  The backward
+// epilogue also reduces the module and potential energy per tile.
 #include <cuda_bf16.h>
 
 
@@ -37,7 +39,6 @@
 namespace qd {
 
 namespace {
-constexpr int TC_THREADS = 256;     // 8 warps: staging, slicing and epilogue; thread 0 issues the MMAs
 constexpr int TC_POINTS = 64;        // 128 real rows
 constexpr uint64_t WAIT_NS = 1000000000ull;   // give up waiting for the MMA chain after 1 s
 
@@ -115,17 +116,6 @@ __device__ inline void tmem_ld16(uint32_t taddr, float *v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
-}
-
-__device__ inline void split3(float x, uint16_t &a0, uint16_t &a1, uint16_t &a2) {
-  const __nv_bfloat16 b0 = __float2bfloat16_rn(x);
-  float r = x - __bfloat162float(b0);
-  const __nv_bfloat16 b1 = __float2bfloat16_rn(r);
-  r = r - __bfloat162float(b1);
-  const __nv_bfloat16 b2 = __float2bfloat16_rn(r);
-  a0 = __bfloat16_as_ushort(b0);
-  a1 = __bfloat16_as_ushort(b1);
-  a2 = __bfloat16_as_ushort(b2);
 }
 
 __host__ __device__ inline int round16(int x) { return (x + 15) & ~15; }
@@ -229,12 +219,13 @@ __device__ inline void rot_lift2(float &x, float &y, float2 ts) {
 
 // ---------------------------------------------------------------------------
 // Persistent, warp-specialised form.  Each CTA walks a contiguous range of
-// (block, 64-point tile) pairs.  Warps 0-3 (producers) stage and slice tile
-// t+1 while warps 4-7 (consumers) drain tile t from TMEM; thread 128 issues
-// the MMA chain of each tile.  Three mbarriers carry the hand-offs:
-//   slices_ready (128 producer arrivals)  -> the MMA may read A/B slices
+// (block, 64-point tile) pairs.  Warps 0-7 (producers) stage and slice tile
+// t+1 while warps 8-15 (consumers) drain tile t from TMEM; consumer thread
+// MMA_ISSUER issues the MMA chain of each tile.  Three mbarriers carry the
+// hand-offs:
+//   slices_ready (256 producer arrivals)  -> the MMA may read A/B slices
 //   mma_done     (tcgen05.commit)         -> TMEM holds tile t; A/B reusable
-//   tmem_free    (128 consumer arrivals)  -> the next MMA may overwrite TMEM
+//   tmem_free    (256 consumer arrivals)  -> the next MMA may overwrite TMEM
 // Every wait is bounded (1 s); a timeout sets the error status and the CTA
 // stops issuing work, waits (bounded) for its MMAs, frees TMEM and returns.
 __device__ inline void named_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
