@@ -456,8 +456,9 @@ static EnergyParts energy_parts(qd_session *s, bool mod, bool ke, bool re, bool 
 
 static void enqueue_tail(qd_session *s);
 
-// Mixed form of the same step: tensor-core Legendre contractions, FP32 FFT and
-// FP32 three-shear phases; Coriolis, energies and flux in FP64.
+// Mixed form of the same step on the c64 pools: tensor-core Legendre
+// contractions, the separable FP32 slab FFT, FP32 Coriolis (FP64-exact
+// operator) and FP32 three-shear phases; energies and flux accumulate in FP64.
 static void enqueue_step_mixed(qd_session *s, bool first) {
   cudaStream_t st = s->stream;
   const Grid &g = s->g;
