@@ -13,7 +13,8 @@ BUILD = HERE / "_build"
 LIB = HERE / "libqd.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-SOURCES = ["qd_api.cu", "k_pointwise.cu", "k_legendre.cu", "k_fft.cu", "k_coriolis.cu", "k_flux.cu", "k_diag.cu", "k_legendre_tc.cu", "k_noalloc.cu"]
+SOURCES = ["qd_api.cu", "k_pointwise.cu", "k_legendre.cu", "k_fft.cu", "k_coriolis.cu", "k_coriolis_fp64_small.cu", "k_coriolis_fp64_n32.cu",
+           "k_coriolis_fp64_n48.cu", "k_coriolis_fp64_n48_c64.cu", "k_flux.cu", "k_diag.cu", "k_legendre_tc.cu", "k_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -11,6 +11,8 @@
 // problem, loads the whole Omega column, applies U = V diag(phase(R)) V^T as
 // two real n x n products around the diagonal phase, and writes the column
 // back in place: no scratch, no memset, no copy, one read and one write.
+// This file holds the phase tables, the FP32 kernel of the mixed form and the
+// dispatch of the FP64 kernel, whose body is in qd_coriolis64.cuh.
 // The coupling energy (omegawavepacket.cu:503-553) is evaluated on the
 // pre-update values in the same pass: sum over |Omega-Omega1| <= 1 of
 // conj(psi^Omega) H_{Omega Omega1}/(2 m1 R^2) psi^Omega1, doubled off the
@@ -18,13 +20,11 @@
 #include "qd_internal.h"
 #include "qd_device.cuh"
 
+#include <type_traits>
+
 namespace qd {
 
-namespace {
-constexpr int COR_THREADS = 128;
-}
-
-int coriolis_tiles(const Grid &g) { return (int)((g.npt + COR_THREADS - 1) / COR_THREADS); }
+int coriolis_tiles(const Grid &g) { return (int)((g.npt + CORIOLIS_THREADS - 1) / CORIOLIS_THREADS); }
 
 __global__ void k_build_coriolis_phase(Grid g, const CoriolisGroup *__restrict__ groups, const double *__restrict__ e,
                                        double dt, double2 *__restrict__ ph) {
@@ -102,7 +102,8 @@ __device__ __forceinline__ void coriolis_f32_body(const Grid &g, float2 *__restr
   float ce[NE], re[NE];
 #pragma unroll
   for (int o = 0; o < NE; o++) ce[o] = re[o] = 0.0f;
-  for (int64_t pt = (int64_t)blockIdx.x * COR_THREADS + threadIdx.x; pt < g.npt; pt += (int64_t)tiles * COR_THREADS) {
+  for (int64_t pt = (int64_t)blockIdx.x * CORIOLIS_THREADS + threadIdx.x; pt < g.npt;
+       pt += (int64_t)tiles * CORIOLIS_THREADS) {
     const int i = (int)(pt % g.n1), j = (int)(pt / g.n1);
     float2 x[MAXN];
 #pragma unroll
@@ -201,7 +202,7 @@ __device__ __forceinline__ void coriolis_f32_body(const Grid &g, float2 *__restr
   __syncthreads();
   for (int o = threadIdx.x; o < n; o += blockDim.x) {
     double c = 0.0, r = 0.0;
-    for (int w = 0; w < COR_THREADS / 32; w++) {
+    for (int w = 0; w < CORIOLIS_THREADS / 32; w++) {
       c += (double)red[w][o];
       r += (double)red[w][CORIOLIS_F32_MAXN + o];
     }
@@ -215,15 +216,15 @@ __device__ __forceinline__ void coriolis_f32_body(const Grid &g, float2 *__restr
 
 int coriolis_f32_class(int n) {
   for (int c = 0; c < CORIOLIS_F32_CLASSES; c++)
-    if (n <= 4 * (c + 1)) return c;
+    if (n <= CORIOLIS_F32_STEP * (c + 1)) return c;
   return -1;
 }
 
 // One launch for every group: each CTA runs the body compiled for its
-// group's size class (at most 4, 8, ..., 4 (MAXC+1) blocks), so small groups
+// group's size class (at most 4, 8, ..., 24 blocks), so small groups
 // do not pay for the largest one's unrolled loops.
 template <int MAXC, bool EN>
-__global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__restrict__ psi_j,
+__global__ void __launch_bounds__(CORIOLIS_THREADS) k_coriolis_f32(Grid g, float2 *__restrict__ psi_j,
                                                               const BlockDesc *__restrict__ blocks,
                                                               const CoriolisGroup *__restrict__ groups,
                                                               const float *__restrict__ Vh, const float *__restrict__ Vl,
@@ -234,16 +235,17 @@ __global__ void __launch_bounds__(COR_THREADS) k_coriolis_f32(Grid g, float2 *__
                                                               double *__restrict__ re_part, int tiles, int ce_n,
                                                               const int *__restrict__ order, const int *status) {
   if (status && *status) return;
-  constexpr int MAXN = 4 * (MAXC + 1);
+  constexpr int MAXN = CORIOLIS_F32_STEP * (MAXC + 1);
   __shared__ float sVh[MAXN * MAXN], sVl[MAXN * MAXN];
   __shared__ float Hd[MAXN], Ho[MAXN];
-  __shared__ float red[COR_THREADS / 32][2 * CORIOLIS_F32_MAXN];
+  __shared__ float red[CORIOLIS_THREADS / 32][2 * CORIOLIS_F32_MAXN];
   __shared__ int64_t base[MAXN];
   const int gid = order[blockIdx.y];
-  const int cls = (groups[gid].n + 3) / 4 - 1;
-#define QD_BODY(C)                                                                                                \
-  coriolis_f32_body<4 * ((C) + 1), EN>(g, psi_j, blocks, groups, Vh, Vl, phl, Hp, rotR, rotr, pro, epi, I1f, I2f, \
-                                        ce_part, re_part, tiles, ce_n, gid, sVh, sVl, Hd, Ho, red, base)
+  const int cls = (groups[gid].n + CORIOLIS_F32_STEP - 1) / CORIOLIS_F32_STEP - 1;
+#define QD_BODY(C)                                                                                       \
+  coriolis_f32_body<CORIOLIS_F32_STEP * ((C) + 1), EN>(g, psi_j, blocks, groups, Vh, Vl, phl, Hp, rotR, rotr, \
+                                                       pro, epi, I1f, I2f, ce_part, re_part, tiles, ce_n, gid,  \
+                                                       sVh, sVl, Hd, Ho, red, base)
   if (MAXC >= 5 && cls == 5) QD_BODY(MAXC >= 5 ? 5 : 0);
   else if (MAXC >= 4 && cls == 4) QD_BODY(MAXC >= 4 ? 4 : 0);
   else if (MAXC >= 3 && cls == 3) QD_BODY(MAXC >= 3 ? 3 : 0);
@@ -260,16 +262,18 @@ void launch_coriolis_f32(cudaStream_t s, const Grid &g, float2 *psi_j, const Blo
                          int tiles, const int *status) {
   if (n_groups == 0) return;
   const dim3 grid((unsigned)tiles, (unsigned)n_groups);
-#define QD_COR32(C)                                                                                              \
-  do {                                                                                                           \
-    if (ce_part)                                                                                                 \
-      k_coriolis_f32<C, true><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H, rotR, rotr,    \
-                                                           pro ? 1 : 0, epi ? 1 : 0, I1f, I2f, ce_part, re_part,    \
-                                                           tiles, max_n, order, status);                          \
-    else                                                                                                         \
-      k_coriolis_f32<C, false><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H, rotR, rotr,   \
-                                                            pro ? 1 : 0, epi ? 1 : 0, I1f, I2f, nullptr, nullptr,   \
-                                                            tiles, max_n, order, status);                        \
+#define QD_COR32(C)                                                                                         \
+  do {                                                                                                      \
+    if (ce_part)                                                                                            \
+      k_coriolis_f32<C, true><<<grid, CORIOLIS_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H,    \
+                                                                rotR, rotr, pro ? 1 : 0, epi ? 1 : 0, I1f, \
+                                                                I2f, ce_part, re_part, tiles, max_n, order, \
+                                                                status);                                   \
+    else                                                                                                    \
+      k_coriolis_f32<C, false><<<grid, CORIOLIS_THREADS, 0, s>>>(g, psi_j, blocks, groups, Vh, Vl, phl, H,   \
+                                                                 rotR, rotr, pro ? 1 : 0, epi ? 1 : 0, I1f, \
+                                                                 I2f, nullptr, nullptr, tiles, max_n, order, \
+                                                                 status);                                   \
   } while (0)
   switch (coriolis_f32_class(max_n)) {
     case 0: QD_COR32(0); break;
@@ -305,105 +309,28 @@ void launch_build_coriolis_lift(cudaStream_t s, const Grid &g, const CoriolisGro
   k_build_coriolis_lift<<<dim3(4, n_groups), 256, 0, s>>>(g, groups, e, dt, phl);
 }
 
-template <int MAXN, typename S>
-__global__ void __launch_bounds__(COR_THREADS) k_coriolis(Grid g, S *__restrict__ psi_j,
-                                                          const BlockDesc *__restrict__ blocks,
-                                                          const CoriolisGroup *__restrict__ groups,
-                                                          const double *__restrict__ Vp, const double2 *__restrict__ php,
-                                                          const double *__restrict__ Hp, double *__restrict__ ce_part,
-                                                          int ce_tiles, int ce_n, const double2 *__restrict__ tabE,
-                                                          const int *status, const double2 *__restrict__ tabP) {
-  if (status && *status) return;
-  __shared__ double Vs[MAXN * MAXN];
-  __shared__ double Hd[MAXN], Ho[MAXN];
-  __shared__ double red[32];
-  const CoriolisGroup gr = groups[blockIdx.y];
-  const int n = gr.n;
-  for (int q = threadIdx.x; q < n * n; q += blockDim.x) Vs[q] = Vp[gr.v0 + q];
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    Hd[q] = Hp[gr.h0 + q * n + q];
-    Ho[q] = q + 1 < n ? Hp[gr.h0 + q * n + q + 1] : 0.0;
-  }
-  __syncthreads();
-  const int64_t pt = (int64_t)blockIdx.x * COR_THREADS + threadIdx.x;
-  const bool active = pt < g.npt;
-  const int i = active ? (int)(pt % g.n1) : 0;
-  double2 x[MAXN];
-  int64_t addr[MAXN];
-#pragma unroll
-  for (int o = 0; o < MAXN; o++) {
-    if (o < n) {
-      const BlockDesc bd = blocks[gr.block_lo + o];
-      addr[o] = (int64_t)(bd.slab0 + (gr.l - bd.omega)) * g.npt + pt;
-      x[o] = active ? load_c(psi_j + addr[o]) : make_double2(0.0, 0.0);
-      if (tabP && active) x[o] = cmul(x[o], ldg2(tabP + (int64_t)gr.l * g.npt + pt));
-    }
-  }
-  if (ce_part) {
-    const double R = g.left1 + i * g.dr1;
-    const double inv = 1.0 / (2 * g.m1 * R * R);
-#pragma unroll
-    for (int o = 0; o < MAXN; o++) {
-      if (o < n) {
-        double c = Hd[o] * inv * (x[o].x * x[o].x + x[o].y * x[o].y);
-        if (o + 1 < n) c += 2.0 * Ho[o] * inv * (x[o].x * x[o + 1].x + x[o].y * x[o + 1].y);
-        c = block_sum(active ? c : 0.0, red);
-        if (threadIdx.x == 0)
-          ce_part[((int64_t)blockIdx.y * ce_n + o) * ce_tiles + blockIdx.x] = c;
-      }
-    }
-  }
-  double2 y[MAXN];
-#pragma unroll
-  for (int a = 0; a < MAXN; a++) {
-    if (a < n) {
-      double2 acc = make_double2(0.0, 0.0);
-#pragma unroll
-      for (int o = 0; o < MAXN; o++)
-        if (o < n) {
-          const double v = Vs[o * n + a];
-          acc.x = fma(v, x[o].x, acc.x);
-          acc.y = fma(v, x[o].y, acc.y);
-        }
-      y[a] = cmul(acc, ldg2(php + gr.ph0 + (int64_t)a * g.n1 + i));
-    }
-  }
-  if (!active) return;
-#pragma unroll
-  for (int o = 0; o < MAXN; o++) {
-    if (o < n) {
-      double2 acc = make_double2(0.0, 0.0);
-#pragma unroll
-      for (int a = 0; a < MAXN; a++)
-        if (a < n) {
-          const double v = Vs[o * n + a];
-          acc.x = fma(v, y[a].x, acc.x);
-          acc.y = fma(v, y[a].y, acc.y);
-        }
-      if (tabE) acc = cmul(acc, ldg2(tabE + (int64_t)gr.l * g.npt + pt));
-      store_c(psi_j + addr[o], acc);
-    }
-  }
-}
-
 template <typename S>
 void launch_coriolis(cudaStream_t s, const Grid &g, S *psi_j, const BlockDesc *blocks,
                      const CoriolisGroup *groups, int n_groups, int max_n, const double *V, const double2 *ph,
                      const double *H, double *ce_part, int ce_tiles, const double2 *tabE, const int *status,
                      const double2 *tabP) {
   if (n_groups == 0) return;
-  dim3 grid((unsigned)coriolis_tiles(g), (unsigned)n_groups);
-#define QD_COR(M)                                                                                        \
-  k_coriolis<M, S><<<grid, COR_THREADS, 0, s>>>(g, psi_j, blocks, groups, V, ph, H, ce_part, ce_tiles, max_n, \
-                                             tabE, status, tabP)
-  if (max_n <= 2) QD_COR(2);
-  else if (max_n <= 4) QD_COR(4);
-  else if (max_n <= 8) QD_COR(8);
-  else if (max_n <= 16) QD_COR(16);
-  else if (max_n <= 24) QD_COR(24);
-  else if (max_n <= 32) QD_COR(32);
-  else if (max_n <= 48) QD_COR(48);
-  else throw Error{QD_ERR_UNSUPPORTED, "more than 48 coupled Omega blocks"};
+#define QD_COR(M) \
+  launch_coriolis_n<M, S>(s, g, psi_j, blocks, groups, n_groups, max_n, V, ph, H, ce_part, ce_tiles, tabE, status, tabP)
+  if (max_n > 48) throw Error{QD_ERR_UNSUPPORTED, "more than 48 coupled Omega blocks"};
+  if constexpr (std::is_same<S, float2>::value) {
+    // the mixed form uses this kernel only above the FP32 kernel's 24 blocks
+    if (max_n <= 32) QD_COR(32);
+    else QD_COR(48);
+  } else {
+    if (max_n <= 2) QD_COR(2);
+    else if (max_n <= 4) QD_COR(4);
+    else if (max_n <= 8) QD_COR(8);
+    else if (max_n <= 16) QD_COR(16);
+    else if (max_n <= 24) QD_COR(24);
+    else if (max_n <= 32) QD_COR(32);
+    else QD_COR(48);
+  }
 #undef QD_COR
 }
 template void launch_coriolis<double2>(cudaStream_t, const Grid &, double2 *, const BlockDesc *,

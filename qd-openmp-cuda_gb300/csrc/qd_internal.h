@@ -168,6 +168,12 @@ void launch_coriolis(cudaStream_t s, const Grid &g, S *psi_j, const BlockDesc *b
 void launch_build_coriolis_phase(cudaStream_t s, const Grid &g, const CoriolisGroup *groups, int n_groups,
                                  int max_n, const double *e, double dt, double2 *ph);
 int coriolis_tiles(const Grid &g);
+constexpr int CORIOLIS_THREADS = 128;    // points per CTA of the Coriolis kernels
+// one FP64 kernel variant for groups of at most MAXN blocks (instantiated in k_coriolis_fp64_*.cu)
+template <int MAXN, typename S>
+void launch_coriolis_n(cudaStream_t s, const Grid &g, S *psi_j, const BlockDesc *blocks, const CoriolisGroup *groups,
+                       int n_groups, int max_n, const double *V, const double2 *ph, const double *H, double *ce_part,
+                       int ce_tiles, const double2 *tabE, const int *status, const double2 *tabP);
 // Mixed form (FP32 arithmetic, c64 pool, at most CORIOLIS_F32_MAXN coupled
 // blocks): V = Vh + Vl as FP32 pairs, phases as three-shear coefficients
 // (phl from launch_build_coriolis_lift; rotR/rotr the dt/4 rotational phase,
@@ -175,7 +181,8 @@ int coriolis_tiles(const Grid &g);
 // [group][omega][tiles] and rotational-energy partials [slab][tiles] of the
 // outgoing state.
 constexpr int CORIOLIS_F32_MAXN = 24;
-constexpr int CORIOLIS_F32_CLASSES = 6;  // size classes of at most 4, 8, ..., 24 blocks (one body each)
+constexpr int CORIOLIS_F32_STEP = 4;     // size classes of at most 4, 8, ..., 24 blocks (one body each)
+constexpr int CORIOLIS_F32_CLASSES = 6;
 constexpr int CORIOLIS_F32_TILES = 16;   // CTAs per group (its partial tiles)
 int coriolis_f32_class(int n);           // size class of a group of n blocks, -1 above the limit
 // order: the group indices, largest groups first

@@ -248,6 +248,20 @@ def test_mixed_stages_match_oracle(qd, oracle, gpu, case):
         np.testing.assert_allclose(s.energies()[:, 1], o.potential_energy(), rtol=1e-5, atol=1e-12)
 
 
+@pytest.mark.parametrize("J", [28, 40])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_large_coriolis_groups(qd, oracle, gpu, J, prec):
+    """29 and 41 coupled Omega blocks: the FP64 Coriolis variants for 25-32 and 33-48 blocks with
+    complex128 (FP64 form) and complex64 (mixed form) storage, four full steps against the oracle."""
+    cfg, d, dref = make(qd, J=J, parity=0, n1=16, n2=8, n_theta=44, l_max=42, steps=4)
+    assert len(np.ravel(d["OmegaStates"]["omegas"])) == J + 1
+    d["options"]["precision"] = prec
+    o = oracle.Oracle(dref)
+    o.run(cfg.total_steps)
+    qd.cudaOpenMPEvolution(d)
+    assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < (1e-12 if prec == 0 else 1e-5)
+
+
 def test_mixed_production_grid_tracks_fp64(qd, gpu):
     """256x128x96: 40 steps of the mixed form stay within 1e-5 of the FP64 form; norm drift <= 1e-6."""
     cfg = qd.inputs.CONFIGS["fh2_j0_256x128x96"]
