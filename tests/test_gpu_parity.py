@@ -145,6 +145,32 @@ def test_callback_sees_copied_wave_packets(qd, oracle, gpu):
         assert rel(psi, o.wave_packets()) < 1e-12
 
 
+@pytest.mark.parametrize("J", [0, 2])
+def test_mixed_graph_chunks_equal_single_steps(qd, gpu, J):
+    """140 mixed steps replayed from 64-step graphs (device-side step counter, flux slot and
+    record index) equal the same steps enqueued one at a time (a callback after every step):
+    wave packets and energy records bit for bit; P(E) to 1e-12 of its maximum (a callback may
+    flush the surface buffer at other steps, which regroups the FP64 sums)."""
+    out = []
+    for every_step in (False, True):
+        cfg, d, _ = make(qd, J=J, parity=0, n1=32, n2=16, n_theta=8, l_max=6, steps=140, n_energies=8)
+        d["options"]["precision"] = 1
+        nb = len(np.ravel(d["OmegaStates"]["omegas"]))
+        d["options"]["energies"] = np.zeros((cfg.total_steps, nb, 6))
+        if every_step:
+            d["options"]["wave_to_matlab"] = "FH2Matlab.m"
+            d["options"]["steps_to_copy_psi_from_device_to_host"] = 1
+            qd.cudaOpenMPEvolution(d, callback=lambda data: 0)
+        else:
+            qd.cudaOpenMPEvolution(d)
+        assert int(d["time"]["steps"]) == cfg.total_steps
+        out.append(d)
+    a, b = out
+    assert np.array_equal(a["OmegaStates"]["wave_packets"], b["OmegaStates"]["wave_packets"])
+    assert np.array_equal(a["options"]["energies"], b["options"]["energies"])
+    assert np.max(np.abs(a["CRP"]["CRP"] - b["CRP"]["CRP"])) <= 1e-12 * np.abs(b["CRP"]["CRP"]).max()
+
+
 def test_callback_error_aborts(qd, gpu):
     cfg, d, _ = make(qd, J=0, steps=4)
     d["options"]["wave_to_matlab"] = "FH2Matlab.m"
