@@ -67,6 +67,15 @@ __device__ inline void lift2c(float2 &v, float2 ts) {
   v.x = x;
   v.y = y;
 }
+// Two (hi, lo) eigenvector pairs in one 16-byte shared-memory load.  The load
+// is volatile so that it stays inside the point loop: V held in registers
+// across the loop would leave room for only a few warps.
+__device__ __forceinline__ float4 lds_pair2(const float *p) {
+  float4 v;
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+  return v;
+}
 }  // namespace
 
 template <int MAXN, bool EN>
@@ -79,14 +88,18 @@ __device__ __forceinline__ void coriolis_f32_body(const Grid &g, float2 *__restr
                                                               int pro, int epi, const float *__restrict__ I1f,
                                                               const float *__restrict__ I2f, double *__restrict__ ce_part,
                                                               double *__restrict__ re_part, int tiles, int ce_n,
-                                                              int gid, float *sVh, float *sVl, float *Hd, float *Ho,
+                                                              int gid, float *sV, float *Hd, float *Ho,
                                                               float (*red)[2 * CORIOLIS_F32_MAXN], int64_t *base) {
   const CoriolisGroup gr = groups[gid];
   const int n = gr.n, l = gr.l;
-  // row stride MAXN: every (o, a) offset below is a compile-time constant
-  for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
-    sVh[(q / n) * MAXN + q % n] = Vh[gr.v0 + q];
-    sVl[(q / n) * MAXN + q % n] = Vl[gr.v0 + q];
+  // sV[(o MAXN + a) 2 + {0, 1}] = (Vh, Vl)[o][a], zero outside n x n: row
+  // stride MAXN makes every offset below a compile-time constant, and the
+  // zero padding lets the products run over whole pairs of a
+  for (int q = threadIdx.x; q < MAXN * MAXN; q += blockDim.x) {
+    const int o = q / MAXN, a = q % MAXN;
+    const bool in = o < n && a < n;
+    sV[2 * q] = in ? Vh[gr.v0 + o * n + a] : 0.0f;
+    sV[2 * q + 1] = in ? Vl[gr.v0 + o * n + a] : 0.0f;
   }
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
     Hd[q] = (float)Hp[gr.h0 + q * n + q];
@@ -131,10 +144,8 @@ __device__ __forceinline__ void coriolis_f32_body(const Grid &g, float2 *__restr
           ce[o] = fmaf(inv1, c, ce[o]);
         }
     }
-    // y = V^T x: one pass over the members o, every a accumulating independently.
-    // V is re-read from shared memory per point (volatile): held in registers
-    // across the point loop it would leave room for only a few warps
-    const volatile float *vVh = sVh, *vVl = sVl;
+    // y = V^T x: one pass over the members o, every a accumulating independently;
+    // V is re-read from shared memory per point, two elements per load
     float2 y[MAXN];
 #pragma unroll
     for (int a = 0; a < MAXN; a++) y[a] = make_float2(0.0f, 0.0f);
@@ -142,31 +153,35 @@ __device__ __forceinline__ void coriolis_f32_body(const Grid &g, float2 *__restr
     for (int o = 0; o < MAXN; o++) {
       if (o < n) {
 #pragma unroll
-        for (int a = 0; a < MAXN; a++)
+        for (int a = 0; a < MAXN; a += 2)
           if (a < n) {
-            const float vh = vVh[o * MAXN + a], vl = vVl[o * MAXN + a];
-            y[a].x = fmaf(vl, x[o].x, fmaf(vh, x[o].x, y[a].x));
-            y[a].y = fmaf(vl, x[o].y, fmaf(vh, x[o].y, y[a].y));
+            const float4 v = lds_pair2(sV + 2 * (o * MAXN + a));
+            y[a].x = fmaf(v.y, x[o].x, fmaf(v.x, x[o].x, y[a].x));
+            y[a].y = fmaf(v.y, x[o].y, fmaf(v.x, x[o].y, y[a].y));
+            y[a + 1].x = fmaf(v.w, x[o].x, fmaf(v.z, x[o].x, y[a + 1].x));
+            y[a + 1].y = fmaf(v.w, x[o].y, fmaf(v.z, x[o].y, y[a + 1].y));
           }
       }
     }
 #pragma unroll
     for (int a = 0; a < MAXN; a++)
       if (a < n) lift2c(y[a], __ldg(phl + gr.ph0 + (int64_t)a * g.n1 + i));
-    // x = V y
+    // x = V y, each x[o] summed over a in ascending order (y beyond n is zero)
 #pragma unroll
-    for (int o = 0; o < MAXN; o++) x[o] = make_float2(0.0f, 0.0f);
+    for (int o = 0; o < MAXN; o++) {
+      float2 acc = make_float2(0.0f, 0.0f);
+      if (o < n) {
 #pragma unroll
-    for (int a = 0; a < MAXN; a++) {
-      if (a < n) {
-#pragma unroll
-        for (int o = 0; o < MAXN; o++)
-          if (o < n) {
-            const float vh = vVh[o * MAXN + a], vl = vVl[o * MAXN + a];
-            x[o].x = fmaf(vl, y[a].x, fmaf(vh, y[a].x, x[o].x));
-            x[o].y = fmaf(vl, y[a].y, fmaf(vh, y[a].y, x[o].y));
+        for (int a = 0; a < MAXN; a += 2)
+          if (a < n) {
+            const float4 v = lds_pair2(sV + 2 * (o * MAXN + a));
+            acc.x = fmaf(v.y, y[a].x, fmaf(v.x, y[a].x, acc.x));
+            acc.y = fmaf(v.y, y[a].y, fmaf(v.x, y[a].y, acc.y));
+            acc.x = fmaf(v.w, y[a + 1].x, fmaf(v.z, y[a + 1].x, acc.x));
+            acc.y = fmaf(v.w, y[a + 1].y, fmaf(v.z, y[a + 1].y, acc.y));
           }
       }
+      x[o] = acc;
     }
     const float rI = ll * (inv1 + __ldg(I2f + j));
 #pragma unroll
@@ -236,7 +251,7 @@ __global__ void __launch_bounds__(CORIOLIS_THREADS) k_coriolis_f32(Grid g, float
                                                               const int *__restrict__ order, const int *status) {
   if (status && *status) return;
   constexpr int MAXN = CORIOLIS_F32_STEP * (MAXC + 1);
-  __shared__ float sVh[MAXN * MAXN], sVl[MAXN * MAXN];
+  __shared__ __align__(16) float sV[2 * MAXN * MAXN];
   __shared__ float Hd[MAXN], Ho[MAXN];
   __shared__ float red[CORIOLIS_THREADS / 32][2 * CORIOLIS_F32_MAXN];
   __shared__ int64_t base[MAXN];
@@ -245,7 +260,7 @@ __global__ void __launch_bounds__(CORIOLIS_THREADS) k_coriolis_f32(Grid g, float
 #define QD_BODY(C)                                                                                       \
   coriolis_f32_body<CORIOLIS_F32_STEP * ((C) + 1), EN>(g, psi_j, blocks, groups, Vh, Vl, phl, Hp, rotR, rotr, \
                                                        pro, epi, I1f, I2f, ce_part, re_part, tiles, ce_n, gid,  \
-                                                       sVh, sVl, Hd, Ho, red, base)
+                                                       sV, Hd, Ho, red, base)
   if (MAXC >= 5 && cls == 5) QD_BODY(MAXC >= 5 ? 5 : 0);
   else if (MAXC >= 4 && cls == 4) QD_BODY(MAXC >= 4 ? 4 : 0);
   else if (MAXC >= 3 && cls == 3) QD_BODY(MAXC >= 3 ? 3 : 0);
