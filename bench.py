@@ -389,18 +389,20 @@ def main():
     if args.accuracy:
         print(json.dumps({"accuracy": accuracy(qd, args.accuracy)}), flush=True)
         return
-    if args.workload:
-        line = workload_mode(qd, args.workload, 1 if args.precision == "mixed" else 0, args.steps, args.warmup)
-        if rank == 0:
-            print(json.dumps(line), flush=True)
-        return
+    prec = 1 if args.precision == "mixed" else 0
     if args.profile_steps:
-        d = qd.inputs.build_fh2data(qd.inputs.CONFIGS[WORKLOAD])
-        d["options"]["precision"] = 1 if args.precision == "mixed" else 0
-        with qd.Session(d) as s:
+        # a plain run of K steps (graphs and all) for an external profiler's launch list
+        ds = workload_problems(qd, args.workload or WORKLOAD, prec)
+        with qd.Session(ds) as s:
             s.run(args.profile_steps)
             s.synchronize()
-        print(json.dumps({"profile_steps": args.profile_steps, "precision": args.precision}), flush=True)
+        print(json.dumps({"profile_steps": args.profile_steps, "precision": args.precision,
+                          "workload": args.workload or WORKLOAD}), flush=True)
+        return
+    if args.workload:
+        line = workload_mode(qd, args.workload, prec, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
         return
     gpu_index = local
     if os.environ.get("CUDA_VISIBLE_DEVICES"):
