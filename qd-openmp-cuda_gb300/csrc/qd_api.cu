@@ -890,8 +890,12 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   s->t_modpe = s->precision == QD_PRECISION_MIXED ? legendre_tc_part_tiles(g) : legendre_bwd_part_tiles(g);
   s->t_ke = fft_col_tiles(s->fft, s->precision);
   // coupled: partials of the rotational-energy pass (or of the fused FP32 Coriolis)
-  s->t_re = s->any_coupled ? CORIOLIS_F32_TILES : fft_row_tiles(s->fft, s->precision);
-  s->t_ce = s->cor_f32 ? CORIOLIS_F32_TILES : coriolis_tiles(g);
+  // CTAs per group of the FP32 Coriolis passes: twice the base while the groups are few (one
+  // coupled problem has about l_max of them), the base for batched runs with thousands, where
+  // more tiles only add partial sums
+  const int cor_tiles = s->n_groups < CORIOLIS_F32_FEW_GROUPS ? 2 * CORIOLIS_F32_TILES : CORIOLIS_F32_TILES;
+  s->t_re = s->any_coupled ? (s->cor_f32 ? cor_tiles : CORIOLIS_F32_TILES) : fft_row_tiles(s->fft, s->precision);
+  s->t_ce = s->cor_f32 ? cor_tiles : coriolis_tiles(g);
   s->part_modpe = dalloc<double>((size_t)s->n_blocks * s->t_modpe * 2);
   s->part_ke = dalloc<double>((size_t)s->n_slabs * s->t_ke);
   s->part_re = dalloc<double>((size_t)s->n_slabs * s->t_re);

@@ -183,7 +183,8 @@ void launch_coriolis_n(cudaStream_t s, const Grid &g, S *psi_j, const BlockDesc 
 constexpr int CORIOLIS_F32_MAXN = 24;
 constexpr int CORIOLIS_F32_STEP = 4;     // size classes of at most 4, 8, ..., 24 blocks (one body each)
 constexpr int CORIOLIS_F32_CLASSES = 6;
-constexpr int CORIOLIS_F32_TILES = 16;   // CTAs per group (its partial tiles)
+constexpr int CORIOLIS_F32_TILES = 16;   // CTAs per group (its partial tiles), doubled below
+constexpr int CORIOLIS_F32_FEW_GROUPS = 512;   // ... this many groups
 int coriolis_f32_class(int n);           // size class of a group of n blocks, -1 above the limit
 // order: the group indices, largest groups first
 void launch_coriolis_f32(cudaStream_t s, const Grid &g, float2 *psi_j, const BlockDesc *blocks,
