@@ -217,6 +217,8 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_f32(int64_t ns2, int 
   float2 a[FLUX_EB32];
 #pragma unroll
   for (int e = 0; e < FLUX_EB32; e++) a[e] = make_float2(0.0f, 0.0f);
+  // unrolled so that several steps' surface values are loaded ahead of their use
+#pragma unroll 4
   for (int n = 0; n < count; n++) {
     const float2 vd = buf[((int64_t)n * n_blocks + b) * ns2 + s];
     const float vx = vd.x, vy = vd.y;
