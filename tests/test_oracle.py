@@ -46,11 +46,12 @@ def test_legendre_orthonormal_and_round_trip(qd):
     assert abs(s2 - s1) < 1e-12 * s1
 
 
-@pytest.mark.parametrize("J,p", [(1, 0), (1, 1), (4, 1), (12, 0), (7, 1)])
+@pytest.mark.parametrize("J,p", [(1, 0), (1, 1), (4, 1), (12, 0), (7, 1), (28, 0), (40, 0)])
 def test_coriolis_matrix_exponential(oracle, J, p):
     """U = sum_a exp(-i dt e_a/I) V V^T equals expm(-i dt H / I) (evolutionCUDAaux.cu:178-209),
-    V diag(e) V^T reconstructs H (evolutionCUDAaux.cu:114-128) and U is unitary."""
-    for l in range((J + p) % 2, 15):
+    V diag(e) V^T reconstructs H (evolutionCUDAaux.cu:114-128) and U is unitary; J = 28 and 40
+    reach the 29- and 41-block groups of the large-group GPU cases."""
+    for l in range((J + p) % 2, max(15, J + 6)):
         omin, omax, d, e = oracle.coriolis_matrix(J, p, l)
         H = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
         _, _, ev, V = oracle.coriolis_eigen(J, p, l)
