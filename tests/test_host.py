@@ -71,3 +71,23 @@ def test_output_arrays_must_be_writable_in_place(qd, lib):
     d["OmegaStates"]["wave_packets"] = d["OmegaStates"]["wave_packets"].astype(np.complex64)
     with pytest.raises(qd.QDError):
         qd.cudaOpenMPEvolution(d)
+
+
+def test_bench_algorithmic_bytes_of_the_headline(qd):
+    """The roofline numerator: algorithmic bytes per launch at 256x128x96, J=0, mixed form
+    (8 B per c64 value of psi; forward reads psi_theta and the potential's shear pair and
+    writes psi_l, backward reads psi_l and w V and writes psi_theta, the slab FFT reads and
+    writes every psi_l value once)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("bench", Path(__file__).resolve().parents[1] / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    d = qd.inputs.build_fh2data(qd.inputs.CONFIGS["fh2_j0_256x128x96"])
+    d["options"]["precision"] = 1
+    npt, nth, nl = 256 * 128, 96, 96
+    assert bench.algorithmic("legendre_forward", d) == ("hbm", 8.0 * npt * (nth + nth + nl), "GB/s")
+    assert bench.algorithmic("legendre_backward", d) == ("hbm", npt * (8.0 * nl + 8.0 * nth + 4.0 * nth), "GB/s")
+    assert bench.algorithmic("fft_slab", d) == ("hbm", 50_331_648.0, "GB/s")
+    assert bench.algorithmic("legendre_forward", d)[1] == 75_497_472.0
+    assert bench.algorithmic("legendre_backward", d)[1] == 62_914_560.0
