@@ -283,7 +283,7 @@ def e2e(qd, precision: int, steps: int):
                     "K steps, D2H of psi and P(E); bytes are per step over the call"}
 
 
-def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 1):
+def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 3):
     cfg = qd.inputs.CONFIGS[WORKLOAD]
     d = qd.inputs.build_fh2data(cfg)
     o = oracle.Oracle(d)
@@ -296,7 +296,7 @@ def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 1):
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     return {"value": n_steps * len(o.omegas) / sec, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{n_steps} FP64 oracle steps (numpy/scipy, pocketfft + OpenBLAS) of the "
-                      f"{WORKLOAD} workload after {warm} warm-up step"}
+                      f"{WORKLOAD} workload after {warm} warm-up step{'s' if warm != 1 else ''}"}
 
 
 def accuracy(qd, total: int, checkpoints=(10, 40, 160, 640, 2560, 10240, 20000)):
@@ -343,10 +343,13 @@ def reference_arm(args, world, rank):
         return
     qd = entry.load_package()
     oracle = entry.load_oracle()
+    # bounded sample: at most 10 timed oracle steps (about 0.4 s each on 16 Grace cores) after
+    # at least 3 warm-up steps
     n = max(1, min(args.steps, 10))
-    cb = cpu_baseline(qd, oracle, n_steps=n, warm=min(args.warmup, 1))
+    warm = max(3, min(args.warmup, 8))
+    cb = cpu_baseline(qd, oracle, n_steps=n, warm=warm)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 / cb["value"],
+            "steps": n, "warmup": warm, "ms_per_step": 1e3 / cb["value"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (c128)",
             "data": "synthetic (LEPS F+H2, seeded/deterministic)",
             "config": {"workload": WORKLOAD, "grid": [256, 128, 96], "l_max": 95, "J": 0, "dt": 10.0,
