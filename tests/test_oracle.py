@@ -90,6 +90,40 @@ def test_fft_stage_is_the_unnormalised_dft(qd, oracle):
     np.testing.assert_allclose(o.lpsi[0], x, atol=1e-13)
 
 
+def _free_gaussian(x, x0, sig, k0, m, t):
+    """Closed-form free-particle solution (hbar = 1) from exp(-(x-x0)^2/(4 sig^2) + i k0 x)."""
+    a = 1 + 1j * t / (2 * m * sig ** 2)
+    v = k0 / m
+    return a ** -0.5 * np.exp(-(x - x0 - v * t) ** 2 / (4 * sig ** 2 * a)) * np.exp(1j * k0 * (x - v * t / 2))
+
+
+def test_kinetic_stage_is_the_free_particle_propagator(qd, oracle):
+    """Known answer for forward FFT + _evolution_with_kinetic_ + inverse FFT (evolutionCUDAaux.cu:13-31):
+    a Gaussian packet (width L/24, momentum 0.3/dr in R and r) propagates as the closed-form
+    free particle of masses m1, m2 (to 1e-12 at t = 50, before it reaches the periodic edge), and
+    the kinetic-energy sum (omegawavepacket.cu:364-395) equals (k0^2 + 1/(4 sigma^2))/(2m) per
+    coordinate times the norm."""
+    cfg = qd.inputs.small_config(J=0, n1=128, n2=64, n_theta=6, l_max=5, steps=1)
+    o = oracle.Oracle(qd.inputs.build_fh2data(cfg))
+    LR, Lr = o.n1 * o.dr1, o.n2 * o.dr2
+    sR, sr, kR, kr = LR / 24, Lr / 24, 0.3 / o.dr1, 0.3 / o.dr2
+    x0R, x0r = o.R[0] + 0.45 * LR, o.r[0] + 0.45 * Lr
+
+    def packet(t):
+        return np.outer(_free_gaussian(o.r, x0r, sr, kr, o.m2, t), _free_gaussian(o.R, x0R, sR, kR, o.m1, t))
+
+    psi0 = packet(0.0)
+    o.lpsi[0][...] = 0
+    o.lpsi[0][0] = psi0
+    o.forward_fft()
+    norm = np.sum(np.abs(psi0) ** 2) * o.dr1 * o.dr2
+    ke = norm * ((kR ** 2 + 1 / (4 * sR ** 2)) / (2 * o.m1) + (kr ** 2 + 1 / (4 * sr ** 2)) / (2 * o.m2))
+    np.testing.assert_allclose(o.kinetic_energy()[0], ke, rtol=1e-12)
+    o.evolution_with_kinetic(50.0)
+    o.backward_fft()
+    assert np.abs(o.lpsi[0][0] - packet(50.0)).max() < 1e-12
+
+
 @pytest.mark.parametrize("J,p", [(0, 0), (2, 0), (3, 1)])
 def test_norm_conserved_without_mask(qd, oracle, J, p):
     """Without the absorbing mask every factor is unitary: the module stays 1."""
