@@ -156,7 +156,7 @@ def peaks():
 
 def read_traffic():
     """Per-launch DRAM bytes from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / "dram_traffic.txt"
+    f = ROOT / "profiles" / "dram_traffic_mixed_256x128x96.txt"
     out = {}
     if f.exists():
         for line in f.read_text().splitlines():
