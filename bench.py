@@ -8,6 +8,8 @@ Contract (one JSON line on rank 0):
                device set-up inside the timed region (the reference's own timing
                hook: tic/toc around the MEX call, FH2main.m:212-215)
   fp64       = the plain FP64 form on the same GPU, and the mixed/FP64 ratio
+  accuracy_gate = max |P_mixed(E) - P_fp64(E)| in the packet's energy window
+               after 2000 steps of both forms on this GPU (gate 1e-4)
   roofline   = dominant kernel of the mixed form, per-launch CUDA-event time
   cpu_baseline = the FP64 numpy oracle on the host cores (bounded sample)
 
@@ -169,7 +171,17 @@ def read_traffic():
     return out
 
 
-def run_form(qd, precision: int, steps: int, warmup: int, sampler=None):
+def flux_flushes(steps: int, chunk: int = 64) -> int:
+    """Flux-transform flushes inside a timed region of ``steps`` steps that starts with no
+    buffered surface values and ends with Session.flush(): one per whole 64-step graph
+    chunk, plus one for the remainder."""
+    return steps // chunk + (1 if steps % chunk else 0)
+
+
+def run_form(qd, precision: int, steps: int, warmup: int):
+    """Device-resident steps of one form: ``warmup`` untimed steps (their flux work flushed),
+    then CUDA events on the session stream around exactly ``steps`` steps and the flux
+    transform of those steps (Session.flush() inside the timed region)."""
     import torch
 
     cfg = qd.inputs.CONFIGS[WORKLOAD]
@@ -178,30 +190,26 @@ def run_form(qd, precision: int, steps: int, warmup: int, sampler=None):
     with qd.Session(d) as s:
         stream = torch.cuda.ExternalStream(s.stream())
         s.run(warmup)
+        s.flush()
         s.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         if torch.distributed.is_initialized():
             torch.distributed.barrier()
         torch.cuda.synchronize()
-        if sampler:
-            sampler.start()
         e0.record(stream)
         s.run(steps)
+        s.flush()
         e1.record(stream)
         e1.synchronize()
         s.synchronize()
-        if sampler:
-            clocks = sampler.stop()
-        else:
-            clocks = None
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         ms = max_over_ranks(ms)
         prof = s.profile(64)
         psi = s.get_psi("theta", 0)
         return {"ms": ms, "n_blocks": s.n_blocks, "launches_per_step": s.launches_per_step, "profile": prof,
-                "clocks": clocks, "psi": psi, "d": d}
+                "psi": psi, "d": d}
 
 
 OTHER_WORKLOADS = ("fh2_j12_256x128x96", "fh2_batched_j0-40_192x96x80")
@@ -226,12 +234,14 @@ def workload_mode(qd, name: str, precision: int, steps: int, warmup: int):
     with qd.Session(ds) as s:
         stream = torch.cuda.ExternalStream(s.stream())
         s.run(warmup)
+        s.flush()
         s.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
         s.run(steps)
+        s.flush()
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
@@ -248,7 +258,9 @@ def workload_mode(qd, name: str, precision: int, steps: int, warmup: int):
 
 
 def e2e(qd, precision: int, steps: int):
-    """K steps through cudaOpenMPEvolution with pinned host buffers."""
+    """K steps through cudaOpenMPEvolution (qd_evolve) with pinned host buffers: the H2D
+    copies of psi, pot and the Legendre matrices, device set-up, K steps with their flux
+    work, and the D2H copies of psi and P(E) are all inside the timed region."""
     import torch
 
     cfg = qd.inputs.CONFIGS[WORKLOAD]
@@ -264,11 +276,14 @@ def e2e(qd, precision: int, steps: int):
         return out, t
 
     keep = []
-    wp, t1 = pinned(d["OmegaStates"]["wave_packets"])
-    pot, t2 = pinned(d["pot"])
-    keep += [t1, t2]
-    d["OmegaStates"]["wave_packets"] = wp
+    for key in ("wave_packets", "associated_legendres"):
+        arr, t = pinned(d["OmegaStates"][key])
+        keep.append(t)
+        d["OmegaStates"][key] = arr
+    pot, t = pinned(d["pot"])
+    keep.append(t)
     d["pot"] = pot
+    wp = d["OmegaStates"]["wave_packets"]
     h2d = wp.nbytes + pot.nbytes + d["OmegaStates"]["associated_legendres"].nbytes
     d2h = wp.nbytes + d["CRP"]["CRP"].nbytes
     torch.cuda.synchronize()
@@ -279,8 +294,37 @@ def e2e(qd, precision: int, steps: int):
     nb = len(np.ravel(d["OmegaStates"]["omegas"]))
     return {"value": steps * nb / sec, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
             "d2h_bytes_per_step": d2h / steps, "seconds": sec, "steps": steps,
+            "precision": "mixed" if precision else "fp64",
             "note": "one qd_evolve call of K steps: H2D of psi/pot/Legendre matrices, table build, "
-                    "K steps, D2H of psi and P(E); bytes are per step over the call"}
+                    "K steps with their flux transform, D2H of psi and P(E); bytes are per step over the call"}
+
+
+def pe_gate(qd, steps: int):
+    """The mixed form's accuracy gate on the bench workload: both forms run ``steps`` steps
+    on this GPU from the same inputs (qd_evolve); max |P_mixed(E) - P_fp64(E)| over the
+    initial packet's energy window, relative |dpsi|_2 and the largest module difference
+    over all steps."""
+    cfg = qd.inputs.CONFIGS[WORKLOAD]
+    out = {}
+    t0 = time.perf_counter()
+    for prec in (0, 1):
+        d = qd.inputs.build_fh2data(cfg)
+        d["options"]["precision"] = prec
+        d["time"]["total_steps"] = steps
+        nb = len(np.ravel(d["OmegaStates"]["omegas"]))
+        d["options"]["energies"] = np.zeros((steps, nb, 6))
+        qd.cudaOpenMPEvolution(d)
+        out[prec] = d
+    win = qd.inputs.energy_window(out[0]["CRP"]["eta_sq"])
+    pf, pm = out[0]["CRP"]["CRP"], out[1]["CRP"]["CRP"]
+    a, b = out[1]["OmegaStates"]["wave_packets"], out[0]["OmegaStates"]["wave_packets"]
+    mod = np.abs(out[1]["options"]["energies"][:, :, 0].sum(1) - out[0]["options"]["energies"][:, :, 0].sum(1))
+    dp = float(np.max(np.abs(pm - pf)[win]))
+    return {"steps": steps, "max_abs_dP_window": dp, "gate": 1e-4, "passed": bool(dp <= 1e-4),
+            "max_P_fp64_window": float(np.max(np.abs(pf[win]))), "n_energies_window": int(win.sum()),
+            "rel_dpsi": float(np.linalg.norm(a - b) / np.linalg.norm(b)), "max_dmodule": float(mod.max()),
+            "seconds": round(time.perf_counter() - t0, 2),
+            "note": "mixed vs FP64 form of this library on this GPU, same inputs, qd_evolve"}
 
 
 def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 3):
@@ -374,6 +418,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--workload", default="", choices=("",) + OTHER_WORKLOADS,
                     help="time a secondary configuration (--precision) instead of the headline benchmark")
+    ap.add_argument("--gate-steps", type=int, default=2000,
+                    help="steps of the in-line mixed-vs-FP64 P(E) gate (0 skips it)")
     ap.add_argument("--accuracy", type=int, default=0,
                     help="run the mixed-vs-FP64 accuracy study for this many steps instead of the benchmark")
     args = ap.parse_args()
@@ -413,8 +459,15 @@ def main():
         if local < len(vis) and vis[local].strip().isdigit():
             gpu_index = int(vis[local])
     fp64_peak, fp32_peak = qd.fma_peaks()
-    mixed = run_form(qd, 1, args.steps, args.warmup, ClockSampler(gpu_index))
+    # clocks sampled from before the mixed form's warm-up until after the FP64 leg and the
+    # accuracy gate: the timed regions themselves are milliseconds long at small --steps
+    sampler = ClockSampler(gpu_index)
+    sampler.start()
+    mixed = run_form(qd, 1, args.steps, args.warmup)
     fp64 = run_form(qd, 0, args.steps, args.warmup)
+    gate = pe_gate(qd, args.gate_steps) if rank == 0 and args.gate_steps > 0 else None
+    clocks = sampler.stop()
+    clocks["window"] = "sampled every 100 ms from the mixed warm-up through the FP64 leg and the accuracy gate"
     nb = mixed["n_blocks"]
     value = replica_throughput(mixed["ms"], args.steps, nb)
     fp64_value = replica_throughput(fp64["ms"], args.steps, nb)
@@ -441,6 +494,7 @@ def main():
     fdom = max(fp64_prof, key=lambda k: fp64_prof[k]["ms"] * fp64_prof[k]["per_step"])
     fb, fa, fu = algorithmic(fdom, fp64["d"])
     fach = fa / (fp64_prof[fdom]["ms"] * 1e-3) / (1e12 if fu == "TFLOP/s" else 1e9)
+    flushes = flux_flushes(args.steps)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
@@ -449,24 +503,33 @@ def main():
         "data": "synthetic (LEPS F+H2, deterministic inputs built on the host)",
         "config": {"workload": WORKLOAD, "grid": [256, 128, 96], "l_max": 95, "J": 0, "omega_blocks": nb,
                    "dt": 10.0, "n_energies": 400, "flux": True, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2: each timed 64-step graph launch reads and writes ~0.45 GB "
-                         "(psi, tables, 315 MB of flux accumulators) > 129 MB L2; inside it each step (~90 MB) "
-                         "reads what the step before wrote, as in production; no flush between steps"},
+                   "timed": f"{args.steps} steps and the flux transform of exactly those steps "
+                            f"({flushes} flush{'es' if flushes != 1 else ''}: one per whole 64-step graph "
+                            f"chunk, one for the remainder); the warm-up's flux work is flushed before",
+                   "l2": "inputs larger than L2: a step reads and writes psi in both spaces, the V shear "
+                         "table and w V (~90 MB), and each flux flush the 315 MB of FP64 accumulators, "
+                         "so the working set (~0.45 GB) exceeds the 129 MB L2; each step reads what the "
+                         "step before it wrote, as in production; no flush between steps"},
         "fp64": {"value": fp64_value, "ms_per_step": fp64["ms"] / args.steps,
                  "dominant_kernel": fdom, "dominant_achieved": fach, "dominant_unit": fu,
                  "fp64_fma_peak_tflops": fp64_peak},
         "mixed_over_fp64": value / fp64_value,
         "mixed_rel_dpsi_vs_fp64": dpsi, "accuracy_steps": steps_done,
+        "accuracy_gate": gate,
         "roofline": {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "peak_source": psrc,
                      "unit": unit, "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch from the ncu "
+                                       "capture summarised in profiles/dram_traffic_mixed_256x128x96.txt "
+                                       "(a separate run of the same kernel and workload, not this one)",
                      "algorithmic_per_launch": amount},
         "kernels": kernels,
-        "gpu_launches": mixed["launches_per_step"] * args.steps + 3 * (args.steps // 64),
-        "clocks": mixed["clocks"],
+        "gpu_launches": mixed["launches_per_step"] * args.steps + 3 * flushes,
+        "clocks": clocks,
         "measured_fma_tflops": {"fp64": fp64_peak, "fp32": fp32_peak},
     }
     if rank == 0:
         line["e2e"] = e2e(qd, 1, args.steps)
+        line["fp64"]["e2e"] = e2e(qd, 0, args.steps)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(qd, entry.load_oracle())
         print(json.dumps(line), flush=True)

@@ -36,7 +36,9 @@ typedef enum qd_status {
   QD_ERR_NORM = 4,        /* norm guard: total module > 1 (cudaOpenMP2.cu:437-440) */
   QD_ERR_CALLBACK = 5,    /* the wave_to_matlab callback returned non-zero */
   QD_ERR_UNSUPPORTED = 6, /* valid input the library does not handle (e.g. odd FFT grid) */
-  QD_ERR_NO_DEVICE = 7    /* no CUDA device, or not an sm_103 device */
+  QD_ERR_NO_DEVICE = 7,   /* no CUDA device, or not an sm_103 device */
+  QD_ERR_TIMEOUT = 8      /* a bounded device-side wait gave up (a kernel's
+                             pipeline stalled); the context stays usable */
 } qd_status;
 
 typedef enum qd_precision {
@@ -179,6 +181,11 @@ int qd_session_destroy(qd_session *s);
 /* enqueue n_steps full time steps on the session stream (no host sync) */
 int qd_session_run(qd_session *s, int32_t n_steps);
 int qd_session_synchronize(qd_session *s);
+/* enqueue the time-to-energy transform of the flux surface values buffered by
+   the steps run so far (it otherwise runs once per 64 steps, and before any
+   download), so that a timed region can hold exactly its own steps' flux work;
+   no host sync.  A no-op without CRP.calculate_CRP or with nothing buffered. */
+int qd_session_flush(qd_session *s);
 /* copy psi (theta space), time.steps, CRP and energies back into the structs */
 int qd_session_download(qd_session *s, qd_fh2data *const *problems, int32_t n_problems);
 /* upload psi (theta space) from the structs again */
@@ -228,9 +235,10 @@ int qd_session_get_energies(qd_session *s, double *host_out, size_t n_doubles);
    library (every GPU that loads the library holds it until exit), so
    l_max - omega + 1 may be at most 4096; larger values return QD_ERR_INVALID.
    All calls share that array, so calls that overlap on the GPU (on different
-   streams, or on different host threads) race.  The first call on each device
-   looks up the array's device address with that device current; make that
-   first call before any stream capture. */
+   streams, or on different host threads) race.  Every call looks up the
+   array's device address in the current device's context (no allocation); the
+   first call on a device may also load the library's device code, so make it
+   before any stream capture. */
 int qd_rotational_energy_noalloc(const double *psi_j, int32_t n1, int32_t n2, int32_t omega, int32_t l_max,
                                  double r1_left, double r1_dr, double r1_mass, double r2_left, double r2_dr,
                                  double r2_mass, double *rotational_energy, void *stream);
@@ -243,6 +251,14 @@ int qd_rotational_energy_noalloc(const double *psi_j, int32_t n1, int32_t n2, in
    names receives the kernel names separated by '\n'. */
 int qd_session_profile(qd_session *s, int32_t n_steps, char *names, size_t names_cap, double *avg_ms,
                        int32_t *launches, int32_t max_kernels, int32_t *n_kernels);
+
+/* Self-test of the bounded device-side wait that every pipelined kernel of the
+   library uses: one CTA waits on an mbarrier with a budget of budget_ms.  With
+   arrive = 0 nothing ever arrives, the wait gives up after the budget and the
+   call returns QD_ERR_TIMEOUT (the device status word the kernels set); with
+   arrive = 1 a second thread arrives and the call returns QD_OK.  Either way
+   the kernel ends and the context stays usable. */
+int qd_device_wait_selftest(double budget_ms, int32_t arrive);
 
 /* Measured FP64 fused-multiply-add throughput of the current device
    (TFLOP/s, 2 flops per FMA) from a register-resident DFMA loop, and the

@@ -173,7 +173,10 @@ class Oracle:
 
     def evolution_with_potential(self, dt):
         """``_evolution_with_potential_`` (evolutionCUDAaux.cu:5-11)."""
-        ph = np.exp(-1j * dt * self.pot)
+        cache = self.__dict__.setdefault("_pot_cache", {})
+        if float(dt) not in cache:
+            cache[float(dt)] = np.exp(-1j * dt * self.pot)
+        ph = cache[float(dt)]
         for b in range(len(self.psi)):
             self.psi[b] *= ph
 
@@ -192,10 +195,15 @@ class Oracle:
             self.psi[b] = (self.P[b] @ C).reshape(self.nth, self.n2, self.n1)
 
     def rot_phase(self, omega, dt):
-        l = np.arange(omega, self.l_max + 1, dtype=np.float64)
-        ll = l * (l + 1.0)
-        I = self.I2[:, None] + self.I1[None, :]
-        return np.exp(-1j * dt * ll[:, None, None] * I[None, :, :])
+        """exp(-i dt l(l+1) (1/(2 m1 R^2) + 1/(2 m2 r^2))) for l = omega..l_max, cached per (omega, dt)."""
+        key = (int(omega), float(dt))
+        cache = self.__dict__.setdefault("_rot_cache", {})
+        if key not in cache:
+            l = np.arange(omega, self.l_max + 1, dtype=np.float64)
+            ll = l * (l + 1.0)
+            I = self.I2[:, None] + self.I1[None, :]
+            cache[key] = np.exp(-1j * dt * ll[:, None, None] * I[None, :, :])
+        return cache[key]
 
     def evolution_with_rotational(self, dt):
         """``_evolution_with_rotational_`` (evolutionCUDAaux.cu:33-54)."""
@@ -229,24 +237,27 @@ class Oracle:
     def evolution_with_coriolis(self, dt, calculate_energy=False):
         """Coriolis half step (cudaOpenMP2.cu:392-423, wavepackets1device.cu:485-495,
         omegawavepacket.cu:430-489).  The coupling energy is evaluated on the
-        pre-update psi (omegawavepacket.cu:503-553 runs before the D2D update)."""
+        pre-update psi (omegawavepacket.cu:503-553 runs before the D2D update).
+        Per l, the blocks present in the l-matrix are stacked and updated together:
+        psi'[Omega](R, r) = sum_Omega1 U_{Omega Omega1}(R) psi[Omega1](R, r)."""
         nb = len(self.omegas)
         if calculate_energy:
+            # sum over pairs |Omega - Omega1| <= 1, weight 2 off the diagonal
+            # (wavepackets1device.cu:515-530); H_{Omega Omega1} = sum_a e_a V V / (2 m1 R^2)
             ce = np.zeros(nb)
-            for i in range(nb):
-                for j in range(i, nb):
-                    oi, oj = self.omegas[i], self.omegas[j]
-                    if abs(oi - oj) > 1:
-                        continue
-                    for l in range(max(oi, oj), self.l_max + 1):
-                        omin, omax, ev, V = self.cor[l]
-                        if oi > omax or oj > omax:
+            inv2mR2 = 1.0 / (2.0 * self.m1 * self.R ** 2)
+            for l in range(self.omegas[0], self.l_max + 1):
+                omin, omax, ev, V = self.cor[l]
+                present = [b for b, o in enumerate(self.omegas) if o <= l and omin <= o <= omax]
+                for i in present:
+                    for j in present:
+                        oi, oj = self.omegas[i], self.omegas[j]
+                        if oj < oi or oj - oi > 1:
                             continue
                         h = np.sum(ev * V[oi - omin] * V[oj - omin])
-                        cR = h / (2.0 * self.m1 * self.R ** 2)
                         a = self.lpsi[i][l - oi]
                         bb = self.lpsi[j][l - oj]
-                        dot = np.sum(np.conj(a) * cR[None, :] * bb)
+                        dot = np.vdot(a * inv2mR2[None, :], bb) * h
                         if oi != oj:
                             dot *= 2.0
                         ce[i] += dot.real * self.dr1 * self.dr2
@@ -257,14 +268,13 @@ class Oracle:
             present = [b for b, o in enumerate(self.omegas) if o <= l and omin <= o <= omax]
             if not present:
                 continue
-            U = self.coriolis_factors(l, dt)
-            for b in present:
-                ob = self.omegas[b]
-                acc = np.zeros((self.n2, self.n1), np.complex128)
-                for b1 in present:
-                    o1 = self.omegas[b1]
-                    acc += U[ob - omin, o1 - omin][None, :] * self.lpsi[b1][l - o1]
-                new[b][l - ob] = acc
+            U = self.coriolis_factors(l, dt)                          # (n, n, n1)
+            idx = [self.omegas[b] - omin for b in present]
+            Us = U[np.ix_(idx, idx)]                                  # (m, m, n1)
+            S = np.stack([self.lpsi[b][l - self.omegas[b]] for b in present])   # (m, n2, n1)
+            out = np.einsum("pqi,qji->pji", Us, S, optimize=True)
+            for k, b in enumerate(present):
+                new[b][l - self.omegas[b]] = out[k]
         self.lpsi = new
 
     # ------------------------------------------------------------- energies
@@ -299,23 +309,39 @@ class Oracle:
         """Energy-resolved flux through r = r_s (the reference parses CRP but has
         no flux code; this is the project's own definition).  psi(t_{n+1}) on the
         stencil rows is exp(-i V dt/2) psi_theta; A_E += dt e^{iEt} psi(R, r_s, x_k),
-        D_E += dt e^{iEt} d_r psi(R, r_s, x_k) with a centred FD stencil."""
+        D_E += dt e^{iEt} d_r psi(R, r_s, x_k) with a centred FD stencil.  The
+        surface values are buffered and added to the accumulators as one
+        (energies x steps) @ (steps x points) product every 32 steps."""
         if not self.flux_on:
             return
-        t = (self.steps + 1) * self.dt
-        ph = self.dt * np.exp(1j * self.E * t)                           # (nE,)
         h = (self.n_g - 1) // 2
+        surf = []
         for b in range(len(self.psi)):
             s = self.half_v * self.psi[b][:, self.rows, :]              # (nθ, n_g, n1)
-            A = s[:, h, :]
-            D = np.einsum("g,kgi->ki", self.fd, s)
-            self.accA[b] += ph[:, None, None] * A[None]
-            self.accD[b] += ph[:, None, None] * D[None]
+            surf.append((s[:, h, :], np.einsum("g,kgi->ki", self.fd, s)))
+        buf = self.__dict__.setdefault("_flux_buf", [])
+        buf.append(((self.steps + 1) * self.dt, surf))
+        if len(buf) >= 32:
+            self._flush_flux()
+
+    def _flush_flux(self):
+        buf = self.__dict__.get("_flux_buf", [])
+        if not buf:
+            return
+        t = np.array([x[0] for x in buf])
+        ph = self.dt * np.exp(1j * self.E[:, None] * t[None, :])         # (nE, n_steps)
+        for b in range(len(self.psi)):
+            A = np.stack([x[1][b][0] for x in buf]).reshape(len(buf), -1)
+            D = np.stack([x[1][b][1] for x in buf]).reshape(len(buf), -1)
+            self.accA[b] += (ph @ A).reshape(self.accA[b].shape)
+            self.accD[b] += (ph @ D).reshape(self.accD[b].shape)
+        buf.clear()
 
     def crp(self):
         """P(E) = Im sum_{Omega,k,i} w_k dR conj(A_E) D_E / (2 pi mu_r eta^2(E))."""
         if not self.flux_on:
             return None
+        self._flush_flux()
         s = np.einsum("k,beki->e", self.w, np.conj(self.accA) * self.accD) * self.dr1
         return s.imag / (2.0 * math.pi * self.m2 * self.eta_sq)
 

@@ -28,7 +28,7 @@ LIB_PATH = HERE / "libqd.so"
 
 QD_OK = 0
 STATUS_NAMES = {0: "QD_OK", 1: "QD_ERR_INVALID", 2: "QD_ERR_CUDA", 3: "QD_ERR_NOMEM", 4: "QD_ERR_NORM",
-                5: "QD_ERR_CALLBACK", 6: "QD_ERR_UNSUPPORTED", 7: "QD_ERR_NO_DEVICE"}
+                5: "QD_ERR_CALLBACK", 6: "QD_ERR_UNSUPPORTED", 7: "QD_ERR_NO_DEVICE", 8: "QD_ERR_TIMEOUT"}
 PRECISION = {"fp64": 0, "mixed": 1}
 STAGES = {"dump": 0, "potential": 1, "forward_legendre": 2, "backward_legendre": 3, "rotational": 4,
           "coriolis": 5, "coriolis_energy": 6, "fft_kinetic": 7, "energies": 8, "flux": 9}
@@ -93,9 +93,10 @@ CALLBACK = C.CFUNCTYPE(C.c_int, C.POINTER(FH2Data), C.c_void_p)
 _lib = None
 
 EXPORTED = ("qd_evolve", "qd_evolve_batch", "qd_last_error", "qd_version", "qd_session_create",
-            "qd_session_destroy", "qd_session_run", "qd_session_synchronize", "qd_session_download",
+            "qd_session_destroy", "qd_session_run", "qd_session_synchronize", "qd_session_flush", "qd_session_download",
             "qd_session_upload", "qd_session_stream", "qd_session_info", "qd_session_apply", "qd_session_get_psi",
             "qd_session_set_psi", "qd_session_get_energies", "qd_session_profile", "qd_device_fma_peaks",
+            "qd_device_wait_selftest",
             "qd_rotational_energy_noalloc")
 
 
@@ -121,6 +122,7 @@ def load_library():
     lib.qd_session_destroy.argtypes = [C.c_void_p]
     lib.qd_session_run.argtypes = [C.c_void_p, C.c_int32]
     lib.qd_session_synchronize.argtypes = [C.c_void_p]
+    lib.qd_session_flush.argtypes = [C.c_void_p]
     lib.qd_session_download.argtypes = [C.c_void_p, P(P(FH2Data)), C.c_int32]
     lib.qd_session_upload.argtypes = [C.c_void_p, P(P(FH2Data)), C.c_int32]
     lib.qd_session_stream.argtypes = [C.c_void_p]
@@ -133,6 +135,7 @@ def load_library():
     lib.qd_session_profile.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t, P(C.c_double),
                                        P(C.c_int32), C.c_int32, P(C.c_int32)]
     lib.qd_device_fma_peaks.argtypes = [P(C.c_double), P(C.c_double)]
+    lib.qd_device_wait_selftest.argtypes = [C.c_double, C.c_int32]
     lib.qd_rotational_energy_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                                  C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                                  C.c_double, C.c_void_p, C.c_void_p]
@@ -323,6 +326,10 @@ class Session:
     def synchronize(self):
         _check(self.lib.qd_session_synchronize(self.h))
 
+    def flush(self):
+        """Enqueue the flux transform of the steps buffered so far (no host sync)."""
+        _check(self.lib.qd_session_flush(self.h))
+
     def download(self):
         _check(self.lib.qd_session_download(self.h, self.arr, len(self.ms)))
         for m in self.ms:
@@ -374,6 +381,13 @@ def fma_peaks() -> tuple:
     a, b = C.c_double(), C.c_double()
     _check(lib.qd_device_fma_peaks(C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+def device_wait_selftest(budget_ms: float, arrive: bool) -> None:
+    """Run the bounded-wait self-test (qd_device_wait_selftest); raises QDError
+    (status QD_ERR_TIMEOUT) when the wait gave up."""
+    lib = load_library()
+    _check(lib.qd_device_wait_selftest(float(budget_ms), 1 if arrive else 0))
 
 
 def build(force: bool = False) -> Path:

@@ -1,6 +1,10 @@
 // Diagnostics: a register-resident FMA loop to measure the device's FP64 and
-// FP32 FMA throughput (the denominators of the FP64 roofline fractions).
+// FP32 FMA throughput (the denominators of the FP64 roofline fractions), and a
+// self-test of the bounded mbarrier wait used by the pipelined kernels.
+#include <string>
+
 #include "qd_internal.h"
+#include "qd_mbarrier.cuh"
 
 namespace qd {
 
@@ -42,5 +46,52 @@ static double measure(int iters) {
 
 double measure_fp64_tflops() { return measure<double>(20000); }
 double measure_fp32_tflops() { return measure<float>(400000); }
+
+// Thread 0 waits (bounded) on a fresh mbarrier of count 1; thread 1 arrives on
+// it only when `arrive` is set.  A wait that gives up records QD_ERR_TIMEOUT,
+// exactly as the tensor-core kernels do.
+__global__ void k_wait_selftest(uint64_t budget_ns, int arrive, int *status, unsigned long long *elapsed_ns) {
+  __shared__ uint64_t mb;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&mb), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 1 && arrive) mbar_arrive(smem_u32(&mb));
+  if (threadIdx.x == 0) {
+    const uint64_t t0 = globaltimer();
+    const bool ok = mbar_wait_bounded(smem_u32(&mb), 0u, budget_ns);
+    *elapsed_ns = globaltimer() - t0;
+    if (!ok) atomicCAS(status, 0, QD_ERR_TIMEOUT);
+  }
+}
+
+void device_wait_selftest(double budget_ms, int arrive) {
+  QD_REQUIRE(budget_ms > 0.0 && budget_ms <= 2000.0, "0 < budget_ms <= 2000");
+  int *status = nullptr;
+  unsigned long long *elapsed = nullptr;
+  QD_CUDA(cudaMalloc(&status, sizeof(int)));
+  cudaError_t e = cudaMalloc(&elapsed, sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    cudaFree(status);
+    QD_CUDA(e);
+  }
+  int st = 0;
+  unsigned long long ns = 0;
+  e = cudaMemset(status, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    k_wait_selftest<<<1, 32>>>((uint64_t)(budget_ms * 1e6), arrive ? 1 : 0, status, elapsed);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&st, status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&ns, elapsed, sizeof(ns), cudaMemcpyDeviceToHost);
+  cudaFree(status);
+  cudaFree(elapsed);
+  QD_CUDA(e);
+  if (st)
+    throw Error{st, "device wait gave up after " + std::to_string(ns * 1e-6) + " ms (budget " +
+                        std::to_string(budget_ms) + " ms)"};
+}
 
 }  // namespace qd

@@ -35,20 +35,12 @@
 
 #include "qd_internal.h"
 #include "qd_device.cuh"
+#include "qd_mbarrier.cuh"
 
 namespace qd {
 
 namespace {
 constexpr int TC_POINTS = 64;        // 128 real rows
-constexpr uint64_t WAIT_NS = 1000000000ull;   // give up waiting for the MMA chain after 1 s
-
-__device__ inline uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ inline uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // SWIZZLE_NONE, K-major shared-memory matrix descriptor (tcgen05 form):
 // start address, leading byte offset (between core matrices along K), stride
@@ -65,21 +57,6 @@ __device__ inline uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major.
 __host__ __device__ inline uint32_t make_idesc(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ inline void mbar_init(uint32_t a, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
-}
-__device__ inline bool mbar_try_wait(uint32_t a, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(a), "r"(parity)
-      : "memory");
-  return ok != 0;
 }
 
 __device__ inline void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -226,19 +203,10 @@ __device__ inline void rot_lift2(float &x, float &y, float2 ts) {
 //   slices_ready (256 producer arrivals)  -> the MMA may read A/B slices
 //   mma_done     (tcgen05.commit)         -> TMEM holds tile t; A/B reusable
 //   tmem_free    (256 consumer arrivals)  -> the next MMA may overwrite TMEM
-// Every wait is bounded (1 s); a timeout sets the error status and the CTA
-// stops issuing work, waits (bounded) for its MMAs, frees TMEM and returns.
+// Every wait is bounded (1 s, qd_mbarrier.cuh); a timeout sets QD_ERR_TIMEOUT
+// in the status word and the CTA stops issuing work, waits (bounded) for its
+// MMAs, frees TMEM and returns.
 __device__ inline void named_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
-__device__ inline void mbar_arrive(uint32_t a) {
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(a) : "memory");
-}
-__device__ inline bool mbar_wait_bounded(uint32_t a, uint32_t parity) {
-  const uint64_t t0 = globaltimer();
-  while (!mbar_try_wait(a, parity))
-    if (globaltimer() - t0 > WAIT_NS) return false;
-  return true;
-}
-
 struct TcTile {
   int b, mt, Kv, Nv, Kp, Np;
   uint32_t SBO, A_TERM, B_TERM;
@@ -371,7 +339,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       // the MMA of the previous tile must be done before A (and B) are rewritten;
       // one thread waits and the group decides together (no divergent exit)
       if (tid == 0 && it > 0 && !mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((it - 1) & 1))) {
-        if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_CUDA);
+        if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
         abort_p = 1;
       }
       named_bar(1, WS_PROD);
@@ -463,7 +431,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         bool ok = mbar_wait_bounded(smem_u32(&mb_ready), (uint32_t)(it & 1));
         if (ok && it > 0) ok = mbar_wait_bounded(smem_u32(&mb_free), (uint32_t)((it - 1) & 1));
         if (!ok) {
-          if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_CUDA);
+          if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
           abort_c = 1;
         } else {
           tc_fence_after();
@@ -500,7 +468,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
           n_issued = it + 1;
           // this thread observes completion for the group
           if (!mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)(it & 1))) {
-            if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_CUDA);
+            if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
             abort_c = 1;
           }
         }

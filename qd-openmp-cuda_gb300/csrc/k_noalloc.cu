@@ -9,8 +9,6 @@
 // gpuArray pool, or a loop in which the implicit device synchronisation of
 // cudaMalloc is not allowed) can still call it with only its own input and
 // output buffers.
-#include <mutex>
-
 #include "qd_internal.h"
 #include "qd_device.cuh"
 
@@ -22,29 +20,19 @@ namespace {
 constexpr int QD_NOALLOC_MAX_PARTIALS = 65536;
 constexpr int NOALLOC_TILES = 16;     // CTAs per Legendre slab
 constexpr int NOALLOC_THREADS = 256;
-constexpr int MAX_DEVICES = 64;
-
 static __device__ __align__(256) double g_rot_energy_scratch[QD_NOALLOC_MAX_PARTIALS];
 
-// Device address of the scratch array, resolved once per device.  In host code
-// the array's name is only a host-side stand-in, never a device address.
-double *g_scratch_ptr[MAX_DEVICES] = {};
-std::mutex g_scratch_mutex;
-
+// Device address of the scratch array in the current device's context.  In host
+// code the array's name is only a host-side stand-in, never a device address, so
+// every call looks the address up again: that is cheap, allocates nothing, and
+// stays right after a cudaDeviceReset or under a different context on the device,
+// where an address cached from an earlier call would no longer be valid.
 double *scratch_for_current_device() {
-  int dev = 0;
-  QD_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= MAX_DEVICES) throw Error{QD_ERR_UNSUPPORTED, "device index above 63"};
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_rot_energy_scratch);
-    if (e != cudaSuccess)
-      throw Error{QD_ERR_CUDA, std::string("cudaGetSymbolAddress(rotational-energy scratch): ") +
-                                   cudaGetErrorString(e)};
-    g_scratch_ptr[dev] = static_cast<double *>(p);
-  }
-  return g_scratch_ptr[dev];
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_rot_energy_scratch);
+  if (e != cudaSuccess)
+    throw Error{QD_ERR_CUDA, std::string("cudaGetSymbolAddress(rotational-energy scratch): ") + cudaGetErrorString(e)};
+  return static_cast<double *>(p);
 }
 }  // namespace
 
@@ -106,12 +94,21 @@ extern "C" int qd_rotational_energy_noalloc(const double *psi_j, int32_t n1, int
     g.dr2 = r2_dr;
     g.m2 = r2_mass;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // every partial slot that the sum reads is written by this call first
-    k_rot_energy_block<<<dim3(NOALLOC_TILES, n_slabs), NOALLOC_THREADS, 0, st>>>(
-        g, reinterpret_cast<const double2 *>(psi_j), omega, scratch);
-    k_rot_energy_sum<<<1, NOALLOC_THREADS, 0, st>>>(scratch, n_slabs * NOALLOC_TILES, r1_dr * r2_dr,
-                                                   rotational_energy);
-    QD_CUDA(cudaGetLastError());
+    // every partial slot that the sum reads is written by this call first.  The
+    // launches report through their own return codes, so an error left pending by
+    // the caller's earlier work is neither cleared nor reported as this call's.
+    const double2 *psi = reinterpret_cast<const double2 *>(psi_j);
+    void *block_args[] = {&g, &psi, &omega, &scratch};
+    cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void *>(&k_rot_energy_block),
+                                     dim3(NOALLOC_TILES, n_slabs), dim3(NOALLOC_THREADS), block_args, 0, st);
+    if (e != cudaSuccess) throw Error{QD_ERR_CUDA, std::string("rotational-energy partials: ") + cudaGetErrorString(e)};
+    int n_part = n_slabs * NOALLOC_TILES;
+    double scale = r1_dr * r2_dr;
+    const double *part = scratch;
+    void *sum_args[] = {&part, &n_part, &scale, &rotational_energy};
+    e = cudaLaunchKernel(reinterpret_cast<const void *>(&k_rot_energy_sum), dim3(1), dim3(NOALLOC_THREADS), sum_args,
+                         0, st);
+    if (e != cudaSuccess) throw Error{QD_ERR_CUDA, std::string("rotational-energy sum: ") + cudaGetErrorString(e)};
     return QD_OK;
   } catch (const Error &e) {
     set_error(e.msg);

@@ -969,11 +969,15 @@ static void check_status(qd_session *s) {
   QD_CUDA(cudaGetLastError());
   int st = 0, stp = 0;
   QD_CUDA(cudaMemcpy(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost));
-  if (st) {
+  if (st == QD_ERR_NORM) {
     QD_CUDA(cudaMemcpy(&stp, s->status_step, sizeof(int), cudaMemcpyDeviceToHost));
     throw Error{st, "Total module error: norm above 1 at step " + std::to_string(stp) +
                         " (print_energies, cudaOpenMP2.cu:437-440)"};
   }
+  if (st == QD_ERR_TIMEOUT)
+    throw Error{st, "a device-side wait gave up after 1 s: a tensor-core contraction's pipeline stalled"};
+  if (st == QD_ERR_INVALID) throw Error{st, "flux surface buffer full (more steps buffered than its capacity)"};
+  if (st) throw Error{st, "device status " + std::to_string(st)};
 }
 
 static void flush_flux(qd_session *s) {
@@ -1188,6 +1192,14 @@ int qd_session_synchronize(qd_session *s) {
   QD_GUARD({
     QD_REQUIRE(s, "session");
     check_status(s);
+  })
+}
+
+int qd_session_flush(qd_session *s) {
+  QD_GUARD({
+    QD_REQUIRE(s, "session");
+    flush_flux(s);
+    QD_CUDA(cudaGetLastError());
   })
 }
 
@@ -1490,6 +1502,14 @@ int qd_device_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw Error{QD_ERR_NO_DEVICE, "no CUDA device"};
     if (fp64_tflops) *fp64_tflops = measure_fp64_tflops();
     if (fp32_tflops) *fp32_tflops = measure_fp32_tflops();
+  })
+}
+
+int qd_device_wait_selftest(double budget_ms, int32_t arrive) {
+  QD_GUARD({
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw Error{QD_ERR_NO_DEVICE, "no CUDA device"};
+    device_wait_selftest(budget_ms, arrive);
   })
 }
 

@@ -171,6 +171,16 @@ def h2_ground_state(r: np.ndarray, dr: float, mass: float):
     return float(e[0]), chi
 
 
+def woods_saxon(x, Cd: float, xd: float) -> np.ndarray:
+    """Woods-Saxon absorbing mask 1 / (1 + exp(Cd (x - xd))) of the reference's
+    front end (``FH2main.m:97-99,113-115``; the same function as
+    ``cudaMath.h:159-162``), applied once per step as ``dump1``/``dump2``."""
+    x = np.asarray(x, dtype=np.float64)
+    # exp overflows to inf far beyond xd, where the mask is 0 anyway
+    with np.errstate(over="ignore"):
+        return 1.0 / (1.0 + np.exp(Cd * (x - xd)))
+
+
 def cap_mask(x: np.ndarray, width: float, strength: float, dt: float) -> np.ndarray:
     """Multiplicative form exp(-strength (x-x0)^2 dt) of a quadratic absorbing
     potential -i strength (x-x0)^2 over the last ``width`` of the grid."""
@@ -186,6 +196,16 @@ def eta_sq(energies_coll, mass: float, r0: float, delta: float, k0: float):
     e = np.asarray(energies_coll, dtype=np.float64)
     k = np.sqrt(2.0 * mass * e)
     return mass / k * (delta / math.sqrt(math.pi)) * np.exp(-(delta ** 2) * (k - k0) ** 2)
+
+
+def energy_window(eta_sq_values, rel: float = 1e-4) -> np.ndarray:
+    """Energies the initial packet carries: |a(E)|^2 >= rel * max |a(E)|^2.
+
+    P(E) = flux(E) / |a(E)|^2 is a probability only where the packet has weight;
+    outside this window |a(E)|^2 falls to 1e-11 and below and P(E) divides
+    rounding noise by it, so P(E) comparisons are made inside the window."""
+    e = np.asarray(eta_sq_values, dtype=np.float64)
+    return e >= rel * e.max()
 
 
 def finite_difference_weights(n_points: int) -> np.ndarray:
@@ -243,9 +263,13 @@ class FH2Config:
     R0: float = 9.0
     delta: float = 0.5
     e_coll: float = 0.05
-    # absorbing potential
+    # absorbing potential: "cap" (quadratic CAP over the last cap_width of each grid) or
+    # "woods_saxon" (the reference's own masks, FH2main.m:97-99,113-115: Cd, xd per coordinate)
+    mask: str = "cap"
     cap_width: float = 2.0
     cap_strength: float = 0.01
+    ws_r1: tuple = (4.0, 12.0)
+    ws_r2: tuple = (4.0, 10.0)
     # flux / P(E)
     r_flux: float = 3.5
     n_gradient_points: int = 21
@@ -275,10 +299,14 @@ CONFIGS: Dict[str, FH2Config] = {
 def batched_partial_waves(J_max: int = 40, omega_cap: int = 20, n1: int = 192, n2: int = 96,
                           n_theta: int = 80, l_max: int = 79, total_steps: int = 8000,
                           precision: str = "fp64") -> List[FH2Config]:
-    """Configurations of the batched J=0..J_max partial-wave run (one per J)."""
+    """Configurations of the batched J=0..J_max partial-wave run (one per J).
+
+    Each J takes the parity p = J mod 2, so that (J + p) mod 2 = 0 and its helicities start
+    at Omega = 0 (``OmegaList.m:2-16``, ``CoriolisMatrix.C:52-61``): Omega = 0..min(J,
+    omega_cap), 651 Omega blocks for J = 0..40 with omega_cap = 20."""
     out = []
     for J in range(J_max + 1):
-        out.append(FH2Config(n1=n1, n2=n2, n_theta=n_theta, l_max=l_max, J=J, parity=0,
+        out.append(FH2Config(n1=n1, n2=n2, n_theta=n_theta, l_max=l_max, J=J, parity=J % 2,
                              omega_cap=omega_cap, total_steps=total_steps, precision=precision,
                              name=f"fh2_batched_J{J}"))
     return out
@@ -332,8 +360,14 @@ def build_fh2data(cfg: FH2Config) -> dict:
     if cfg.init_omega in omegas:
         wave_packets[omegas.index(cfg.init_omega)] = psi0
 
-    dump1 = {"dump": cap_mask(r1["r"], cfg.cap_width, cfg.cap_strength, cfg.dt)}
-    dump2 = {"dump": cap_mask(r2["r"], cfg.cap_width, cfg.cap_strength, cfg.dt)}
+    if cfg.mask == "woods_saxon":
+        dump1 = {"dump": woods_saxon(r1["r"], *cfg.ws_r1)}
+        dump2 = {"dump": woods_saxon(r2["r"], *cfg.ws_r2)}
+    elif cfg.mask == "cap":
+        dump1 = {"dump": cap_mask(r1["r"], cfg.cap_width, cfg.cap_strength, cfg.dt)}
+        dump2 = {"dump": cap_mask(r2["r"], cfg.cap_width, cfg.cap_strength, cfg.dt)}
+    else:
+        raise ValueError(f"unknown mask kind {cfg.mask!r} (cap or woods_saxon)")
 
     n_ds = int(round((cfg.r_flux - r2["left"]) / r2["dr"]))
     e_coll = np.linspace(cfg.e_range[0], cfg.e_range[1], cfg.n_energies)

@@ -1,8 +1,11 @@
 """GPU parity: the CUDA path through the C ABI against the FP64 oracle.
 
 Tolerances: FP64 form, element-wise relative L2 error of psi <= 1e-12 after a
-few steps and <= 1e-10 after 500 steps; energies to 1e-11 relative;
-P(E) to 1e-9 of max|P|.  Mixed form: psi <= 1e-5 relative, P(E) <= 1e-4.
+few steps and <= 1e-10 after 1000 steps; energies to 1e-11 relative; P(E)
+within 1e-8 absolute.  Mixed form: psi <= 1e-5 relative, P(E) within 1e-4
+absolute.  P(E) is compared inside the initial packet's energy window
+(|a(E)|^2 >= 1e-4 max |a|^2): outside it P = flux/|a|^2 divides rounding
+noise by |a|^2 < 1e-11 and is not a probability in either form.
 """
 import numpy as np
 import pytest
@@ -12,6 +15,13 @@ pytestmark = pytest.mark.gpu
 
 def rel(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300))
+
+
+def dP_window(qd, d, got, ref):
+    """max |P_got - P_ref| over the energies the initial packet carries."""
+    win = qd.inputs.energy_window(d["CRP"]["eta_sq"])
+    assert win.any()
+    return float(np.max(np.abs(np.asarray(got) - np.asarray(ref))[win]))
 
 
 def make(qd, **kw):
@@ -24,7 +34,8 @@ CASES = [
     dict(J=0, n1=16, n2=8, n_theta=6, l_max=5),
     dict(J=2, parity=0, n1=16, n2=8, n_theta=8, l_max=6),
     dict(J=3, parity=1, n1=24, n2=12, n_theta=8, l_max=7),
-    dict(J=4, parity=1, n1=32, n2=16, n_theta=10, l_max=8, n_energies=12),
+    # (J + p) odd: Omega = 1..4, so the packet starts in Omega = 1
+    dict(J=4, parity=1, n1=32, n2=16, n_theta=10, l_max=8, n_energies=12, init_omega=1),
 ]
 
 
@@ -94,12 +105,12 @@ def test_evolve_matches_oracle(qd, oracle, gpu, case):
     assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-12
     np.testing.assert_allclose(d["options"]["energies"][:, :, :4], rec[:, :, :4], rtol=1e-10, atol=1e-15)
     np.testing.assert_allclose(d["options"]["energies"][:, :, 4], rec[:, :, 4], rtol=1e-8, atol=1e-14)
-    crp = o.crp()
-    assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-9 * max(1e-30, np.abs(crp).max())
+    assert np.abs(o.wave_packets()).max() > 0
+    assert dP_window(qd, d, d["CRP"]["CRP"], o.crp()) <= 1e-8
 
 
 def test_fp64_1000_steps_reference_grid(qd, oracle, gpu):
-    """64x32x24, J=0, dt=10, 1000 steps: relative |dpsi| <= 1e-10 and |dP| <= 1e-8 (relative to max P)."""
+    """64x32x24, J=0, dt=10, 1000 steps: relative |dpsi| <= 1e-10 and |dP(E)| <= 1e-8 in the window."""
     cfg = qd.inputs.CONFIGS["fh2_j0_64x32x24"]
     d = qd.inputs.build_fh2data(cfg)
     d["time"]["total_steps"] = 1000
@@ -108,7 +119,9 @@ def test_fp64_1000_steps_reference_grid(qd, oracle, gpu):
     qd.cudaOpenMPEvolution(d)
     assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-10
     crp = o.crp()
-    assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-8 * np.abs(crp).max()
+    win = qd.inputs.energy_window(d["CRP"]["eta_sq"])
+    assert np.abs(crp[win]).max() > 1.0     # a propagated flux, not a vacuous comparison
+    assert dP_window(qd, d, d["CRP"]["CRP"], crp) <= 1e-8
 
 
 def test_batch_equals_separate_problems(qd, oracle, gpu):
@@ -121,8 +134,7 @@ def test_batch_equals_separate_problems(qd, oracle, gpu):
         o = oracle.Oracle(qd.inputs.build_fh2data(c))
         o.run(c.total_steps)
         assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-12
-        crp = o.crp()
-        assert np.max(np.abs(d["CRP"]["CRP"] - crp)) <= 1e-9 * np.abs(crp).max()
+        assert dP_window(qd, d, d["CRP"]["CRP"], o.crp()) <= 1e-8
 
 
 def test_callback_sees_copied_wave_packets(qd, oracle, gpu):
@@ -149,8 +161,9 @@ def test_callback_sees_copied_wave_packets(qd, oracle, gpu):
 def test_mixed_graph_chunks_equal_single_steps(qd, gpu, J):
     """140 mixed steps replayed from 64-step graphs (device-side step counter, flux slot and
     record index) equal the same steps enqueued one at a time (a callback after every step):
-    wave packets and energy records bit for bit; P(E) to 1e-12 of its maximum (a callback may
-    flush the surface buffer at other steps, which regroups the FP64 sums)."""
+    wave packets and energy records bit for bit; P(E) in the energy window to 1e-12 of its
+    maximum there (a callback may flush the surface buffer at other steps, which regroups the
+    FP64 sums)."""
     out = []
     for every_step in (False, True):
         cfg, d, _ = make(qd, J=J, parity=0, n1=32, n2=16, n_theta=8, l_max=6, steps=140, n_energies=8)
@@ -168,7 +181,8 @@ def test_mixed_graph_chunks_equal_single_steps(qd, gpu, J):
     a, b = out
     assert np.array_equal(a["OmegaStates"]["wave_packets"], b["OmegaStates"]["wave_packets"])
     assert np.array_equal(a["options"]["energies"], b["options"]["energies"])
-    assert np.max(np.abs(a["CRP"]["CRP"] - b["CRP"]["CRP"])) <= 1e-12 * np.abs(b["CRP"]["CRP"]).max()
+    win = qd.inputs.energy_window(b["CRP"]["eta_sq"])
+    assert dP_window(qd, b, a["CRP"]["CRP"], b["CRP"]["CRP"]) <= 1e-12 * np.abs(b["CRP"]["CRP"][win]).max()
 
 
 def test_callback_error_aborts(qd, gpu):
@@ -224,18 +238,17 @@ def test_norm_conserved_at_production_grid(qd, gpu):
 
 
 def test_mixed_precision_close_to_fp64(qd, oracle, gpu):
-    cfg, d, dref = make(qd, J=2, parity=0, n1=32, n2=16, n_theta=8, l_max=6, steps=20, n_energies=8)
+    cfg, d, dref = make(qd, J=2, parity=0, n1=32, n2=16, n_theta=8, l_max=6, steps=20, n_energies=64)
     d["options"]["precision"] = 1
     o = oracle.Oracle(dref)
     o.run(cfg.total_steps)
     qd.cudaOpenMPEvolution(d)
     assert rel(d["OmegaStates"]["wave_packets"], o.wave_packets()) < 1e-5
     crp = o.crp()
-    # |dP| <= 1e-4 where P is a probability; on this coarse toy grid the edge
-    # energies have eta^2 ~ 1e-10 and P(E) far outside [0, 1]
-    phys = np.abs(crp) <= 2.0
-    assert phys.sum() >= 4
-    assert np.max(np.abs(d["CRP"]["CRP"] - crp)[phys]) <= 1e-4
+    dp = dP_window(qd, d, d["CRP"]["CRP"], crp)
+    win = qd.inputs.energy_window(d["CRP"]["eta_sq"])
+    assert dp <= 1e-4
+    assert dp <= 1e-3 * np.abs(crp[win]).max()
 
 
 @pytest.mark.parametrize("case", [dict(J=0, n1=16, n2=8, n_theta=6, l_max=5),
