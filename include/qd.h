@@ -162,6 +162,14 @@ int qd_evolve(qd_fh2data *data, qd_callback cb, void *user);
    together (each stage one launch over every Omega block of every problem). */
 int qd_evolve_batch(qd_fh2data *const *problems, int32_t n_problems, qd_callback cb, void *user);
 
+/* qd_evolve and qd_evolve_batch keep the device state of their last call on
+   each device (up to QD_SESSION_CACHE_BYTES of device memory, default 8 GiB;
+   the environment variable set to 0 turns this off) and reuse it for the next
+   call with the same grids, time step, precision, Omega lists and flux
+   surface: only the wave packets and the inputs that changed are loaded again.
+   This releases the kept state and its device memory. */
+int qd_release_session_cache(void);
+
 /* Last error message of the calling thread ("" if none). */
 const char *qd_last_error(void);
 

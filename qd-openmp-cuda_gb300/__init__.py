@@ -92,7 +92,7 @@ CALLBACK = C.CFUNCTYPE(C.c_int, C.POINTER(FH2Data), C.c_void_p)
 
 _lib = None
 
-EXPORTED = ("qd_evolve", "qd_evolve_batch", "qd_last_error", "qd_version", "qd_session_create",
+EXPORTED = ("qd_evolve", "qd_evolve_batch", "qd_release_session_cache", "qd_last_error", "qd_version", "qd_session_create",
             "qd_session_destroy", "qd_session_run", "qd_session_synchronize", "qd_session_flush", "qd_session_download",
             "qd_session_upload", "qd_session_stream", "qd_session_info", "qd_session_apply", "qd_session_get_psi",
             "qd_session_set_psi", "qd_session_get_energies", "qd_session_profile", "qd_device_fma_peaks",
@@ -118,6 +118,7 @@ def load_library():
     lib.qd_last_error.restype = C.c_char_p
     lib.qd_evolve.argtypes = [P(FH2Data), CALLBACK, C.c_void_p]
     lib.qd_evolve_batch.argtypes = [P(P(FH2Data)), C.c_int32, CALLBACK, C.c_void_p]
+    lib.qd_release_session_cache.argtypes = []
     lib.qd_session_create.argtypes = [P(P(FH2Data)), C.c_int32, P(C.c_void_p)]
     lib.qd_session_destroy.argtypes = [C.c_void_p]
     lib.qd_session_run.argtypes = [C.c_void_p, C.c_int32]
@@ -281,6 +282,11 @@ def evolve_batch(problems: Sequence[dict], callback=None) -> None:
     for m in ms:
         m.write_back()
     _check(st)
+
+
+def release_session_cache() -> None:
+    """Release the device state that qd_evolve keeps for its next call of the same shape."""
+    _check(load_library().qd_release_session_cache())
 
 
 class Session:

@@ -14,7 +14,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -219,6 +221,36 @@ static std::vector<double> fd_weights(int n) {
   return w;
 }
 
+// Device memory of one session: a few cudaMalloc chunks of growing size (16 MiB
+// doubling, or the request when larger), sub-allocated 256-byte aligned and
+// released together.  A session makes about 60 buffers; this keeps the
+// allocation (and the device synchronisation of cudaFree) to a handful of calls.
+struct Arena {
+  std::vector<void *> chunks;
+  char *cur = nullptr;
+  size_t left = 0, next = (size_t)16 << 20, total = 0;
+  void *take(size_t bytes) {
+    bytes = (bytes + 255) & ~(size_t)255;
+    if (bytes > left) {
+      const size_t chunk = std::max(bytes, next);
+      next = std::min(next * 2, (size_t)1 << 30);
+      void *p = nullptr;
+      QD_CUDA(cudaMalloc(&p, chunk));
+      chunks.push_back(p);
+      cur = static_cast<char *>(p);
+      left = chunk;
+      total += chunk;
+    }
+    void *r = cur;
+    cur += bytes;
+    left -= bytes;
+    return r;
+  }
+  ~Arena() {
+    for (void *p : chunks) cudaFree(p);
+  }
+};
+
 template <typename T> static T *dalloc(size_t n) {
   T *p = nullptr;
   if (n == 0) return nullptr;
@@ -242,6 +274,7 @@ using namespace qd;
 
 // ------------------------------------------------------------------ session
 struct qd_session {
+  qd::Arena arena;   // every device buffer of the session (released last)
   int device = 0;
   cudaStream_t stream = nullptr;
   Grid g{};
@@ -311,6 +344,25 @@ struct qd_session {
   int launches_per_step = 0;
   cudaGraphExec_t graph_chunk = nullptr;
   int graph_steps = 0;
+  // reuse across qd_evolve calls of the same shape: the key, host copies of the
+  // small inputs the tables were built from, a staging buffer and a flag for the
+  // on-device comparison of the potential
+  std::vector<double> key;
+  std::vector<double> h_w, h_d1, h_d2, h_Bf, h_Bb;
+  double *pot_stage = nullptr;
+  int *d_flag = nullptr;
+  double *rec_buf = nullptr;
+  size_t rec_buf_cap = 0;
+  // energy-record arguments the step graph was captured with
+  double *graph_rec = nullptr;
+  int graph_rec_base = 0, graph_rec_cap = 0;
+
+  template <typename T> T *alloc(size_t n) { return n ? static_cast<T *>(arena.take(n * sizeof(T))) : nullptr; }
+  template <typename T> T *upload(const T *h, size_t n) {
+    T *p = alloc<T>(n);
+    if (n) QD_CUDA(cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return p;
+  }
 
   ~qd_session();
 };
@@ -396,17 +448,12 @@ __global__ void k_flux_reset(int *count) { *count = 0; }
 
 qd_session::~qd_session() {
   if (graph_chunk) cudaGraphExecDestroy(graph_chunk);
-  void *ptrs[] = {d_blocks, d_slabs, d_pblock0, psi_th, psi_j, psi_thf, psi_jf, xfer, pot, w, T1, T2, I1, I2, d1, d2, tab_v, tab_v0,
-                  tab_rot2, tab_rot4, tab_kin, Bf, Bb, d_groups, cor_V, cor_e, cor_H, cor_ph, cor_Vh, cor_Vl, cor_phl, cor_order,
-                  d_pgroup0,
-                  part_modpe, part_ke, part_re, part_ce, energies, rec, status, status_step, d_step, flux_buf, flux_buf_f,
-                  flux_acc, flux_phase, half_v, fd, flux_E, flux_eta, crp, flux_t0, flux_count, flux_slot,
-                  img_f, img_b, bscale_f, bscale_b, imgoff_f, imgoff_b, vph, vph0, lrotR, lrotr, lkinR, lkinr, wf, wvf, d1f, d2f,
-                  T1f, T2f, I1f, I2f, step_done, half_v_lift, fdf};
-  for (void *p : ptrs)
-    if (p) cudaFree(p);
   fft_plan_free(fft);
-  if (stream) cudaStreamDestroy(stream);
+  if (stream) {
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+  // the arena's chunks are released by its destructor
 }
 
 namespace qd {
@@ -623,6 +670,39 @@ static void theta_to_host(qd_session *s, int64_t off, int64_t n, double *host) {
 }
 
 // ------------------------------------------------------------ create
+// Everything the device state of a batch depends on besides the per-call inputs
+// (wave packets, potential, masks, quadrature weights, Legendre matrices, CRP
+// energies, |a(E)|^2 and accumulators): sizes, grids, time step, precision,
+// the Omega lists and the flux surface.  Two calls with equal keys can share
+// one session's buffers, tables and step graph.
+static std::vector<double> session_key(qd_fh2data *const *pr, int n) {
+  std::vector<double> k;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const qd_fh2data *d = pr[0];
+  k.insert(k.end(), {(double)dev, (double)n, (double)d->r1.n, d->r1.left, d->r1.dr, d->r1.mass, (double)d->r2.n,
+                     d->r2.left, d->r2.dr, d->r2.mass, (double)d->theta.n, (double)d->OmegaStates.l_max,
+                     d->time.time_step, (double)d->options.precision, (double)(d->dump1.dump && d->dump2.dump),
+                     (double)d->CRP.calculate_CRP});
+  if (d->CRP.calculate_CRP)
+    k.insert(k.end(), {(double)d->CRP.n_energies, (double)d->CRP.n_gradient_points, (double)d->CRP.n_dividing_surface});
+  for (int p = 0; p < n; p++) {
+    const qd_omega_states &om = pr[p]->OmegaStates;
+    k.insert(k.end(), {(double)om.J, (double)om.parity, (double)om.n_omegas});
+    for (int i = 0; i < om.n_omegas; i++) k.push_back((double)om.omegas[i]);
+  }
+  return k;
+}
+
+__global__ void k_differs(const double *__restrict__ a, const double *__restrict__ b, int64_t n, int *flag) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    if (__double_as_longlong(a[q]) != __double_as_longlong(b[q])) {
+      *flag = 1;
+      return;
+    }
+}
+
+// Layout, buffers and the tables that depend only on the key.
 static void session_build(qd_session *s, qd_fh2data *const *problems, int n_problems) {
   validate_batch(problems, n_problems, s->probs);
   int dev_count = 0;
@@ -630,6 +710,7 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     throw Error{QD_ERR_NO_DEVICE, "no CUDA device"};
   QD_CUDA(cudaGetDevice(&s->device));
   QD_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  s->key = session_key(problems, n_problems);
   cudaStream_t st = s->stream;
   const qd_fh2data *d0 = problems[0];
   Grid &g = s->g;
@@ -646,7 +727,6 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   g.left2 = d0->r2.left;
   s->precision = d0->options.precision;
   s->dt = d0->time.time_step;
-  s->steps = d0->time.steps;
   s->norm_tol = s->precision == QD_PRECISION_MIXED ? 1e-4 : 1e-10;
   s->n_problems = n_problems;
   fft_plan_init(s->fft, g.n1, g.n2);
@@ -675,28 +755,24 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   }
   s->n_blocks = (int)s->h_blocks.size();
   s->n_slabs = slab;
-  s->d_blocks = dupload(s->h_blocks.data(), s->h_blocks.size(), st);
-  s->d_slabs = dupload(s->h_slabs.data(), s->h_slabs.size(), st);
-  s->d_pblock0 = dupload(s->h_pblock0.data(), s->h_pblock0.size(), st);
+  s->d_blocks = s->upload(s->h_blocks.data(), s->h_blocks.size());
+  s->d_slabs = s->upload(s->h_slabs.data(), s->h_slabs.size());
+  s->d_pblock0 = s->upload(s->h_pblock0.data(), s->h_pblock0.size());
 
-  // wave packets
+  // wave packets: the mixed form keeps both pools in c64 (every value its step
+  // writes there, tensor-core epilogues and FP32 FFT, is an FP32 number)
   const int64_t nth_pt = g.npt * g.nth;
-  // the mixed form keeps both pools in c64: every value its step writes there
-  // (tensor-core epilogues, FP32 FFT) is an FP32 number
   if (s->precision == QD_PRECISION_MIXED) {
-    s->psi_thf = dalloc<float2>((size_t)s->n_blocks * nth_pt);
-    s->psi_jf = dalloc<float2>((size_t)s->n_slabs * g.npt);
+    s->psi_thf = s->alloc<float2>((size_t)s->n_blocks * nth_pt);
+    s->psi_jf = s->alloc<float2>((size_t)s->n_slabs * g.npt);
     s->xfer_elems = std::min<int64_t>((int64_t)s->n_blocks * nth_pt, (int64_t)1 << 25);
-    s->xfer = dalloc<double2>((size_t)s->xfer_elems);
+    s->xfer = s->alloc<double2>((size_t)s->xfer_elems);
   } else {
-    s->psi_th = dalloc<double2>((size_t)s->n_blocks * nth_pt);
-    s->psi_j = dalloc<double2>((size_t)s->n_slabs * g.npt);
+    s->psi_th = s->alloc<double2>((size_t)s->n_blocks * nth_pt);
+    s->psi_j = s->alloc<double2>((size_t)s->n_slabs * g.npt);
   }
-  for (int p = 0; p < n_problems; p++)
-    theta_from_host(s, (int64_t)s->h_pblock0[p] * nth_pt, (int64_t)s->probs[p].n_omegas * nth_pt,
-                    problems[p]->OmegaStates.wave_packets);
 
-  // grid tables
+  // tables of the key: kinetic, rotational, inverse inertia
   std::vector<double> T1(g.n1), T2(g.n2);
   auto kin = [](int n, double dr, double mass, std::vector<double> &T) {
     const double two_pi_xl = 2 * M_PI / (n * dr);   // cudaMath.h:117-130
@@ -707,79 +783,64 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   };
   kin(g.n1, g.dr1, g.m1, T1);
   kin(g.n2, g.dr2, g.m2, T2);
-  s->T1 = dupload(T1.data(), T1.size(), st);
-  s->T2 = dupload(T2.data(), T2.size(), st);
-  s->pot = dupload(d0->pot, (size_t)nth_pt, st);
-  s->w = dupload(d0->theta.w, (size_t)g.nth, st);
+  s->T1 = s->upload(T1.data(), T1.size());
+  s->T2 = s->upload(T2.data(), T2.size());
+  s->pot = s->alloc<double>((size_t)nth_pt);
+  s->pot_stage = s->alloc<double>((size_t)nth_pt);
+  s->d_flag = s->alloc<int>(1);
+  s->w = s->alloc<double>((size_t)g.nth);
   s->has_mask = d0->dump1.dump && d0->dump2.dump;   // MatlabData::dump_wavepacket (matlabData.h:27)
   if (s->has_mask) {
-    s->d1 = dupload(d0->dump1.dump, (size_t)g.n1, st);
-    s->d2 = dupload(d0->dump2.dump, (size_t)g.n2, st);
+    s->d1 = s->alloc<double>((size_t)g.n1);
+    s->d2 = s->alloc<double>((size_t)g.n2);
   }
   const bool fp64 = s->precision == QD_PRECISION_FP64;
   if (fp64) {
-    s->tab_v = dalloc<double2>((size_t)nth_pt);
-    s->tab_v0 = dalloc<double2>((size_t)nth_pt);
-    launch_build_theta_table(st, g, s->pot, s->d1, s->d2, s->dt, s->tab_v);
-    launch_build_theta_table(st, g, s->pot, s->d1, s->d2, 0.5 * s->dt, s->tab_v0);
+    s->tab_v = s->alloc<double2>((size_t)nth_pt);
+    s->tab_v0 = s->alloc<double2>((size_t)nth_pt);
   }
   const int64_t nrot = g.npt * (g.l_max + 1);
   if (s->any_coupled) {
-    s->tab_rot4 = dalloc<double2>((size_t)nrot);
+    s->tab_rot4 = s->alloc<double2>((size_t)nrot);
     launch_build_rot_table(st, g, 0.25 * s->dt, s->tab_rot4);
   } else if (fp64) {
-    s->tab_rot2 = dalloc<double2>((size_t)nrot);
+    s->tab_rot2 = s->alloc<double2>((size_t)nrot);
     launch_build_rot_table(st, g, 0.5 * s->dt, s->tab_rot2);
   }
-  s->tab_kin = dalloc<double2>((size_t)g.npt);
+  s->tab_kin = s->alloc<double2>((size_t)g.npt);
   launch_build_kin_table(st, g, s->T1, s->T2, s->dt, s->tab_kin);
   // FP32 tables (the mixed form; also used by mixed-precision stage calls)
-  s->wf = dalloc<float>((size_t)g.nth);
-  s->wvf = dalloc<float>((size_t)nth_pt);
-  s->T1f = dalloc<float>((size_t)g.n1);
-  s->T2f = dalloc<float>((size_t)g.n2);
-  s->I1f = dalloc<float>((size_t)g.n1);
-  s->I2f = dalloc<float>((size_t)g.n2);
+  s->wf = s->alloc<float>((size_t)g.nth);
+  s->wvf = s->alloc<float>((size_t)nth_pt);
+  s->T1f = s->alloc<float>((size_t)g.n1);
+  s->T2f = s->alloc<float>((size_t)g.n2);
+  s->I1f = s->alloc<float>((size_t)g.n1);
+  s->I2f = s->alloc<float>((size_t)g.n2);
   if (s->has_mask) {
-    s->d1f = dalloc<float>((size_t)g.n1);
-    s->d2f = dalloc<float>((size_t)g.n2);
+    s->d1f = s->alloc<float>((size_t)g.n1);
+    s->d2f = s->alloc<float>((size_t)g.n2);
   }
-  launch_build_float_tables(st, g, s->w, s->pot, s->d1, s->d2, s->T1, s->T2, s->wf, s->wvf, s->d1f, s->d2f, s->T1f,
-                            s->T2f, s->I1f, s->I2f);
   if (!fp64) {
-    s->vph = dalloc<float2>((size_t)nth_pt);
-    s->vph0 = dalloc<float2>((size_t)nth_pt);
-    launch_build_lift_theta(st, g, s->pot, s->dt, s->vph);
-    launch_build_lift_theta(st, g, s->pot, 0.5 * s->dt, s->vph0);
+    s->vph = s->alloc<float2>((size_t)nth_pt);
+    s->vph0 = s->alloc<float2>((size_t)nth_pt);
     const double drot = (s->any_coupled ? 0.25 : 0.5) * s->dt;
-    s->lrotR = dalloc<float2>((size_t)(g.l_max + 1) * g.n1);
-    s->lrotr = dalloc<float2>((size_t)(g.l_max + 1) * g.n2);
+    s->lrotR = s->alloc<float2>((size_t)(g.l_max + 1) * g.n1);
+    s->lrotr = s->alloc<float2>((size_t)(g.l_max + 1) * g.n2);
     launch_build_lift_rot(st, g.n1, g.l_max, g.left1, g.dr1, g.m1, drot, s->lrotR);
     launch_build_lift_rot(st, g.n2, g.l_max, g.left2, g.dr2, g.m2, drot, s->lrotr);
-    s->lkinR = dalloc<float2>((size_t)g.n1);
-    s->lkinr = dalloc<float2>((size_t)g.n2);
+    s->lkinR = s->alloc<float2>((size_t)g.n1);
+    s->lkinr = s->alloc<float2>((size_t)g.n2);
     launch_build_lift_kin(st, g.n1, s->T1, s->dt, s->lkinR);
     launch_build_lift_kin(st, g.n2, s->T2, s->dt, s->lkinr);
   }
 
-  // Legendre matrices: forward B = w_k P (k, n) as [k][n]; backward P as [n][k]
-  std::vector<double> Bf((size_t)bmat), Bb((size_t)bmat);
-  for (int b = 0; b < s->n_blocks; b++) {
-    const BlockDesc &bd = s->h_blocks[b];
-    const ProblemHost &ph = s->probs[bd.problem];
-    const qd_omega_states &om = ph.d->OmegaStates;
-    const int bi = b - s->h_pblock0[bd.problem];
-    for (int n = 0; n < bd.nl; n++)
-      for (int k = 0; k < g.nth; k++) {
-        const double P = om.associated_legendres[((int64_t)bi * om.n_cols + n) * g.nth + k];
-        Bf[bd.bmat0 + (int64_t)k * bd.nl + n] = ph.d->theta.w[k] * P;
-        Bb[bd.bmat0 + (int64_t)n * g.nth + k] = P;
-      }
-  }
-  s->Bf = dupload(Bf.data(), Bf.size(), st);
-  s->Bb = dupload(Bb.data(), Bb.size(), st);
+  // Legendre matrices (filled per call): forward B = w_k P (k, n) as [k][n];
+  // backward P as [n][k]; their tensor-core images (BF16x3 split, shared-memory layout)
+  s->h_Bf.assign((size_t)bmat, 0.0);
+  s->h_Bb.assign((size_t)bmat, 0.0);
+  s->Bf = s->alloc<double>((size_t)bmat);
+  s->Bb = s->alloc<double>((size_t)bmat);
   {
-    // tensor-core images (BF16x3 split, shared-memory layout) of both directions
     auto r16 = [](int x) { return (x + 15) & ~15; };
     std::vector<int64_t> of, ob;
     int64_t tf = 0, tb = 0;
@@ -800,16 +861,12 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
                                         "(contraction <= 192, columns <= 160)"};
     } else {
       tc_set_smem_limit(std::max(s->smem_f, s->smem_b));
-      s->imgoff_f = dupload(of.data(), of.size(), st);
-      s->imgoff_b = dupload(ob.data(), ob.size(), st);
-      s->img_f = dalloc<uint16_t>((size_t)tf / 2);
-      s->img_b = dalloc<uint16_t>((size_t)tb / 2);
-      s->bscale_f = dalloc<float>((size_t)s->n_blocks * 256);
-      s->bscale_b = dalloc<float>((size_t)s->n_blocks * 256);
-      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bf, g.nth, true, s->imgoff_f, s->img_f, s->bscale_f,
-                             r16(s->max_nl));
-      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bb, g.nth, false, s->imgoff_b, s->img_b, s->bscale_b,
-                             r16(g.nth));
+      s->imgoff_f = s->upload(of.data(), of.size());
+      s->imgoff_b = s->upload(ob.data(), ob.size());
+      s->img_f = s->alloc<uint16_t>((size_t)tf / 2);
+      s->img_b = s->alloc<uint16_t>((size_t)tb / 2);
+      s->bscale_f = s->alloc<float>((size_t)s->n_blocks * 256);
+      s->bscale_b = s->alloc<float>((size_t)s->n_blocks * 256);
     }
   }
 
@@ -820,51 +877,49 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     int64_t ph0 = 0;
     for (int p = 0; p < n_problems; p++) {
       const ProblemHost &ph = s->probs[p];
-      {
-        // J = 0 problems of a coupled batch get 1x1 zero matrices: identity
-        // coupling, but their second rotational quarter step still applies
-        for (int l = ph.omega_min; l <= g.l_max; l++) {
-          const int omax = std::min(std::min(ph.J, l), ph.omega_cap);
-          const int n = omax - ph.omega_min + 1;
-          if (n < 1) continue;
-          std::vector<double> a((size_t)n * n, 0.0);
-          for (int k = 0; k < n; k++) {
-            const int om = k + ph.omega_min;
-            a[(size_t)k * n + k] = ph.J * (ph.J + 1.0) - 2.0 * om * om;
-            if (k + 1 < n) {
-              const double off = -lam(ph.J, om) * lam(l, om) * std::sqrt(1.0 + (om == 0 ? 1.0 : 0.0));
-              a[(size_t)k * n + k + 1] = off;
-              a[(size_t)(k + 1) * n + k] = off;
-            }
+      // J = 0 problems of a coupled batch get 1x1 zero matrices: identity
+      // coupling, but their second rotational quarter step still applies
+      for (int l = ph.omega_min; l <= g.l_max; l++) {
+        const int omax = std::min(std::min(ph.J, l), ph.omega_cap);
+        const int n = omax - ph.omega_min + 1;
+        if (n < 1) continue;
+        std::vector<double> a((size_t)n * n, 0.0);
+        for (int k = 0; k < n; k++) {
+          const int om = k + ph.omega_min;
+          a[(size_t)k * n + k] = ph.J * (ph.J + 1.0) - 2.0 * om * om;
+          if (k + 1 < n) {
+            const double off = -lam(ph.J, om) * lam(l, om) * std::sqrt(1.0 + (om == 0 ? 1.0 : 0.0));
+            a[(size_t)k * n + k + 1] = off;
+            a[(size_t)(k + 1) * n + k] = off;
           }
-          std::vector<double> e, v;
-          jacobi_eigen(n, a, e, v);
-          CoriolisGroup gr{};
-          gr.l = l;
-          gr.n = n;
-          gr.block_lo = s->h_pblock0[p];
-          gr.omega_lo = ph.omega_min;
-          gr.v0 = (int64_t)V.size();
-          gr.e0 = (int64_t)E.size();
-          gr.h0 = (int64_t)H.size();
-          gr.ph0 = ph0;
-          ph0 += (int64_t)n * g.n1;
-          V.insert(V.end(), v.begin(), v.end());
-          E.insert(E.end(), e.begin(), e.end());
-          H.insert(H.end(), a.begin(), a.end());
-          s->h_groups.push_back(gr);
-          s->max_group_n = std::max(s->max_group_n, n);
         }
+        std::vector<double> e, v;
+        jacobi_eigen(n, a, e, v);
+        CoriolisGroup gr{};
+        gr.l = l;
+        gr.n = n;
+        gr.block_lo = s->h_pblock0[p];
+        gr.omega_lo = ph.omega_min;
+        gr.v0 = (int64_t)V.size();
+        gr.e0 = (int64_t)E.size();
+        gr.h0 = (int64_t)H.size();
+        gr.ph0 = ph0;
+        ph0 += (int64_t)n * g.n1;
+        V.insert(V.end(), v.begin(), v.end());
+        E.insert(E.end(), e.begin(), e.end());
+        H.insert(H.end(), a.begin(), a.end());
+        s->h_groups.push_back(gr);
+        s->max_group_n = std::max(s->max_group_n, n);
       }
       s->h_pgroup0.push_back((int)s->h_groups.size());
     }
     s->n_groups = (int)s->h_groups.size();
-    s->d_groups = dupload(s->h_groups.data(), s->h_groups.size(), st);
-    s->d_pgroup0 = dupload(s->h_pgroup0.data(), s->h_pgroup0.size(), st);
-    s->cor_V = dupload(V.data(), V.size(), st);
-    s->cor_e = dupload(E.data(), E.size(), st);
-    s->cor_H = dupload(H.data(), H.size(), st);
-    s->cor_ph = dalloc<double2>((size_t)ph0);
+    s->d_groups = s->upload(s->h_groups.data(), s->h_groups.size());
+    s->d_pgroup0 = s->upload(s->h_pgroup0.data(), s->h_pgroup0.size());
+    s->cor_V = s->upload(V.data(), V.size());
+    s->cor_e = s->upload(E.data(), E.size());
+    s->cor_H = s->upload(H.data(), H.size());
+    s->cor_ph = s->alloc<double2>((size_t)ph0);
     launch_build_coriolis_phase(st, g, s->d_groups, s->n_groups, s->max_group_n, s->cor_e, 0.5 * s->dt, s->cor_ph);
     if (s->precision == QD_PRECISION_MIXED && s->max_group_n <= CORIOLIS_F32_MAXN) {
       // eigenvectors as FP32 pairs (hi + lo) and the phases as three-shear coefficients
@@ -873,15 +928,15 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
         vh[q] = (float)V[q];
         vl[q] = (float)(V[q] - (double)vh[q]);
       }
-      s->cor_Vh = dupload(vh.data(), vh.size(), st);
-      s->cor_Vl = dupload(vl.data(), vl.size(), st);
-      s->cor_phl = dalloc<float2>((size_t)ph0);
+      s->cor_Vh = s->upload(vh.data(), vh.size());
+      s->cor_Vl = s->upload(vl.data(), vl.size());
+      s->cor_phl = s->alloc<float2>((size_t)ph0);
       launch_build_coriolis_lift(st, g, s->d_groups, s->n_groups, s->cor_e, 0.5 * s->dt, s->cor_phl);
       std::vector<int> order;
       for (int c = CORIOLIS_F32_CLASSES - 1; c >= 0; c--)
         for (int gi = 0; gi < s->n_groups; gi++)
           if (coriolis_f32_class(s->h_groups[gi].n) == c) order.push_back(gi);
-      s->cor_order = dupload(order.data(), order.size(), st);
+      s->cor_order = s->upload(order.data(), order.size());
       s->cor_f32 = true;
     }
   }
@@ -889,27 +944,21 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   // energies and partials
   s->t_modpe = s->precision == QD_PRECISION_MIXED ? legendre_tc_part_tiles(g) : legendre_bwd_part_tiles(g);
   s->t_ke = fft_col_tiles(s->fft, s->precision);
-  // coupled: partials of the rotational-energy pass (or of the fused FP32 Coriolis)
   // CTAs per group of the FP32 Coriolis passes: twice the base while the groups are few (one
   // coupled problem has about l_max of them), the base for batched runs with thousands, where
   // more tiles only add partial sums
   const int cor_tiles = s->n_groups < CORIOLIS_F32_FEW_GROUPS ? 2 * CORIOLIS_F32_TILES : CORIOLIS_F32_TILES;
   s->t_re = s->any_coupled ? (s->cor_f32 ? cor_tiles : CORIOLIS_F32_TILES) : fft_row_tiles(s->fft, s->precision);
   s->t_ce = s->cor_f32 ? cor_tiles : coriolis_tiles(g);
-  s->part_modpe = dalloc<double>((size_t)s->n_blocks * s->t_modpe * 2);
-  s->part_ke = dalloc<double>((size_t)s->n_slabs * s->t_ke);
-  s->part_re = dalloc<double>((size_t)s->n_slabs * s->t_re);
-  if (s->any_coupled) s->part_ce = dalloc<double>((size_t)std::max(1, s->n_groups) * s->max_group_n * s->t_ce);
-  s->energies = dalloc<double>((size_t)s->n_blocks * 6);
-  QD_CUDA(cudaMemsetAsync(s->energies, 0, (size_t)s->n_blocks * 6 * sizeof(double), st));
-  s->status = dalloc<int>(1);
-  s->status_step = dalloc<int>(1);
-  s->d_step = dalloc<int>(1);
-  s->step_done = dalloc<unsigned>(1);
-  QD_CUDA(cudaMemsetAsync(s->step_done, 0, sizeof(unsigned), st));
-  QD_CUDA(cudaMemsetAsync(s->status, 0, sizeof(int), st));
-  QD_CUDA(cudaMemsetAsync(s->status_step, 0, sizeof(int), st));
-  QD_CUDA(cudaMemcpyAsync(s->d_step, &s->steps, sizeof(int), cudaMemcpyHostToDevice, st));
+  s->part_modpe = s->alloc<double>((size_t)s->n_blocks * s->t_modpe * 2);
+  s->part_ke = s->alloc<double>((size_t)s->n_slabs * s->t_ke);
+  s->part_re = s->alloc<double>((size_t)s->n_slabs * s->t_re);
+  if (s->any_coupled) s->part_ce = s->alloc<double>((size_t)std::max(1, s->n_groups) * s->max_group_n * s->t_ce);
+  s->energies = s->alloc<double>((size_t)s->n_blocks * 6);
+  s->status = s->alloc<int>(1);
+  s->status_step = s->alloc<int>(1);
+  s->d_step = s->alloc<int>(1);
+  s->step_done = s->alloc<unsigned>(1);
 
   // flux
   const qd_crp &c = d0->CRP;
@@ -923,31 +972,146 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     s->flux.chunk = 64;   // steps per flux DFT flush (and per CUDA graph)
     const int64_t ns = (int64_t)g.nth * g.n1;
     if (s->precision == QD_PRECISION_MIXED)
-      s->flux_buf_f = dalloc<float2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
+      s->flux_buf_f = s->alloc<float2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
     else
-      s->flux_buf = dalloc<double2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
-    s->flux_acc = dalloc<double2>((size_t)s->n_blocks * 2 * c.n_energies * ns);
-    s->flux_phase = dalloc<double2>((size_t)s->flux.chunk * c.n_energies);
-    s->half_v = dalloc<double2>((size_t)g.nth * c.n_gradient_points * g.n1);
-    launch_build_half_v(st, g, s->flux, s->pot, s->dt, s->half_v);
+      s->flux_buf = s->alloc<double2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
+    s->flux_acc = s->alloc<double2>((size_t)s->n_blocks * 2 * c.n_energies * ns);
+    s->flux_phase = s->alloc<double2>((size_t)s->flux.chunk * c.n_energies);
+    s->half_v = s->alloc<double2>((size_t)g.nth * c.n_gradient_points * g.n1);
     std::vector<double> fdw = fd_weights(c.n_gradient_points);
     for (double &x : fdw) x /= g.dr2;
-    s->fd = dupload(fdw.data(), fdw.size(), st);
-    s->flux_E = dupload(c.energies, (size_t)c.n_energies, st);
-    std::vector<double> eta((size_t)n_problems * c.n_energies);
-    for (int p = 0; p < n_problems; p++)
-      std::memcpy(&eta[(size_t)p * c.n_energies], problems[p]->CRP.eta_sq, c.n_energies * sizeof(double));
-    s->flux_eta = dupload(eta.data(), eta.size(), st);
-    s->crp = dalloc<double>((size_t)n_problems * c.n_energies);
-    s->flux_t0 = dalloc<double>(1);
-    s->flux_count = dalloc<int>(1);
-    s->flux_slot = dalloc<int>(1);
-    QD_CUDA(cudaMemsetAsync(s->flux_count, 0, sizeof(int), st));
+    s->fd = s->upload(fdw.data(), fdw.size());
+    s->flux_E = s->alloc<double>((size_t)c.n_energies);
+    s->flux_eta = s->alloc<double>((size_t)n_problems * c.n_energies);
+    s->crp = s->alloc<double>((size_t)n_problems * c.n_energies);
+    s->flux_t0 = s->alloc<double>(1);
+    s->flux_count = s->alloc<int>(1);
+    s->flux_slot = s->alloc<int>(1);
     if (s->precision == QD_PRECISION_MIXED) {
-      s->half_v_lift = dalloc<float2>((size_t)g.nth * c.n_gradient_points * g.n1);
-      launch_build_half_v_lift(st, g, s->flux, s->pot, s->dt, s->half_v_lift);
+      s->half_v_lift = s->alloc<float2>((size_t)g.nth * c.n_gradient_points * g.n1);
       std::vector<float> fdw32(fdw.begin(), fdw.end());
-      s->fdf = dupload(fdw32.data(), fdw32.size(), st);
+      s->fdf = s->upload(fdw32.data(), fdw32.size());
+    }
+  }
+  s->launches_per_step = count_launches_per_step(s);
+}
+
+// Per-call inputs of a session: the wave packets, the potential, masks,
+// quadrature weights and Legendre matrices (with the tables built from them),
+// the CRP inputs and the counters.  On a reused session (`reuse`) the tables
+// are rebuilt only when their inputs changed: the potential is compared on the
+// device (bit for bit, against the copy the tables were built from), the small
+// inputs on the host.
+static void session_load(qd_session *s, qd_fh2data *const *problems, int n_problems, bool reuse) {
+  if (reuse) validate_batch(problems, n_problems, s->probs);
+  cudaStream_t st = s->stream;
+  const Grid &g = s->g;
+  const qd_fh2data *d0 = problems[0];
+  const int64_t nth_pt = g.npt * g.nth;
+  const bool fp64 = s->precision == QD_PRECISION_FP64;
+  s->steps = d0->time.steps;
+  for (int p = 0; p < n_problems; p++) s->probs[p].d = problems[p];
+
+  // potential: compared on the device with the one the tables hold
+  bool pot_changed = !reuse;
+  if (reuse) {
+    QD_CUDA(cudaMemcpyAsync(s->pot_stage, d0->pot, (size_t)nth_pt * sizeof(double), cudaMemcpyHostToDevice, st));
+    QD_CUDA(cudaMemsetAsync(s->d_flag, 0, sizeof(int), st));
+    k_differs<<<grid_for(nth_pt, 256, 152 * 8), 256, 0, st>>>(s->pot_stage, s->pot, nth_pt, s->d_flag);
+  } else {
+    QD_CUDA(cudaMemcpyAsync(s->pot, d0->pot, (size_t)nth_pt * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  // wave packets (uploads overlap the host work below)
+  for (int p = 0; p < n_problems; p++)
+    theta_from_host(s, (int64_t)s->h_pblock0[p] * nth_pt, (int64_t)s->probs[p].n_omegas * nth_pt,
+                    problems[p]->OmegaStates.wave_packets);
+  // small inputs, compared on the host
+  auto same = [](const std::vector<double> &h, const double *x, size_t n) {
+    return h.size() == n && (n == 0 || std::memcmp(h.data(), x, n * sizeof(double)) == 0);
+  };
+  const bool w_changed = !reuse || !same(s->h_w, d0->theta.w, (size_t)g.nth);
+  const bool mask_changed =
+      s->has_mask && (!reuse || !same(s->h_d1, d0->dump1.dump, (size_t)g.n1) || !same(s->h_d2, d0->dump2.dump, (size_t)g.n2));
+  if (w_changed) {
+    s->h_w.assign(d0->theta.w, d0->theta.w + g.nth);
+    QD_CUDA(cudaMemcpyAsync(s->w, s->h_w.data(), g.nth * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  if (mask_changed) {
+    s->h_d1.assign(d0->dump1.dump, d0->dump1.dump + g.n1);
+    s->h_d2.assign(d0->dump2.dump, d0->dump2.dump + g.n2);
+    QD_CUDA(cudaMemcpyAsync(s->d1, s->h_d1.data(), g.n1 * sizeof(double), cudaMemcpyHostToDevice, st));
+    QD_CUDA(cudaMemcpyAsync(s->d2, s->h_d2.data(), g.n2 * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  // Legendre matrices of every block
+  std::vector<double> Bf(s->h_Bf.size()), Bb(s->h_Bb.size());
+  for (int b = 0; b < s->n_blocks; b++) {
+    const BlockDesc &bd = s->h_blocks[b];
+    const ProblemHost &ph = s->probs[bd.problem];
+    const qd_omega_states &om = ph.d->OmegaStates;
+    const int bi = b - s->h_pblock0[bd.problem];
+    for (int n = 0; n < bd.nl; n++)
+      for (int k = 0; k < g.nth; k++) {
+        const double P = om.associated_legendres[((int64_t)bi * om.n_cols + n) * g.nth + k];
+        Bf[bd.bmat0 + (int64_t)k * bd.nl + n] = ph.d->theta.w[k] * P;
+        Bb[bd.bmat0 + (int64_t)n * g.nth + k] = P;
+      }
+  }
+  const bool legendre_changed = !reuse || Bf != s->h_Bf || Bb != s->h_Bb;
+  if (legendre_changed) {
+    s->h_Bf.swap(Bf);
+    s->h_Bb.swap(Bb);
+    QD_CUDA(cudaMemcpyAsync(s->Bf, s->h_Bf.data(), s->h_Bf.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    QD_CUDA(cudaMemcpyAsync(s->Bb, s->h_Bb.data(), s->h_Bb.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (s->img_f) {
+      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bf, g.nth, true, s->imgoff_f, s->img_f, s->bscale_f,
+                             (s->max_nl + 15) & ~15);
+      launch_build_tc_bimage(st, s->d_blocks, s->n_blocks, s->Bb, g.nth, false, s->imgoff_b, s->img_b, s->bscale_b,
+                             (g.nth + 15) & ~15);
+    }
+  }
+  if (reuse) {
+    int flag = 0;
+    QD_CUDA(cudaMemcpyAsync(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    QD_CUDA(cudaStreamSynchronize(st));
+    if (flag) {
+      pot_changed = true;
+      QD_CUDA(cudaMemcpyAsync(s->pot, s->pot_stage, (size_t)nth_pt * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+  }
+  // tables of the potential, masks and weights
+  if (fp64 && (pot_changed || mask_changed)) {
+    launch_build_theta_table(st, g, s->pot, s->d1, s->d2, s->dt, s->tab_v);
+    launch_build_theta_table(st, g, s->pot, s->d1, s->d2, 0.5 * s->dt, s->tab_v0);
+  }
+  if (pot_changed || mask_changed || w_changed)
+    launch_build_float_tables(st, g, s->w, s->pot, s->d1, s->d2, s->T1, s->T2, s->wf, s->wvf, s->d1f, s->d2f, s->T1f,
+                              s->T2f, s->I1f, s->I2f);
+  if (!fp64 && pot_changed) {
+    launch_build_lift_theta(st, g, s->pot, s->dt, s->vph);
+    launch_build_lift_theta(st, g, s->pot, 0.5 * s->dt, s->vph0);
+  }
+  // counters and energies
+  QD_CUDA(cudaMemsetAsync(s->energies, 0, (size_t)s->n_blocks * 6 * sizeof(double), st));
+  QD_CUDA(cudaMemsetAsync(s->step_done, 0, sizeof(unsigned), st));
+  QD_CUDA(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+  QD_CUDA(cudaMemsetAsync(s->status_step, 0, sizeof(int), st));
+  QD_CUDA(cudaMemcpyAsync(s->d_step, &s->steps, sizeof(int), cudaMemcpyHostToDevice, st));
+  s->rec = nullptr;
+  s->rec_cap = 0;
+  s->rec_base = 0;
+  // flux inputs
+  s->flux_pending = 0;
+  if (s->flux.enabled) {
+    const qd_crp &c = d0->CRP;
+    const int64_t ns = (int64_t)g.nth * g.n1;
+    QD_CUDA(cudaMemcpyAsync(s->flux_E, c.energies, (size_t)c.n_energies * sizeof(double), cudaMemcpyHostToDevice, st));
+    for (int p = 0; p < n_problems; p++)
+      QD_CUDA(cudaMemcpyAsync(s->flux_eta + (size_t)p * c.n_energies, problems[p]->CRP.eta_sq,
+                              (size_t)c.n_energies * sizeof(double), cudaMemcpyHostToDevice, st));
+    QD_CUDA(cudaMemsetAsync(s->flux_count, 0, sizeof(int), st));
+    if (pot_changed) {
+      launch_build_half_v(st, g, s->flux, s->pot, s->dt, s->half_v);
+      if (s->half_v_lift) launch_build_half_v_lift(st, g, s->flux, s->pot, s->dt, s->half_v_lift);
     }
     for (int p = 0; p < n_problems; p++) {
       double2 *dst = s->flux_acc + (int64_t)s->h_pblock0[p] * 2 * c.n_energies * ns;
@@ -958,8 +1122,13 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
         QD_CUDA(cudaMemsetAsync(dst, 0, bytes, st));
     }
   }
-  s->launches_per_step = count_launches_per_step(s);
-  QD_CUDA(cudaStreamSynchronize(st));
+  QD_CUDA(cudaGetLastError());
+}
+
+static void session_create(qd_session *s, qd_fh2data *const *problems, int n_problems) {
+  session_build(s, problems, n_problems);
+  session_load(s, problems, n_problems, false);
+  QD_CUDA(cudaStreamSynchronize(s->stream));
   QD_CUDA(cudaGetLastError());
 }
 
@@ -1005,6 +1174,9 @@ static void build_chunk_graph(qd_session *s, int steps) {
   QD_CUDA(cudaGraphInstantiate(&s->graph_chunk, graph, 0));
   cudaGraphDestroy(graph);
   s->graph_steps = steps;
+  s->graph_rec = s->rec;
+  s->graph_rec_base = s->rec_base;
+  s->graph_rec_cap = s->rec_cap;
 }
 
 // Enqueue n steps without host synchronisation.
@@ -1021,7 +1193,9 @@ static void run_steps(qd_session *s, int n) {
       continue;
     }
     if (n >= chunk && s->flux_pending == 0) {
-      if (!s->graph_chunk || s->graph_steps != chunk) build_chunk_graph(s, chunk);
+      if (!s->graph_chunk || s->graph_steps != chunk || s->graph_rec != s->rec || s->graph_rec_base != s->rec_base ||
+          s->graph_rec_cap != s->rec_cap)
+        build_chunk_graph(s, chunk);
       QD_CUDA(cudaGraphLaunch(s->graph_chunk, s->stream));
       s->steps += chunk;
       n -= chunk;
@@ -1070,18 +1244,93 @@ static void print_energies(qd_session *s, const std::vector<double> &e) {
   std::printf(" Total: %.12f %.12f\n", total_module, total_energy);
 }
 
+// ------------------------------------------------------- session reuse
+// One idle session per device is kept after a qd_evolve call for the next call
+// with the same key (session_key): its buffers, key tables and step graph are
+// reused and only the per-call inputs are loaded again (session_load).  A
+// session whose device memory exceeds the limit (QD_SESSION_CACHE_BYTES, default
+// 8 GiB; 0 turns reuse off) is released at the end of its call instead.
+// qd_release_session_cache() releases the kept sessions.
+constexpr int CACHE_DEVICES = 64;
+static std::mutex g_cache_mutex;
+static qd_session *g_cache[CACHE_DEVICES] = {};   // released by qd_release_session_cache, else at exit
+
+static size_t cache_limit() {
+  const char *e = std::getenv("QD_SESSION_CACHE_BYTES");
+  if (e && *e) return (size_t)std::strtoull(e, nullptr, 10);
+  return (size_t)8 << 30;
+}
+
+static std::unique_ptr<qd_session> acquire_session(qd_fh2data *const *problems, int n) {
+  std::vector<ProblemHost> checked;
+  validate_batch(problems, n, checked);   // before reading any array the key names
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < CACHE_DEVICES) {
+    const std::vector<double> key = session_key(problems, n);
+    std::unique_ptr<qd_session> hit;
+    {
+      std::lock_guard<std::mutex> lock(g_cache_mutex);
+      if (g_cache[dev] && g_cache[dev]->key == key) {
+        hit.reset(g_cache[dev]);
+        g_cache[dev] = nullptr;
+      }
+    }
+    if (hit) {
+      session_load(hit.get(), problems, n, true);
+      return hit;
+    }
+  }
+  std::unique_ptr<qd_session> s(new qd_session());
+  session_create(s.get(), problems, n);
+  return s;
+}
+
+static void park_session(std::unique_ptr<qd_session> s) {
+  if (s->device < 0 || s->device >= CACHE_DEVICES || s->arena.total > cache_limit()) return;
+  qd_session *old = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mutex);
+    old = g_cache[s->device];
+    g_cache[s->device] = s.release();
+  }
+  delete old;
+}
+
+static void release_session_cache() {
+  std::vector<qd_session *> all;
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mutex);
+    for (qd_session *&c : g_cache)
+      if (c) {
+        all.push_back(c);
+        c = nullptr;
+      }
+  }
+  for (qd_session *c : all) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(c->device);
+    delete c;
+    cudaSetDevice(cur);
+  }
+}
+
 // The evolution loop of test_multiple_cards with callbacks and outputs.
 static void evolve(qd_fh2data *const *problems, int n, qd_callback cb, void *user) {
-  std::unique_ptr<qd_session> s(new qd_session());
-  session_build(s.get(), problems, n);
+  std::unique_ptr<qd_session> s = acquire_session(problems, n);
   const qd_fh2data *d0 = problems[0];
   const int total = d0->time.total_steps;
   const qd_options &op = d0->options;
   const bool want_rec = op.energies != nullptr;
   if (want_rec && total > 0) {
+    const size_t need = (size_t)total * s->n_blocks * 6;
+    if (s->rec_buf_cap < need) {
+      s->rec_buf = s->alloc<double>(need);
+      s->rec_buf_cap = need;
+    }
     s->rec_cap = total;
     s->rec_base = s->steps;
-    s->rec = dalloc<double>((size_t)total * s->n_blocks * 6);
+    s->rec = s->rec_buf;
   }
   const int every = op.wave_to_matlab ? op.steps_to_copy_psi_from_device_to_host : 0;
   int done = 0;
@@ -1130,6 +1379,7 @@ static void evolve(qd_fh2data *const *problems, int n, qd_callback cb, void *use
         std::memcpy(out + ((size_t)t * nb) * 6, &r[((size_t)t * s->n_blocks + b0) * 6], (size_t)nb * 6 * sizeof(double));
     }
   }
+  park_session(std::move(s));
 }
 
 // ---------------------------------------------------------------- C ABI
@@ -1171,10 +1421,12 @@ int qd_session_create(qd_fh2data *const *problems, int32_t n_problems, qd_sessio
     QD_REQUIRE(out != nullptr, "out != NULL");
     *out = nullptr;
     std::unique_ptr<qd_session> s(new qd_session());
-    session_build(s.get(), problems, n_problems);
+    session_create(s.get(), problems, n_problems);
     *out = s.release();
   })
 }
+
+int qd_release_session_cache(void) { QD_GUARD(release_session_cache()) }
 
 int qd_session_destroy(qd_session *s) {
   QD_GUARD(delete s)

@@ -1,0 +1,74 @@
+"""Reuse of the device state between qd_evolve calls of the same shape.
+
+A call parks its session; the next call with the same grids, time step, precision,
+Omega lists and flux surface reloads only its own inputs into it, and rebuilds the
+tables whose inputs changed (potential compared on the device, masks, weights and
+Legendre matrices on the host).  Every result must equal, bit for bit, that of a
+fresh session on the same inputs.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(qd, cfg, prec, modify=None, record=False):
+    d = qd.inputs.build_fh2data(cfg)
+    d["options"]["precision"] = prec
+    if modify:
+        modify(d)
+    if record:
+        nb = len(np.ravel(d["OmegaStates"]["omegas"]))
+        d["options"]["energies"] = np.zeros((cfg.total_steps, nb, 6))
+    qd.cudaOpenMPEvolution(d)
+    return d
+
+
+def _same(a, b):
+    assert np.array_equal(a["OmegaStates"]["wave_packets"], b["OmegaStates"]["wave_packets"])
+    assert np.array_equal(a["CRP"]["CRP"], b["CRP"]["CRP"])
+    assert int(a["time"]["steps"]) == int(b["time"]["steps"])
+
+
+def _deeper_pot(d):
+    d["pot"] = np.ascontiguousarray(d["pot"] * 1.01)
+
+
+def _other_masks(d):
+    d["dump1"]["dump"] = np.ascontiguousarray(d["dump1"]["dump"] ** 2)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])
+def test_reused_session_equals_fresh_session(qd, lib, prec):
+    # 70 steps: step 0, one 64-step graph chunk and five single steps
+    cfg = qd.inputs.small_config(J=2, parity=0, n1=32, n2=16, n_theta=8, l_max=6, steps=70, n_energies=8)
+    fresh = {}
+    for name, mod, rec in (("pot", _deeper_pot, True), ("mask", _other_masks, False), ("same", None, False)):
+        qd.release_session_cache()
+        fresh[name] = _run(qd, cfg, prec, mod, rec)
+    qd.release_session_cache()
+    _same(_run(qd, cfg, prec), fresh["same"])          # parks a session
+    b = _run(qd, cfg, prec, _deeper_pot, True)           # another potential, energies recorded
+    _same(b, fresh["pot"])
+    assert np.array_equal(b["options"]["energies"], fresh["pot"]["options"]["energies"])
+    _same(_run(qd, cfg, prec, _other_masks), fresh["mask"])
+    _same(_run(qd, cfg, prec), fresh["same"])            # and back to the first inputs
+    qd.release_session_cache()
+
+
+def test_reuse_resumes_across_calls(qd, lib):
+    """time.steps and the flux accumulators carried over two calls on one kept session
+    equal one call of twice the steps."""
+    cfg = qd.inputs.small_config(J=0, n1=32, n2=16, n_theta=8, l_max=6, steps=80, n_energies=8)
+    qd.release_session_cache()
+    whole = _run(qd, cfg, 1)
+    d = qd.inputs.build_fh2data(cfg)
+    d["options"]["precision"] = 1
+    d["time"]["total_steps"] = 40
+    d["CRP"]["accumulators"] = np.zeros((1, 2, 8, cfg.n_theta, cfg.n1), np.complex128)
+    qd.cudaOpenMPEvolution(d)
+    qd.cudaOpenMPEvolution(d)
+    assert int(d["time"]["steps"]) == 80
+    assert np.linalg.norm(d["OmegaStates"]["wave_packets"] - whole["OmegaStates"]["wave_packets"]) <= \
+        1e-6 * np.linalg.norm(whole["OmegaStates"]["wave_packets"])
+    qd.release_session_cache()
