@@ -1286,12 +1286,13 @@ static std::unique_ptr<qd_session> acquire_session(qd_fh2data *const *problems, 
 }
 
 static void park_session(std::unique_ptr<qd_session> s) {
-  if (s->device < 0 || s->device >= CACHE_DEVICES || s->arena.total > cache_limit()) return;
+  const int dev = s->device;
+  if (dev < 0 || dev >= CACHE_DEVICES || s->arena.total > cache_limit()) return;
   qd_session *old = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_cache_mutex);
-    old = g_cache[s->device];
-    g_cache[s->device] = s.release();
+    old = g_cache[dev];
+    g_cache[dev] = s.release();
   }
   delete old;
 }
