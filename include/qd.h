@@ -89,6 +89,9 @@ typedef struct qd_options {
   double *energies;           /* optional out: [total_steps][n_omegas][6] =
                                  module, potential, kinetic, rotational,
                                  coriolis, total (wavepackets1device.cu:442-451) */
+  const char *autotune_cache; /* optional file of the autotuner's kernel choices
+                                 (NULL: the QD_AUTOTUNE_CACHE environment
+                                 variable, else kept in the process only) */
 } qd_options;
 
 /* dump1 / dump2 absorbing masks: matlabStructures.C:67-72 (NULL = absent) */
@@ -259,6 +262,10 @@ int qd_rotational_energy_noalloc(const double *psi_j, int32_t n1, int32_t n2, in
    names receives the kernel names separated by '\n'. */
 int qd_session_profile(qd_session *s, int32_t n_steps, char *names, size_t names_cap, double *avg_ms,
                        int32_t *launches, int32_t max_kernels, int32_t *n_kernels);
+
+/* What the autotuner chose for this session's mixed-form FFT (kernel, and the
+   measured microseconds per launch of every candidate, or "cached"), as text. */
+int qd_session_tuning(qd_session *s, char *text, size_t text_cap);
 
 /* Self-test of the bounded device-side wait that every pipelined kernel of the
    library uses: one CTA waits on an mbarrier with a budget of budget_ms.  With

@@ -60,7 +60,8 @@ class EvolutionTime(C.Structure):
 class Options(C.Structure):
     _fields_ = [("wave_to_matlab", C.c_char_p), ("test_name", C.c_char_p),
                 ("steps_to_copy_psi_from_device_to_host", C.c_int32), ("use_p2p_async", C.c_int32),
-                ("precision", C.c_int32), ("print_energies", C.c_int32), ("energies", C.POINTER(C.c_double))]
+                ("precision", C.c_int32), ("print_energies", C.c_int32), ("energies", C.POINTER(C.c_double)),
+                ("autotune_cache", C.c_char_p)]
 
 
 class DumpFunction(C.Structure):
@@ -96,7 +97,7 @@ EXPORTED = ("qd_evolve", "qd_evolve_batch", "qd_release_session_cache", "qd_last
             "qd_session_destroy", "qd_session_run", "qd_session_synchronize", "qd_session_flush", "qd_session_download",
             "qd_session_upload", "qd_session_stream", "qd_session_info", "qd_session_apply", "qd_session_get_psi",
             "qd_session_set_psi", "qd_session_get_energies", "qd_session_profile", "qd_device_fma_peaks",
-            "qd_device_wait_selftest",
+            "qd_device_wait_selftest", "qd_session_tuning",
             "qd_rotational_energy_noalloc")
 
 
@@ -137,6 +138,7 @@ def load_library():
                                        P(C.c_int32), C.c_int32, P(C.c_int32)]
     lib.qd_device_fma_peaks.argtypes = [P(C.c_double), P(C.c_double)]
     lib.qd_device_wait_selftest.argtypes = [C.c_double, C.c_int32]
+    lib.qd_session_tuning.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     lib.qd_rotational_energy_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                                  C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                                  C.c_double, C.c_void_p, C.c_void_p]
@@ -193,9 +195,11 @@ class _Marshalled:
         en = op.get("energies")
         if en is not None:
             self._out(en, np.float64)
+        atc = op.get("autotune_cache")
+        self.atc = str(atc).encode() if atc else None
         s.options = Options(self.wtm, self.tn, int(op.get("steps_to_copy_psi_from_device_to_host", 0)),
                             int(op.get("use_p2p_async", 0)), int(op.get("precision", 0)),
-                            int(op.get("print_energies", 0)), _dptr(en))
+                            int(op.get("print_energies", 0)), _dptr(en), self.atc)
         for key in ("dump1", "dump2"):
             dm = d.get(key)
             arr = None if dm is None or dm.get("dump") is None else self._in(dm["dump"])
@@ -374,6 +378,12 @@ class Session:
         _check(self.lib.qd_session_profile(self.h, int(n_steps), names, 4096, avg, cnt, 64, C.byref(nk)))
         keys = names.value.decode().split("\n")
         return {k: {"ms": avg[i], "per_step": cnt[i] / n_steps} for i, k in enumerate(keys[: nk.value])}
+
+    def tuning(self) -> str:
+        """The autotuner's choice of FFT kernel for this session (and its timings)."""
+        buf = C.create_string_buffer(8192)
+        _check(self.lib.qd_session_tuning(self.h, buf, 8192))
+        return buf.value.decode()
 
     def energies(self) -> np.ndarray:
         out = np.empty((self.n_blocks, 6))

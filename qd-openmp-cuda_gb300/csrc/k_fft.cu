@@ -664,7 +664,7 @@ __device__ __forceinline__ void tw_apply(float2 &v, const float2 *tab, int e, in
 // floats2 at Xr + q RS, used as the row transposition buffer and then as the
 // row the other CTAs gather from.  Column transposition buffer Sc[k1][j][col].
 template <int A, int B1, int B2, int THREADS>
-__global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(float2 *__restrict__ psi, Grid g,
+__global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_fft_slab_sep(float2 *__restrict__ psi, Grid g,
                                                              const SlabDesc *__restrict__ slabs,
                                                              const float2 *__restrict__ tw1,
                                                              const float2 *__restrict__ tw2, FFTLift lf,
@@ -845,7 +845,9 @@ __global__ void __launch_bounds__(THREADS, 3) k_fft_slab_sep(float2 *__restrict_
 }
 
 namespace {
-// instantiations of the separable slab FFT: (n1, n2) -> (A, B1, B2, threads)
+// instantiations of the separable slab FFT: (n1, n2) -> (A, B1, B2, threads).  Several
+// thread counts (and so cluster sizes, C = A B2 B1 / threads CTAs per slab) exist for the
+// production grids; the autotuner times them on the session's own slabs.
 struct SepShape {
   int n1, n2, A, B1, B2, threads;
 };
@@ -855,6 +857,10 @@ constexpr SepShape kSepShapes[] = {
     {64, 32, 8, 8, 4, 128},
     {32, 16, 8, 4, 2, 32},
     {16, 8, 4, 4, 2, 32},
+    {256, 128, 16, 16, 8, 512},
+    {256, 128, 16, 16, 8, 128},
+    {192, 96, 24, 8, 4, 192},
+    {192, 96, 24, 8, 4, 384},
 };
 constexpr int kNumSep = (int)(sizeof(kSepShapes) / sizeof(kSepShapes[0]));
 
@@ -872,6 +878,8 @@ template <int A, int B1, int B2, int T>
 void sep_set_attr() {
   QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sep_smem_bytes<A, B1, B2, T>()));
+  if (sep_cluster<A, B1, B2, T>() > 8)
+    QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
 }
 
 template <int A, int B1, int B2, int T>
@@ -894,22 +902,31 @@ void sep_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, 
                              (const float2 *)p.tw2_f, lf, ke_part, re_part, fscale, scale, status));
 }
 
+#define QD_SEP_CASES(X)  \
+  X(0, 16, 16, 8, 256)   \
+  X(1, 24, 8, 4, 96)     \
+  X(2, 8, 8, 4, 128)     \
+  X(3, 8, 4, 2, 32)      \
+  X(4, 4, 4, 2, 32)      \
+  X(5, 16, 16, 8, 512)   \
+  X(6, 16, 16, 8, 128)   \
+  X(7, 24, 8, 4, 192)    \
+  X(8, 24, 8, 4, 384)
+
 void sep_dispatch_attr(int id) {
   switch (id) {
-    case 0: sep_set_attr<16, 16, 8, 256>(); break;
-    case 1: sep_set_attr<24, 8, 4, 96>(); break;
-    case 2: sep_set_attr<8, 8, 4, 128>(); break;
-    case 3: sep_set_attr<8, 4, 2, 32>(); break;
-    case 4: sep_set_attr<4, 4, 2, 32>(); break;
+#define QD_X(i, a, b1, b2, t) \
+  case i: sep_set_attr<a, b1, b2, t>(); break;
+    QD_SEP_CASES(QD_X)
+#undef QD_X
   }
 }
 int sep_dispatch_cluster(int id) {
   switch (id) {
-    case 0: return sep_cluster<16, 16, 8, 256>();
-    case 1: return sep_cluster<24, 8, 4, 96>();
-    case 2: return sep_cluster<8, 8, 4, 128>();
-    case 3: return sep_cluster<8, 4, 2, 32>();
-    case 4: return sep_cluster<4, 4, 2, 32>();
+#define QD_X(i, a, b1, b2, t) \
+  case i: return sep_cluster<a, b1, b2, t>();
+    QD_SEP_CASES(QD_X)
+#undef QD_X
   }
   return 0;
 }
@@ -917,11 +934,10 @@ void sep_dispatch_launch(int id, cudaStream_t s, const Grid &g, const FFTPlan &p
                          const SlabDesc *slabs, int n_slabs, const FFTLift &lf, double *ke_part, double *re_part,
                          float fscale, double scale, const int *status) {
   switch (id) {
-    case 0: sep_launch<16, 16, 8, 256>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
-    case 1: sep_launch<24, 8, 4, 96>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
-    case 2: sep_launch<8, 8, 4, 128>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
-    case 3: sep_launch<8, 4, 2, 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
-    case 4: sep_launch<4, 4, 2, 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+#define QD_X(i, a, b1, b2, t) \
+  case i: sep_launch<a, b1, b2, t>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+    QD_SEP_CASES(QD_X)
+#undef QD_X
   }
 }
 }  // namespace
@@ -967,11 +983,14 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
   p.cluster = choose_cluster(n1, n2);
   p.sep = -1;
   p.sep_cluster = 0;
-  for (int q = 0; q < kNumSep; q++)
-    if (kSepShapes[q].n1 == n1 && kSepShapes[q].n2 == n2) {
-      p.sep = q;
-      p.sep_cluster = sep_dispatch_cluster(q);
-    }
+  // mixed-form candidates in order of preference without timing: separable shapes
+  // (first instantiated first), the two-exchange cluster kernel, the three-pass kernels
+  p.n_cand = 0;
+  for (int q = 0; q < kNumSep && p.n_cand < FFT_MAX_CANDIDATES - 2; q++)
+    if (kSepShapes[q].n1 == n1 && kSepShapes[q].n2 == n2) p.cand[p.n_cand++] = FFT_SEP0 + q;
+  if (p.cluster) p.cand[p.n_cand++] = FFT_CLUSTER;
+  p.cand[p.n_cand++] = FFT_THREE_PASS;
+  fft_plan_choose(p, p.cand[0]);
   p.rows_per_cta = largest_divisor_at_most(n2, std::max(1, FFT_THREADS * MAXV / n1));
   p.rows_per_cta = std::min(p.rows_per_cta, largest_divisor_at_most(n2, 64));
   p.cols_per_cta = largest_divisor_at_most(n1, std::min(32, std::max(1, FFT_THREADS * MAXV / n2)));
@@ -1003,7 +1022,27 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
   QD_CUDA(cudaFuncSetAttribute(k_fft_slab_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   if (p.cluster > 1)
     QD_CUDA(cudaFuncSetAttribute(k_fft_slab_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 0));
-  if (p.sep >= 0) sep_dispatch_attr(p.sep);
+  for (int q = 0; q < p.n_cand; q++)
+    if (p.cand[q] >= FFT_SEP0) sep_dispatch_attr(p.cand[q] - FFT_SEP0);
+}
+
+void fft_plan_choose(FFTPlan &p, int choice) {
+  p.choice = choice;
+  p.sep = choice >= FFT_SEP0 ? choice - FFT_SEP0 : -1;
+  p.sep_cluster = p.sep >= 0 ? sep_dispatch_cluster(p.sep) : 0;
+  p.use_cluster = choice == FFT_CLUSTER;
+}
+
+std::string fft_choice_name(int choice) {
+  std::string name;
+  if (choice >= FFT_SEP0) {
+    const SepShape &q = kSepShapes[choice - FFT_SEP0];
+    name = "separable A=" + std::to_string(q.A) + " B1=" + std::to_string(q.B1) + " B2=" + std::to_string(q.B2) +
+           " threads=" + std::to_string(q.threads) + " cluster=" + std::to_string(sep_dispatch_cluster(choice - FFT_SEP0));
+  } else {
+    name = choice == FFT_CLUSTER ? "cluster two-exchange" : "three-pass";
+  }
+  return name + " [" + std::to_string(choice) + "]";
 }
 
 void fft_plan_free(FFTPlan &p) {
@@ -1019,11 +1058,20 @@ void fft_plan_free(FFTPlan &p) {
 // the cluster, the three-pass forms one per column / row tile
 int fft_col_tiles(const FFTPlan &p, int precision) {
   if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_cluster;
-  return (precision == QD_PRECISION_MIXED && p.cluster) ? p.cluster : p.n1 / p.cols_per_cta;
+  return (precision == QD_PRECISION_MIXED && p.use_cluster) ? p.cluster : p.n1 / p.cols_per_cta;
 }
 int fft_row_tiles(const FFTPlan &p, int precision) {
   if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_cluster;
-  return (precision == QD_PRECISION_MIXED && p.cluster) ? p.cluster : p.n2 / p.rows_per_cta;
+  return (precision == QD_PRECISION_MIXED && p.use_cluster) ? p.cluster : p.n2 / p.rows_per_cta;
+}
+// partial-sum tiles per slab of any mixed-form candidate (buffers sized for tuning)
+int fft_max_tiles(const FFTPlan &p) {
+  int t = std::max(p.n1 / p.cols_per_cta, p.n2 / p.rows_per_cta);
+  for (int q = 0; q < p.n_cand; q++) {
+    if (p.cand[q] >= FFT_SEP0) t = std::max(t, sep_dispatch_cluster(p.cand[q] - FFT_SEP0));
+    if (p.cand[q] == FFT_CLUSTER) t = std::max(t, p.cluster);
+  }
+  return t;
 }
 
 
@@ -1065,7 +1113,7 @@ static void launch_fft_kinetic_t(cudaStream_t s, const Grid &g, const FFTPlan &p
     prof_mark(s, "fft_slab");
     return;
   }
-  if (p.cluster && lf && lf->kinR) {
+  if (p.use_cluster && lf && lf->kinR) {
     const int C = p.cluster;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)(n_slabs * C));

@@ -83,25 +83,38 @@ __device__ inline void mma_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
+// tcgen05.ld of 16 columns into r without waiting; tmem_wait_ld then waits for
+// every load of the thread, and reg_after_wait orders each destination register
+// after that wait (an empty volatile asm the register passes through)
+__device__ inline void tmem_ld16(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ inline void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ inline void reg_after_wait(uint32_t &x) { asm volatile("" : "+r"(x)); }
 
 __host__ __device__ inline int round16(int x) { return (x + 15) & ~15; }
 
+// products a_i * b_j with i + j <= 2
+__constant__ int c_pair_a[6] = {0, 0, 1, 0, 1, 2};
+__constant__ int c_pair_b[6] = {0, 1, 0, 2, 1, 0};
 }  // namespace
 
 // byte size of the B image of one block: 3 terms x Npad x Kpad BF16
 __host__ __device__ inline int64_t tc_bimg_bytes(int Np, int Kp) { return 3LL * Np * Kp * 2; }
 
-// The N columns of a tile are issued and drained in two halves of N0 and
-// Np - N0 columns (multiples of 16, the second possibly empty), each with its
-// own three TMEM accumulators, so that one half's MMA chain overlaps the drain
-// of the other.
-__host__ __device__ inline int tc_split(int Np) { return Np >= 32 ? (((Np / 2) + 15) & ~15) : Np; }
+// TMEM columns for three Np-wide accumulators (power of two >= 32)
+__host__ __device__ inline uint32_t tc_tmem_cols(int Np) {
+  const int need = 3 * Np;
+  return need <= 32 ? 32u : need <= 64 ? 64u : need <= 128 ? 128u : need <= 256 ? 256u : 512u;
+}
 
 // ---------------------------------------------------------------------------
-// B images, per column half h (columns [0, N0) and [N0, Np)), each half with
-// its three terms adjacent: element (n, k) of term t, n = hbase + nn, at
-//   hoff + t*(Nh/8)*SBO + (nn/8)*SBO + (k/8)*128 + (nn%8)*16 + (k%8)*2 bytes,
-// SBO = Kp/8*128 (SWIZZLE_NONE, K-major), hoff = 3*(N0/8)*SBO for h = 1.
+// B images: element (n, k) of term t at t*Np*Kp*2 + (n/8)*SBO + (k/8)*128 +
+// (n%8)*16 + (k%8)*2 bytes with SBO = Kp/8*128 (SWIZZLE_NONE, K-major).
 // fwd: B(n = l, k = theta) = w_k P_l(x_k) = Bf[k*nl + n]
 // bwd: B(n = theta, k = l) = P_l(x_n)     = Bb[k*nth + n]
 // One CTA per (block, column n): the column scale t_n = 2^e (smallest power
@@ -117,15 +130,12 @@ __global__ void k_build_tc_bimage(const BlockDesc *__restrict__ blocks, const do
   if (n >= Np) return;
   uint16_t *out = img + img_off[blockIdx.y] / 2;
   const int SBOe = Kp / 8 * 64;   // in elements
-  const int N0 = tc_split(Np);
-  const int h = n < N0 ? 0 : 1, nn = h ? n - N0 : n, Nh = h ? Np - N0 : N0;
-  const int64_t hoff = h ? 3LL * (N0 / 8) * SBOe : 0;
-  const int64_t term = (int64_t)(Nh / 8) * SBOe;
   auto val = [&](int k) -> double {
     if (n >= Nv || k >= Kv) return 0.0;
     return fwd ? Bsrc[bd.bmat0 + (int64_t)k * bd.nl + n] : Bsrc[bd.bmat0 + (int64_t)k * nth + n];
   };
-  // block-wide max |B(n, :)|
+  // block-wide max |B(n, :)| (max via -sum of negated maxima is not needed: use a
+  // shared reduction with fmax)
   double mx = 0.0;
   for (int k = threadIdx.x; k < Kp; k += blockDim.x) mx = fmax(mx, fabs(val(k)));
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
@@ -148,10 +158,10 @@ __global__ void k_build_tc_bimage(const BlockDesc *__restrict__ blocks, const do
     const double r1 = (b - i0) * 256.0;
     const double i1 = rint(r1);
     const double i2 = rint((r1 - i1) * 256.0);
-    const int64_t el = hoff + (int64_t)(nn / 8) * SBOe + (k / 8) * 64 + (nn % 8) * 8 + (k % 8);
+    const int64_t el = (int64_t)(n / 8) * SBOe + (k / 8) * 64 + (n % 8) * 8 + (k % 8);
     out[el] = __bfloat16_as_ushort(__double2bfloat16(i0));
-    out[term + el] = __bfloat16_as_ushort(__double2bfloat16(i1));
-    out[2 * term + el] = __bfloat16_as_ushort(__double2bfloat16(i2));
+    out[(int64_t)Np * Kp + el] = __bfloat16_as_ushort(__double2bfloat16(i1));
+    out[2LL * Np * Kp + el] = __bfloat16_as_ushort(__double2bfloat16(i2));
   }
 }
 
@@ -185,9 +195,22 @@ __device__ inline void rot_lift2(float &x, float &y, float2 ts) {
 }
 
 
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised form.  Each CTA walks a contiguous range of
+// (block, 64-point tile) pairs.  Warps 0-7 (producers) stage and slice tile
+// t+1 while warps 8-15 (consumers) drain tile t from TMEM; consumer thread
+// MMA_ISSUER issues the MMA chain of each tile.  Three mbarriers carry the
+// hand-offs:
+//   slices_ready (256 producer arrivals)  -> the MMA may read A/B slices
+//   mma_done     (tcgen05.commit)         -> TMEM holds tile t; A/B reusable
+//   tmem_free    (256 consumer arrivals)  -> the next MMA may overwrite TMEM
+// Every wait is bounded (1 s, qd_mbarrier.cuh); a timeout sets QD_ERR_TIMEOUT
+// in the status word and the CTA stops issuing work, waits (bounded) for its
+// MMAs, frees TMEM and returns.
+__device__ inline void named_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 struct TcTile {
-  int b, mt, Kv, Nv, Kp, Np, N0;
-  uint32_t SBO, A_TERM;
+  int b, mt, Kv, Nv, Kp, Np;
+  uint32_t SBO, A_TERM, B_TERM;
 };
 
 template <bool FWD>
@@ -200,46 +223,11 @@ __device__ inline TcTile tc_tile(const TcArgs &P, int tt, int mtiles) {
   t.Nv = FWD ? nl : P.g.nth;
   t.Kp = round16(t.Kv);
   t.Np = round16(t.Nv);
-  t.N0 = tc_split(t.Np);
   t.SBO = (uint32_t)(t.Kp / 8 * 128);
   t.A_TERM = 16u * t.SBO;
+  t.B_TERM = (uint32_t)(t.Np / 8) * t.SBO;
   return t;
 }
-
-// A wait that also gives up when another warp has already recorded a failure.
-__device__ inline bool wait_or_abort(uint32_t a, uint32_t parity, const volatile int *abort_all) {
-  const uint64_t t0 = globaltimer();
-  while (!mbar_try_wait(a, parity)) {
-    if (*abort_all) return false;
-    if (globaltimer() - t0 > WAIT_NS) return false;
-  }
-  return true;
-}
-
-// The MMA chain of one column half (Nh columns at column cb of TMEM, its B
-// terms from byte bh of the B image): four tcgen05.mma per K = 16 step.  The
-// half's B0 and B1 are adjacent in shared memory and its D0, D1, D2 in TMEM, so
-// A0 [B0 B1] -> [D0 D1] and A1 [B0 B1] -> [D1 D2] are single N = 2 Nh MMAs.
-__device__ inline void tc_issue_half(uint32_t tmem, uint32_t a0, uint32_t bh, const TcTile &T, int Nh, uint32_t cb) {
-  const uint32_t idesc = make_idesc(128, Nh), idesc2 = make_idesc(128, 2 * Nh);
-  const uint32_t bterm = (uint32_t)(Nh / 8) * T.SBO;
-  for (int s = 0; s < T.Kp / 16; s++) {
-    const uint32_t acc = s > 0 ? 1u : 0u;
-    const uint64_t bd01 = make_desc(bh + s * 256, 128, T.SBO);
-    const uint64_t ad0 = make_desc(a0 + s * 256, 128, T.SBO);
-    mma_bf16(tmem + cb, ad0, bd01, idesc2, acc);
-    mma_bf16(tmem + cb + (uint32_t)(2 * Nh), ad0, make_desc(bh + 2 * bterm + s * 256, 128, T.SBO), idesc, acc);
-    mma_bf16(tmem + cb + (uint32_t)Nh, make_desc(a0 + T.A_TERM + s * 256, 128, T.SBO), bd01, idesc2, 1u);
-    mma_bf16(tmem + cb + (uint32_t)(2 * Nh), make_desc(a0 + 2 * T.A_TERM + s * 256, 128, T.SBO), bd01, idesc, 1u);
-  }
-}
-
-__device__ inline void tmem_ld8(uint32_t taddr, uint32_t *r) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-}
-__device__ inline void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 constexpr int WS_THREADS = 512;      // 8 producer warps + 8 consumer warps
 // FP32 staging of one A tile, k-major: element (k, point pl, re/im c) at
@@ -247,41 +235,22 @@ constexpr int WS_THREADS = 512;      // 8 producer warps + 8 consumer warps
 // the loader's stores (32 consecutive points) and the slicer's loads (8
 // points x re/im x two k-groups 8 apart) fall in 32 distinct banks.
 constexpr int TC_LDM = 162, TC_IM = 72;
-// consumer thread that issues the MMA chains: not thread 0, which forms the
+// consumer thread that issues the MMA chain: not thread 0, which forms the
 // backward kernel's per-tile module/potential sums after each epilogue
 constexpr int MMA_ISSUER = 32;
 constexpr int WS_PROD = 256;
-constexpr int WS_CONS = WS_THREADS - WS_PROD;
-
-// ---------------------------------------------------------------------------
-// Persistent, warp-specialised form.  Each CTA walks a contiguous range of
-// (block, 64-point tile) pairs.  Warps 0-7 (producers) stage and slice tile
-// t+1 while warps 8-15 (consumers) drain tile t from TMEM.  The columns of a
-// tile are handled in two halves with separate accumulators: the consumers
-// drain half 0 of tile t, then consumer thread MMA_ISSUER issues half 0 of tile
-// t+1 into the freed accumulators while the others drain half 1 of tile t, and
-// so on.  mbarriers carry the hand-offs:
-//   ready          (256 producer arrivals)   -> the MMAs may read A/B slices
-//   done[h]        (tcgen05.commit)          -> TMEM half h holds its tile;
-//                                               done[1]: A/B reusable
-//   free[h]        (256 consumer arrivals)   -> half h may be overwritten
-// Every wait is bounded (1 s, qd_mbarrier.cuh) and also gives up once another
-// warp has recorded a failure; a failure sets QD_ERR_TIMEOUT in the status word
-// and the CTA stops issuing work, waits (bounded) for the MMAs it issued, frees
-// TMEM and returns.
-__device__ inline void named_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 
 template <bool FWD>
 __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int mtiles, int n_tiles, int kp_max,
                                                                    int np_max) {
   if (P.status && *P.status) return;
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t mb_ready, mb_done[2], mb_free[2];
+  __shared__ uint64_t mb_ready, mb_done, mb_free;
   __shared__ uint32_t tmem_base_s;
   __shared__ float srow_s[2][128];
   __shared__ float red_s[16];
   __shared__ float tsc_s[256], w_s[256];   // consumers: column scales and (backward) weights of the block
-  __shared__ int abort_p, abort_all, n_issued[2];
+  __shared__ int abort_p, abort_c, n_issued;
   const Grid &g = P.g;
   const uint32_t a_term_max = 16u * (uint32_t)(kp_max / 8 * 128);
   const uint32_t b_term_max = (uint32_t)(np_max / 8) * (uint32_t)(kp_max / 8 * 128);
@@ -297,21 +266,17 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   if (warp == 0) tmem_alloc(smem_u32(&tmem_base_s), ncols);
   if (tid == 0) {
     mbar_init(smem_u32(&mb_ready), WS_PROD);
-    mbar_init(smem_u32(&mb_done[0]), 1);
-    mbar_init(smem_u32(&mb_done[1]), 1);
-    mbar_init(smem_u32(&mb_free[0]), WS_CONS);
-    mbar_init(smem_u32(&mb_free[1]), WS_CONS);
+    mbar_init(smem_u32(&mb_done), 1);
+    mbar_init(smem_u32(&mb_free), WS_THREADS - WS_PROD);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_p = 0;
-    abort_all = 0;
-    n_issued[0] = 0;
-    n_issued[1] = 0;
+    abort_c = 0;
+    n_issued = 0;
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
-  volatile int *abort_v = &abort_all;
 
   if (tid < WS_PROD) {
     // =============================== producers: 256 threads, two per row
@@ -372,16 +337,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         }
       }
       named_bar(1, WS_PROD);
-      // every MMA of the previous tile must be done before A (and B) are rewritten;
+      // the MMA of the previous tile must be done before A (and B) are rewritten;
       // one thread waits and the group decides together (no divergent exit)
-      if (tid == 0) {
-        bool ok = !*abort_v;
-        if (ok && it > 0) ok = wait_or_abort(smem_u32(&mb_done[1]), (uint32_t)((it - 1) & 1), abort_v);
-        if (!ok) {
-          if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
-          abort_all = 1;
-          abort_p = 1;
-        }
+      if (tid == 0 && it > 0 && !mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((it - 1) & 1))) {
+        if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
+        abort_p = 1;
       }
       named_bar(1, WS_PROD);
       if (abort_p) break;
@@ -440,47 +400,22 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       named_bar(1, WS_PROD);   // sF is rewritten only after every producer has sliced
     }
   } else {
-    // =============================== consumers: 256 threads (+ the MMA issuer, thread 256 + 32)
+    // =============================== consumers: 256 threads (+ the MMA issuer, thread 256)
     const int ctid = tid - WS_PROD, cw = warp - WS_PROD / 32;
     const int quarter = warp & 3, chalf = cw >> 2;
     const int m = 32 * quarter + lane;
     const int pl = m >> 1, c = m & 1;
-    const bool issuer = ctid == MMA_ISSUER;
-    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-    // issues half h of tile number it (tile index tt) after its accumulators are free
-    // Every tile advances each barrier by exactly one phase (waits use parity it & 1):
-    // a tile without a second half still commits to done[1] (it then arrives once the
-    // first half's MMAs are complete) and its consumers still arrive on free[1].
-    auto issue = [&](int it, int tt, int h) -> bool {
-      const TcTile T = tc_tile<FWD>(P, tt, mtiles);
-      const int Nh = h ? T.Np - T.N0 : T.N0;
-      bool ok = !*abort_v;
-      if (ok && h == 0) ok = wait_or_abort(smem_u32(&mb_ready), (uint32_t)(it & 1), abort_v);
-      if (ok && it > 0 && Nh > 0) ok = wait_or_abort(smem_u32(&mb_free[h]), (uint32_t)((it - 1) & 1), abort_v);
-      if (!ok) return false;
-      tc_fence_after();
-      if (Nh > 0)
-        tc_issue_half(tmem, a0, b0 + (h ? 3u * (uint32_t)(T.N0 / 8) * T.SBO : 0u), T, Nh, h ? 3u * T.N0 : 0u);
-      mma_commit(smem_u32(&mb_done[h]));
-      n_issued[h] = it + 1;
-      return true;
-    };
-    auto fail = [&]() {
-      if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
-      abort_all = 1;
-    };
-    if (issuer && t_begin < t_end && !(issue(0, t_begin, 0) && issue(0, t_begin, 1))) fail();
     int cons_b = -1;
     for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
       const TcTile T = tc_tile<FWD>(P, tt, mtiles);
       const BlockDesc bd = P.blocks[T.b];
       const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
       // backward: the tile's w V values [n][64 points], copied asynchronously into
-      // shared memory, 16 bytes (4 points) per copy spread over all consumer threads
-      // (a 4-byte copy per point where the tile ends early)
+      // shared memory before the MMA wait, 16 bytes (4 points) per copy spread over
+      // all consumer threads (a 4-byte copy per point where the tile ends early)
       if (!FWD) {
         const int64_t p0 = (int64_t)T.mt * TC_POINTS;
-        for (int q = ctid; q < T.Nv * (TC_POINTS / 4); q += WS_CONS) {
+        for (int q = ctid; q < T.Nv * (TC_POINTS / 4); q += WS_THREADS - WS_PROD) {
           const int n = q / (TC_POINTS / 4), c4 = 4 * (q % (TC_POINTS / 4));
           const float *src = P.wv + (int64_t)n * g.npt + p0 + c4;
           const uint32_t dst = smem_u32(sWV + n * TC_POINTS + c4);
@@ -492,79 +427,108 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
           }
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
-        asm volatile("cp.async.wait_all;" ::: "memory");   // this thread's w V copies have landed
       }
-      named_bar(2, WS_CONS);   // ... and so have everyone's; abort decisions are uniform here
-      if (abort_all) break;
+      if (ctid == MMA_ISSUER) {
+        bool ok = mbar_wait_bounded(smem_u32(&mb_ready), (uint32_t)(it & 1));
+        if (ok && it > 0) ok = mbar_wait_bounded(smem_u32(&mb_free), (uint32_t)((it - 1) & 1));
+        if (!ok) {
+          if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
+          abort_c = 1;
+        } else {
+          tc_fence_after();
+          const uint32_t idesc = make_idesc(128, T.Np);
+          const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+          if (2 * T.Np <= 256) {
+            // B0 and B1 are adjacent in shared memory and D0, D1, D2 in TMEM, so
+            // A0 [B0 B1] -> [D0 D1] and A1 [B0 B1] -> [D1 D2] are single N = 2 Np
+            // MMAs: four per k step instead of six, same sums
+            const uint32_t idesc2 = make_idesc(128, 2 * T.Np);
+            for (int s = 0; s < T.Kp / 16; s++) {
+              const uint32_t acc = s > 0 ? 1u : 0u;
+              const uint64_t bd0 = make_desc(b0 + s * 256, 128, T.SBO);
+              mma_bf16(tmem, make_desc(a0 + s * 256, 128, T.SBO), bd0, idesc2, acc);
+              mma_bf16(tmem + (uint32_t)(2 * T.Np), make_desc(a0 + s * 256, 128, T.SBO),
+                       make_desc(b0 + 2 * T.B_TERM + s * 256, 128, T.SBO), idesc, acc);
+              mma_bf16(tmem + (uint32_t)T.Np, make_desc(a0 + T.A_TERM + s * 256, 128, T.SBO), bd0, idesc2, 1u);
+              mma_bf16(tmem + (uint32_t)(2 * T.Np), make_desc(a0 + 2 * T.A_TERM + s * 256, 128, T.SBO), bd0, idesc,
+                       1u);
+            }
+          } else {
+            for (int s = 0; s < T.Kp / 16; s++) {
+#pragma unroll
+              for (int q = 0; q < 6; q++) {
+                const int d = c_pair_a[q] + c_pair_b[q];
+                const uint64_t ad = make_desc(a0 + c_pair_a[q] * T.A_TERM + s * 256, 128, T.SBO);
+                const uint64_t bdsc = make_desc(b0 + c_pair_b[q] * T.B_TERM + s * 256, 128, T.SBO);
+                const bool first = s == 0 && (q == 0 || q == 1 || q == 3);
+                mma_bf16(tmem + (uint32_t)(d * T.Np), ad, bdsc, idesc, first ? 0u : 1u);
+              }
+            }
+          }
+          mma_commit(smem_u32(&mb_done));
+          n_issued = it + 1;
+          // this thread observes completion for the group
+          if (!mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)(it & 1))) {
+            if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
+            abort_c = 1;
+          }
+        }
+        tc_fence_before();
+      }
+      __syncwarp();
+      if (!FWD) asm volatile("cp.async.wait_all;" ::: "memory");   // this thread's w V copies have landed
+      named_bar(2, WS_THREADS - WS_PROD);                          // ... and so have everyone's
+      if (abort_c) break;
       if (T.b != cons_b) {
-        for (int n = ctid; n < 256; n += WS_CONS) {
+        for (int n = ctid; n < 256; n += WS_THREADS - WS_PROD) {
           tsc_s[n] = n < T.Np ? __ldg(P.bscale + (int64_t)T.b * 256 + n) : 0.0f;
           if (!FWD) w_s[n] = n < T.Nv ? __ldg(P.w + n) : 0.0f;
         }
         cons_b = T.b;
-        named_bar(2, WS_CONS);
+        named_bar(2, WS_THREADS - WS_PROD);
       }
+      tc_fence_after();
       const float srow = srow_s[it & 1][m];
-      bool next_h0 = false;   // the issuer has issued half 0 of the next tile
       float mod = 0.0f, pe = 0.0f;
       float *Cf = reinterpret_cast<float *>(P.C);
       const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
-      for (int h = 0; h < 2; h++) {
-        const int Nh = h ? T.Np - T.N0 : T.N0;
-        const int nbase = h ? T.N0 : 0;
-        const uint32_t cb = h ? 3u * T.N0 : 0u;
-        bool ok = true;
-        if (lane == 0 && Nh > 0) ok = wait_or_abort(smem_u32(&mb_done[h]), (uint32_t)(it & 1), abort_v);
-        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-        if (Nh == 0) {
-          mbar_arrive(smem_u32(&mb_free[h]));   // no second half in this tile: nothing to drain
-        } else if (!ok) {
-          if (lane == 0) fail();
-        } else {
-          tc_fence_after();
-          for (int j0 = 8 * chalf; j0 < Nh; j0 += 16) {
-            uint32_t r0[8], r1[8], r2[8];
-            tmem_ld8(trow + cb + (uint32_t)j0, r0);
-            tmem_ld8(trow + cb + (uint32_t)(Nh + j0), r1);
-            tmem_ld8(trow + cb + (uint32_t)(2 * Nh + j0), r2);
-            tmem_wait_ld();
-            if (p < g.npt) {
+      for (int n0 = 16 * chalf; n0 < T.Np; n0 += 32) {
+        uint32_t r0[16], r1[16], r2[16];
+        tmem_ld16(trow + (uint32_t)n0, r0);
+        tmem_ld16(trow + (uint32_t)(T.Np + n0), r1);
+        tmem_ld16(trow + (uint32_t)(2 * T.Np + n0), r2);
+        tmem_wait_ld();   // one wait for the three loads
+        float d0[16], d1[16], d2[16];
 #pragma unroll
-              for (int q = 0; q < 8; q++) {
-                const int n = nbase + j0 + q;
-                const float v = fmaf(fmaf(__uint_as_float(r2[q]), 0.00390625f, __uint_as_float(r1[q])), 0.00390625f,
-                                     __uint_as_float(r0[q])) *
-                                (srow * tsc_s[n]);
-                if (n < T.Nv) {
-                  if (FWD) {
-                    Cf[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = v;
-                  } else {
-                    Cf[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = v;
-                    const float v2 = v * v;
-                    mod = fmaf(w_s[n], v2, mod);
-                    pe = fmaf(sWV[n * TC_POINTS + pl], v2, pe);
-                  }
-                }
+        for (int q = 0; q < 16; q++) {
+          reg_after_wait(r0[q]);
+          reg_after_wait(r1[q]);
+          reg_after_wait(r2[q]);
+          d0[q] = __uint_as_float(r0[q]);
+          d1[q] = __uint_as_float(r1[q]);
+          d2[q] = __uint_as_float(r2[q]);
+        }
+        if (p < g.npt) {
+#pragma unroll
+          for (int q = 0; q < 16; q++) {
+            const int n = n0 + q;
+            const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc_s[n]);
+            if (n < T.Nv) {
+              if (FWD) {
+                Cf[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = v;
+              } else {
+                Cf[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = v;
+                const float v2 = v * v;
+                mod = fmaf(w_s[n], v2, mod);
+                pe = fmaf(sWV[n * TC_POINTS + pl], v2, pe);
               }
             }
           }
-          tc_fence_before();
-          mbar_arrive(smem_u32(&mb_free[h]));
-        }
-        __syncwarp();
-        // the freed half takes the next tile's MMA chain while the other half drains.  Half 0
-        // goes now only if the next tile's slices are ready (no wait for the producers in
-        // the middle of this tile's drain), else together with half 1 after the drain.
-        if (issuer && tt + 1 < t_end) {
-          if (h == 0 && mbar_try_wait(smem_u32(&mb_ready), (uint32_t)((it + 1) & 1))) {
-            if (!issue(it + 1, tt + 1, 0)) fail();
-            next_h0 = true;
-          } else if (h == 1) {
-            if (!next_h0 && !issue(it + 1, tt + 1, 0)) fail();
-            if (!issue(it + 1, tt + 1, 1)) fail();
-          }
         }
       }
+      tc_fence_before();
+      mbar_arrive(smem_u32(&mb_free));
+      __syncwarp();
       if (!FWD && P.part) {
         // fixed-order reduction over the 256 consumer threads
         for (int o = 16; o > 0; o >>= 1) {
@@ -575,8 +539,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
           red_s[cw] = mod;
           red_s[8 + cw] = pe;
         }
-        named_bar(2, WS_CONS);   // also: every consumer is done with the w V tile
-        if (ctid == 0) {   // red_s is next written after the next tile's first barrier
+        named_bar(2, WS_THREADS - WS_PROD);   // also: every consumer is done with the w V tile
+        if (ctid == 0) {   // red_s is next written after the next tile's MMA barrier
           float ms = 0.0f, ps = 0.0f;
           for (int q = 0; q < 8; q++) {
             ms += red_s[q];
@@ -586,15 +550,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
           P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 1] = (double)ps;
         }
       } else if (!FWD) {
-        named_bar(2, WS_CONS);   // every consumer is done with the w V tile
+        named_bar(2, WS_THREADS - WS_PROD);   // every consumer is done with the w V tile
       }
     }
   }
-  // ---- drain: after a failure, wait (bounded) for the last MMA chain issued on each half
+  // ---- drain: after a timeout, wait (bounded) for the last MMA chain issued
   __syncthreads();
-  if (tid == WS_PROD + MMA_ISSUER && abort_all)
-    for (int h = 0; h < 2; h++)
-      if (n_issued[h] > 0) mbar_wait_bounded(smem_u32(&mb_done[h]), (uint32_t)((n_issued[h] - 1) & 1));
+  if (tid == WS_PROD + MMA_ISSUER && (abort_p || abort_c) && n_issued > 0)
+    mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((n_issued - 1) & 1));
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {

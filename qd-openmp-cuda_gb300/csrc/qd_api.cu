@@ -15,8 +15,12 @@
 #include <cstdio>
 #include <cstring>
 #include <cstdlib>
+#include <fstream>
+#include <map>
 #include <memory>
 #include <mutex>
+#include <set>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -353,6 +357,7 @@ struct qd_session {
   int *d_flag = nullptr;
   double *rec_buf = nullptr;
   size_t rec_buf_cap = 0;
+  std::string tuning;   // what the autotuner chose (qd_session_tuning)
   // energy-record arguments the step graph was captured with
   double *graph_rec = nullptr;
   int graph_rec_base = 0, graph_rec_cap = 0;
@@ -631,7 +636,7 @@ static void enqueue_tail(qd_session *s) {
 }
 
 static int count_launches_per_step(qd_session *s) {
-  const bool slab = s->precision == QD_PRECISION_MIXED && (s->fft.cluster || s->fft.sep >= 0);
+  const bool slab = s->precision == QD_PRECISION_MIXED && (s->fft.use_cluster || s->fft.sep >= 0);
   int n = 1 + (slab ? 1 : 3) + 1 + 1;   // fwd, fft, bwd, finalize (+ step counter)
   if (s->cor_f32) n += 2;              // coriolis x2 (rotational energy fused)
   else if (s->any_coupled) n += 3;     // coriolis x2, rot energy
@@ -700,6 +705,140 @@ __global__ void k_differs(const double *__restrict__ a, const double *__restrict
       *flag = 1;
       return;
     }
+}
+
+// ------------------------------------------------------------- autotuner
+// The mixed form's 2-D FFT has several kernels for a grid: separable shapes with
+// different CTA and cluster sizes, the two-exchange cluster kernel and the
+// three-pass kernels (FFTPlan::cand).  The first session of a key (device
+// architecture and SM count, grid, slab count, coupled or not) times each
+// candidate on its own slab pool, zeroed before any input is loaded: one
+// warm-up launch, then three launches between CUDA events; the fastest is kept.
+// Choices live in a process-wide map and, when a cache file is named
+// (options.autotune_cache, else the QD_AUTOTUNE_CACHE environment variable), in
+// that file: one line "<key>\t<choice>\t<microseconds>" per key, read before
+// tuning and appended after it.
+static std::mutex g_tune_mutex;
+static std::map<std::string, std::pair<int, double>> *g_tune = nullptr;   // never freed
+static std::set<std::string> *g_tune_read = nullptr;
+
+static std::string tune_key(qd_session *s) {
+  int cc_major = 0, cc_minor = 0, sms = 0;
+  cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, s->device);
+  cudaDeviceGetAttribute(&cc_minor, cudaDevAttrComputeCapabilityMinor, s->device);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+  std::ostringstream k;
+  k << "fft_mixed sm" << cc_major << cc_minor << "x" << sms << " grid " << s->g.n1 << "x" << s->g.n2 << " slabs "
+    << s->n_slabs << " coupled " << (s->any_coupled ? 1 : 0);
+  return k.str();
+}
+
+static const char *tune_path(const qd_fh2data *d) {
+  if (d->options.autotune_cache && *d->options.autotune_cache) return d->options.autotune_cache;
+  const char *e = std::getenv("QD_AUTOTUNE_CACHE");
+  return e && *e ? e : nullptr;
+}
+
+// reads the cache file once per path into the map (caller holds g_tune_mutex)
+static void tune_read_file(const char *path) {
+  if (!path) return;
+  if (!g_tune_read) g_tune_read = new std::set<std::string>();
+  if (!g_tune_read->insert(path).second) return;
+  std::ifstream f(path);
+  std::string line;
+  while (std::getline(f, line)) {
+    const size_t a = line.find('\t'), b = line.find('\t', a == std::string::npos ? a : a + 1);
+    if (a == std::string::npos || b == std::string::npos) continue;
+    try {
+      (*g_tune)[line.substr(0, a)] = {std::stoi(line.substr(a + 1, b - a - 1)), std::stod(line.substr(b + 1))};
+    } catch (const std::exception &) {
+      // a malformed line is skipped
+    }
+  }
+}
+
+static void autotune_fft(qd_session *s, const qd_fh2data *d0) {
+  FFTPlan &p = s->fft;
+  if (s->precision != QD_PRECISION_MIXED || p.n_cand <= 1) {
+    s->tuning = "fft: " + fft_choice_name(p.choice) + " (only candidate)";
+    return;
+  }
+  const std::string key = tune_key(s);
+  const char *path = tune_path(d0);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    if (!g_tune) g_tune = new std::map<std::string, std::pair<int, double>>();
+    tune_read_file(path);
+    auto it = g_tune->find(key);
+    if (it != g_tune->end())
+      for (int q = 0; q < p.n_cand; q++)
+        if (p.cand[q] == it->second.first) {
+          fft_plan_choose(p, it->second.first);
+          s->tuning = "fft: " + fft_choice_name(p.choice) + " (cached, " + std::to_string(it->second.second) + " us)";
+          return;
+        }
+  }
+  // time every candidate on the zeroed slab pool
+  cudaStream_t st = s->stream;
+  const Grid &g = s->g;
+  QD_CUDA(cudaMemsetAsync(s->psi_jf, 0, (size_t)s->n_slabs * g.npt * sizeof(float2), st));
+  for (float *t : {s->T1f, s->I1f}) QD_CUDA(cudaMemsetAsync(t, 0, (size_t)g.n1 * sizeof(float), st));
+  for (float *t : {s->T2f, s->I2f}) QD_CUDA(cudaMemsetAsync(t, 0, (size_t)g.n2 * sizeof(float), st));
+  const int tiles = fft_max_tiles(p);
+  double *ke = s->alloc<double>((size_t)s->n_slabs * tiles);
+  double *re = s->alloc<double>((size_t)s->n_slabs * tiles);
+  FFTLift lf{};
+  lf.proR = s->any_coupled ? nullptr : s->lrotR;
+  lf.pror = s->any_coupled ? nullptr : s->lrotr;
+  lf.epiR = s->lrotR;
+  lf.epir = s->lrotr;
+  lf.kinR = s->lkinR;
+  lf.kinr = s->lkinr;
+  lf.T1f = s->T1f;
+  lf.T2f = s->T2f;
+  lf.I1f = s->I1f;
+  lf.I2f = s->I2f;
+  cudaEvent_t e0, e1;
+  QD_CUDA(cudaEventCreate(&e0));
+  QD_CUDA(cudaEventCreate(&e1));
+  int best = -1;
+  double best_us = 0.0;
+  std::string report;
+  for (int q = 0; q < p.n_cand; q++) {
+    fft_plan_choose(p, p.cand[q]);
+    double us = -1.0;
+    try {
+      launch_fft_kinetic(st, g, p, s->psi_jf, s->d_slabs, s->n_slabs, ke, s->any_coupled ? nullptr : re, s->status, &lf);
+      QD_CUDA(cudaEventRecord(e0, st));
+      for (int r = 0; r < 3; r++)
+        launch_fft_kinetic(st, g, p, s->psi_jf, s->d_slabs, s->n_slabs, ke, s->any_coupled ? nullptr : re, s->status,
+                           &lf);
+      QD_CUDA(cudaEventRecord(e1, st));
+      QD_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      QD_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      us = 1e3 * ms / 3.0;
+    } catch (const Error &) {
+      cudaGetLastError();   // a candidate that cannot launch here is skipped
+      QD_CUDA(cudaStreamSynchronize(st));
+    }
+    report += (q ? ", " : "") + fft_choice_name(p.cand[q]) + " = " + (us < 0 ? std::string("n/a") : std::to_string(us));
+    if (us >= 0 && (best < 0 || us < best_us)) {
+      best = p.cand[q];
+      best_us = us;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best < 0) throw Error{QD_ERR_CUDA, "autotuner: no FFT kernel could run on this device"};
+  fft_plan_choose(p, best);
+  s->tuning = "fft: " + fft_choice_name(best) + " (tuned: " + report + " us)";
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  (*g_tune)[key] = {best, best_us};
+  if (path) {
+    std::ofstream f(path, std::ios::app);
+    if (f) f << key << '\t' << best << '\t' << best_us << '\n';
+  }
 }
 
 // Layout, buffers and the tables that depend only on the key.
@@ -940,6 +1079,9 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
       s->cor_f32 = true;
     }
   }
+
+  // the mixed form's FFT kernel for this grid and slab count (the partial-sum tiles below follow it)
+  autotune_fft(s, d0);
 
   // energies and partials
   s->t_modpe = s->precision == QD_PRECISION_MIXED ? legendre_tc_part_tiles(g) : legendre_bwd_part_tiles(g);
@@ -1755,6 +1897,13 @@ int qd_device_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw Error{QD_ERR_NO_DEVICE, "no CUDA device"};
     if (fp64_tflops) *fp64_tflops = measure_fp64_tflops();
     if (fp32_tflops) *fp32_tflops = measure_fp32_tflops();
+  })
+}
+
+int qd_session_tuning(qd_session *s, char *text, size_t text_cap) {
+  QD_GUARD({
+    QD_REQUIRE(s && text && text_cap > s->tuning.size(), "session, text buffer large enough");
+    std::memcpy(text, s->tuning.c_str(), s->tuning.size() + 1);
   })
 }
 

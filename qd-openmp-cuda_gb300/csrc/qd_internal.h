@@ -115,6 +115,8 @@ int legendre_bwd_part_tiles(const Grid &g);
 
 // 2-D FFT over (R, r) of every Legendre slab with the kinetic phase between
 // the passes.  precision: 0 = FP64 butterflies, 1 = FP32 butterflies.
+constexpr int FFT_MAX_CANDIDATES = 12;
+constexpr int FFT_THREE_PASS = 0, FFT_CLUSTER = 1, FFT_SEP0 = 2;
 struct FFTPlan {
   int n1, n2;
   int rad1[16], nst1;
@@ -126,7 +128,16 @@ struct FFTPlan {
   int cluster;   // CTAs per slab of the single-pass FP32 FFT (0: three-pass form)
   int sep;           // shape index of the separable single-pass FP32 FFT, -1: none
   int sep_cluster;   // its CTAs per slab
+  int use_cluster;   // the two-exchange cluster kernel is the mixed form's FFT
+  // mixed-form FFT kernels that fit this grid (FFT_SEP0 + shape, FFT_CLUSTER,
+  // FFT_THREE_PASS) and the one in use (fft_plan_choose; the autotuner times them)
+  int cand[FFT_MAX_CANDIDATES];
+  int n_cand;
+  int choice;
 };
+void fft_plan_choose(FFTPlan &p, int choice);
+std::string fft_choice_name(int choice);
+int fft_max_tiles(const FFTPlan &p);
 // FP32 three-shear phase tables of the mixed form (float2 (t, s) per entry,
 // see lift tables below); null entries are skipped.
 struct FFTLift {

@@ -123,6 +123,8 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
   q.options.steps_to_copy_psi_from_device_to_host = i32(op, "steps_to_copy_psi_from_device_to_host");
   q.options.use_p2p_async = i32(op, "use_p2p_async");
   if (mxGetField(op, 0, "precision")) q.options.precision = i32(op, "precision");
+  char *autotune_cache = str(op, "autotune_cache");   /* optional extension */
+  q.options.autotune_cache = autotune_cache;
 
   /* masks: optional, active only when both are present (matlabData.h:27) */
   const mxArray *d1 = mxGetField(D, 0, "dump1"), *d2 = mxGetField(D, 0, "dump2");
@@ -171,6 +173,7 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
   *steps = q.time.steps;
   if (script) mxFree(script);
   if (test_name) mxFree(test_name);
+  if (autotune_cache) mxFree(autotune_cache);
   if (ctx.exception) mexCallMATLAB(0, NULL, 1, &ctx.exception, "rethrow");   /* the script's own error */
   if (st != QD_OK) mexErrMsgTxt(qd_last_error());
 }

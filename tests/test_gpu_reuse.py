@@ -72,3 +72,39 @@ def test_reuse_resumes_across_calls(qd, lib):
     assert np.linalg.norm(d["OmegaStates"]["wave_packets"] - whole["OmegaStates"]["wave_packets"]) <= \
         1e-6 * np.linalg.norm(whole["OmegaStates"]["wave_packets"])
     qd.release_session_cache()
+
+
+@pytest.mark.parametrize("grid", [(256, 128, 7), (192, 96, 7)])
+def test_every_fft_candidate_matches_oracle(qd, oracle, lib, tmp_path, grid):
+    """Each FFT kernel the autotuner may pick for a production grid, forced through the
+    autotune cache file, gives the FP32-level FFT-kinetic stage (rel <= 3e-6 of the oracle)."""
+    import re
+    n1, n2, l_max = grid
+    cfg = qd.inputs.small_config(J=0, n1=n1, n2=n2, n_theta=l_max + 1, l_max=l_max, steps=1, n_energies=8)
+    d = qd.inputs.build_fh2data(cfg)
+    d["options"]["precision"] = 1
+    first = tmp_path / "tuned.txt"
+    d["options"]["autotune_cache"] = str(first)
+    with qd.Session(d) as s:
+        text = s.tuning()
+    key = first.read_text().splitlines()[0].split("\t")[0]
+    ids = sorted(set(int(x) for x in re.findall(r"\[(\d+)\] =", text)))
+    assert len(ids) >= 3, text
+    rng = np.random.default_rng(3)
+    for c in ids:
+        forced = tmp_path / f"forced_{c}.txt"
+        forced.write_text(f"{key}\t{c}\t1.0\n")
+        d = qd.inputs.build_fh2data(cfg)
+        d["options"]["precision"] = 1
+        d["options"]["autotune_cache"] = str(forced)
+        o = oracle.Oracle(qd.inputs.build_fh2data(cfg))
+        lp = (rng.standard_normal(o.lpsi[0].shape) + 1j * rng.standard_normal(o.lpsi[0].shape)) * 1e-2
+        o.lpsi[0] = lp.copy()
+        with qd.Session(d) as s:
+            assert f"[{c}] (cached" in s.tuning(), s.tuning()
+            s.set_psi("j", 0, lp)
+            s.apply("fft_kinetic", cfg.dt)
+            got = s.get_psi("j", 0)
+        o.forward_fft(); o.evolution_with_kinetic(cfg.dt); o.backward_fft()
+        err = np.linalg.norm(got - o.lpsi[0]) / np.linalg.norm(o.lpsi[0])
+        assert err < 3e-6, (c, err)
