@@ -215,10 +215,45 @@ def run_form(qd, precision: int, steps: int, warmup: int):
 OTHER_WORKLOADS = ("fh2_j12_256x128x96", "fh2_batched_j0-40_192x96x80")
 
 
-def workload_problems(qd, name: str, precision: int):
-    """FH2Data list of a named workload: one problem, or the batched J=0..40 partial waves."""
+def partition_partial_waves(blocks_per_j, world: int):
+    """Split the total-J partial waves over ``world`` ranks, balanced by Omega-block count
+    (largest first, each to the rank with the fewest blocks so far).  Partial waves are
+    independent (no Coriolis coupling between different J), so the ranks exchange nothing
+    while they step.  Returns one sorted list of J indices per rank."""
+    order = sorted(range(len(blocks_per_j)), key=lambda j: (-blocks_per_j[j], j))
+    load = [0] * world
+    parts = [[] for _ in range(world)]
+    for j in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(j)
+        load[r] += blocks_per_j[j]
+    return [sorted(p) for p in parts]
+
+
+def gather_crp(crp_by_j: dict) -> dict:
+    """P(E) of every partial wave on rank 0: each rank contributes {J: P(E)} of its own
+    partial waves (the one collective, after the timed region)."""
+    import torch
+
+    if not torch.distributed.is_initialized():
+        return dict(crp_by_j)
+    parts = [None] * torch.distributed.get_world_size()
+    torch.distributed.all_gather_object(parts, {int(j): list(map(float, v)) for j, v in crp_by_j.items()})
+    out = {}
+    for p in parts:
+        out.update(p)
+    return dict(sorted(out.items()))
+
+
+def workload_problems(qd, name: str, precision: int, rank: int = 0, world: int = 1):
+    """FH2Data list of a named workload: one problem, or the batched J=0..40 partial waves
+    (with ``world`` > 1, the share of rank ``rank``; every rank runs the single problems)."""
     if name.startswith("fh2_batched"):
-        ds = [qd.inputs.build_fh2data(c) for c in qd.inputs.batched_partial_waves()]
+        cfgs = qd.inputs.batched_partial_waves()
+        if world > 1:
+            nb = [len(qd.inputs.omega_list(c.J, c.parity, c.l_max, c.omega_cap)) for c in cfgs]
+            cfgs = [cfgs[j] for j in partition_partial_waves(nb, world)[rank]]
+        ds = [qd.inputs.build_fh2data(c) for c in cfgs]
     else:
         ds = [qd.inputs.build_fh2data(qd.inputs.CONFIGS[name])]
     for d in ds:
@@ -226,11 +261,13 @@ def workload_problems(qd, name: str, precision: int):
     return ds
 
 
-def workload_mode(qd, name: str, precision: int, steps: int, warmup: int):
-    """Device-timed steps of any named workload (the secondary configurations)."""
+def workload_mode(qd, name: str, precision: int, steps: int, warmup: int, rank: int = 0, world: int = 1):
+    """Device-timed steps of any named workload (the secondary configurations).  With N
+    ranks the batched partial waves are split over them by Omega-block count (weak in the
+    job's size: the whole J = 0..40 set over N GPUs) and rank 0 gathers P(E) per J."""
     import torch
 
-    ds = workload_problems(qd, name, precision)
+    ds = workload_problems(qd, name, precision, rank, world)
     with qd.Session(ds) as s:
         stream = torch.cuda.ExternalStream(s.stream())
         s.run(warmup)
@@ -244,14 +281,22 @@ def workload_mode(qd, name: str, precision: int, steps: int, warmup: int):
         s.flush()
         e1.record(stream)
         e1.synchronize()
-        ms = e0.elapsed_time(e1)
+        ms = max_over_ranks(e0.elapsed_time(e1))
         prof = s.profile(max(1, min(steps, 4)))
         e = s.energies()
         nb = s.n_blocks
+        s.download()
+    crp = gather_crp({int(d["OmegaStates"]["J"]): d["CRP"]["CRP"] for d in ds}) if world > 1 else None
+    nb_all = nb
+    if world > 1:
+        t = torch.tensor([nb], dtype=torch.float64, device="cuda" if torch.distributed.get_backend() == "nccl" else "cpu")
+        torch.distributed.all_reduce(t)
+        nb_all = int(t.item())
     tot = sum(v["ms"] * v["per_step"] for v in prof.values())
     return {"mode": "workload", "workload": name, "precision": "mixed" if precision else "fp64",
-            "problems": len(ds), "omega_blocks": nb, "steps": steps, "warmup": warmup,
-            "value": steps * nb / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+            "problems": len(ds), "omega_blocks": nb_all, "n_gpus": world, "steps": steps, "warmup": warmup,
+            "p_of_e_gathered_for_j": sorted(crp) if crp else None,
+            "value": steps * nb_all / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
             "module_min": float(e[:, 0].min()), "module_max": float(e[:, 0].max()),
             "kernels": {k: {"ms": round(v["ms"], 5), "per_step": v["per_step"],
                             "share": round(v["ms"] * v["per_step"] / tot, 4)} for k, v in prof.items()}}
@@ -463,7 +508,7 @@ def main():
                           "workload": args.workload or WORKLOAD}), flush=True)
         return
     if args.workload:
-        line = workload_mode(qd, args.workload, prec, args.steps, args.warmup)
+        line = workload_mode(qd, args.workload, prec, args.steps, args.warmup, rank, world)
         if rank == 0:
             print(json.dumps(line), flush=True)
         return
@@ -539,7 +584,7 @@ def main():
         "kernels": kernels,
         "gpu_launches": mixed["launches_per_step"] * args.steps + 3 * flushes,
         "clocks": clocks,
-        "measured_fma_tflops": {"fp64": fp64_peak, "fp32": fp32_peak},
+        "measured_fma_tflops": {"fp64": fp64_peak, "fp32": fp32_peak, "fp64_dmma": qd.dmma_peak()},
     }
     if rank == 0:
         line["e2e"] = e2e(qd, 1, args.steps)

@@ -267,6 +267,11 @@ int qd_session_profile(qd_session *s, int32_t n_steps, char *names, size_t names
    measured microseconds per launch of every candidate, or "cached"), as text. */
 int qd_session_tuning(qd_session *s, char *text, size_t text_cap);
 
+/* Measured FP64 tensor-core throughput of the current device (TFLOP/s, 2
+   flops per FMA) from a register-resident loop of mma.sync m8n8k4 f64 (DMMA),
+   to compare with the DFMA figure of qd_device_fma_peaks. */
+int qd_device_dmma_peak(double *fp64_tensor_tflops);
+
 /* Self-test of the bounded device-side wait that every pipelined kernel of the
    library uses: one CTA waits on an mbarrier with a budget of budget_ms.  With
    arrive = 0 nothing ever arrives, the wait gives up after the budget and the

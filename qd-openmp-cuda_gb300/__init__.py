@@ -97,7 +97,7 @@ EXPORTED = ("qd_evolve", "qd_evolve_batch", "qd_release_session_cache", "qd_last
             "qd_session_destroy", "qd_session_run", "qd_session_synchronize", "qd_session_flush", "qd_session_download",
             "qd_session_upload", "qd_session_stream", "qd_session_info", "qd_session_apply", "qd_session_get_psi",
             "qd_session_set_psi", "qd_session_get_energies", "qd_session_profile", "qd_device_fma_peaks",
-            "qd_device_wait_selftest", "qd_session_tuning",
+            "qd_device_wait_selftest", "qd_session_tuning", "qd_device_dmma_peak",
             "qd_rotational_energy_noalloc")
 
 
@@ -139,6 +139,7 @@ def load_library():
     lib.qd_device_fma_peaks.argtypes = [P(C.c_double), P(C.c_double)]
     lib.qd_device_wait_selftest.argtypes = [C.c_double, C.c_int32]
     lib.qd_session_tuning.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
+    lib.qd_device_dmma_peak.argtypes = [P(C.c_double)]
     lib.qd_rotational_energy_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                                  C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                                  C.c_double, C.c_void_p, C.c_void_p]
@@ -397,6 +398,14 @@ def fma_peaks() -> tuple:
     a, b = C.c_double(), C.c_double()
     _check(lib.qd_device_fma_peaks(C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+def dmma_peak() -> float:
+    """Measured FP64 tensor-core (DMMA) throughput of the current device in TFLOP/s."""
+    lib = load_library()
+    a = C.c_double()
+    _check(lib.qd_device_dmma_peak(C.byref(a)))
+    return a.value
 
 
 def device_wait_selftest(budget_ms: float, arrive: bool) -> None:

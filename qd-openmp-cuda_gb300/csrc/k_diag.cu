@@ -47,6 +47,51 @@ static double measure(int iters) {
 double measure_fp64_tflops() { return measure<double>(20000); }
 double measure_fp32_tflops() { return measure<float>(400000); }
 
+// FP64 tensor-core (DMMA) throughput: every warp chains mma.sync m8n8k4 f64
+// products into four independent accumulator tiles held in registers
+// (8 x 8 x 4 = 256 FMA per instruction per warp).
+__global__ void k_dmma_loop(double *out, int iters, double a) {
+  double acc[4][2];
+#pragma unroll
+  for (int t = 0; t < 4; t++) acc[t][0] = acc[t][1] = (double)threadIdx.x * 1e-3 + t;
+  const double x = a, y = a * 0.5;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(acc[t][0]), "+d"(acc[t][1])
+                   : "d"(x), "d"(y));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int t = 0; t < 4; t++) s += acc[t][0] + acc[t][1];
+  if (s == -12345.0) out[threadIdx.x] = s;   // keeps the loop live
+}
+
+double measure_dmma_tflops() {
+  int dev = 0, sms = 0;
+  QD_CUDA(cudaGetDevice(&dev));
+  QD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double *out = nullptr;
+  QD_CUDA(cudaMalloc(&out, 1024 * sizeof(double)));
+  cudaEvent_t e0, e1;
+  QD_CUDA(cudaEventCreate(&e0));
+  QD_CUDA(cudaEventCreate(&e1));
+  const int blocks = sms * 8, threads = 256, iters = 4000;
+  k_dmma_loop<<<blocks, threads>>>(out, iters / 10, 0.999);   // warm-up
+  QD_CUDA(cudaEventRecord(e0));
+  k_dmma_loop<<<blocks, threads>>>(out, iters, 0.999);
+  QD_CUDA(cudaEventRecord(e1));
+  QD_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  QD_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flops = 2.0 * 256.0 * 4.0 * (double)iters * blocks * (threads / 32);
+  return flops / (ms * 1e-3) / 1e12;
+}
+
 // Thread 0 waits (bounded) on a fresh mbarrier of count 1; thread 1 arrives on
 // it only when `arrive` is set.  A wait that gives up records QD_ERR_TIMEOUT,
 // exactly as the tensor-core kernels do.

@@ -1907,6 +1907,15 @@ int qd_session_tuning(qd_session *s, char *text, size_t text_cap) {
   })
 }
 
+int qd_device_dmma_peak(double *fp64_tensor_tflops) {
+  QD_GUARD({
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw Error{QD_ERR_NO_DEVICE, "no CUDA device"};
+    QD_REQUIRE(fp64_tensor_tflops, "fp64_tensor_tflops");
+    *fp64_tensor_tflops = measure_dmma_tflops();
+  })
+}
+
 int qd_device_wait_selftest(double budget_ms, int32_t arrive) {
   QD_GUARD({
     int n = 0;

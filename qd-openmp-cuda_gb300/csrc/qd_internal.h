@@ -75,6 +75,7 @@ enum { E_MODULE = 0, E_POTENTIAL = 1, E_KINETIC = 2, E_ROTATIONAL = 3, E_CORIOLI
 // named CUDA event on its stream right after the launch.
 void prof_mark(cudaStream_t s, const char *name);
 double measure_fp64_tflops();
+double measure_dmma_tflops();
 void device_wait_selftest(double budget_ms, int arrive);
 double measure_fp32_tflops();
 
