@@ -663,14 +663,16 @@ __device__ __forceinline__ void tw_apply(float2 &v, const float2 *tab, int e, in
 // (CPC = n1 / C, B2 threads per column).  Row region of local row q: RS
 // floats2 at Xr + q RS, used as the row transposition buffer and then as the
 // row the other CTAs gather from.  Column transposition buffer Sc[k1][j][col].
-template <int A, int B1, int B2, int THREADS>
-__global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_fft_slab_sep(float2 *__restrict__ psi, Grid g,
-                                                             const SlabDesc *__restrict__ slabs,
-                                                             const float2 *__restrict__ tw1,
-                                                             const float2 *__restrict__ tw2, FFTLift lf,
-                                                             double *__restrict__ ke_part,
-                                                             double *__restrict__ re_part, float fscale,
-                                                             double scale, const int *status) {
+// PIPE: a persistent grid of clusters walks the slabs (slab = cluster index +
+// k x clusters); each thread loads its rows of the next slab into registers
+// right after the current slab's rows are in shared memory, so that load
+// overlaps the column phase.  Otherwise one cluster per slab.
+template <int A, int B1, int B2, int THREADS, bool PIPE>
+__global__ void __launch_bounds__(THREADS, PIPE ? 2 : (THREADS <= 256 ? 3 : 1))
+    k_fft_slab_sep(float2 *__restrict__ psi, Grid g, const SlabDesc *__restrict__ slabs, int n_slabs,
+                   const float2 *__restrict__ tw1, const float2 *__restrict__ tw2, FFTLift lf,
+                   double *__restrict__ ke_part, double *__restrict__ re_part, float fscale, double scale,
+                   const int *status) {
   constexpr int N1 = A * B1, N2 = A * B2;
   constexpr int RPC = THREADS / B1;
   constexpr int C = N2 / RPC;
@@ -687,22 +689,27 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_fft_slab_se
   float2 *t1 = Sc + A * B2 * CPC;
   float2 *t2 = t1 + N1;
   const int tid = threadIdx.x;
-  for (int q = tid; q < N1; q += THREADS) t1[q] = __ldg(tw1 + q);
-  for (int q = tid; q < N2; q += THREADS) t2[q] = __ldg(tw2 + q);
   const int c = (int)cluster.block_rank();
-  const int sl = blockIdx.x / C;
+  const int ncl = PIPE ? (int)(gridDim.x / C) : n_slabs;
+  const int q = tid / B1, j = tid % B1;   // row phase: thread j of local row q
+  const int r = c * RPC + q;
+  float2 v[A];
+  int sl = blockIdx.x / C;
+  if (sl < n_slabs) {
+    const float2 *src = psi + (int64_t)sl * g.npt + (int64_t)r * N1 + j;
+#pragma unroll
+    for (int m = 0; m < A; m++) v[m] = __ldcs(src + B1 * m);
+  }
+  for (int p = tid; p < N1; p += THREADS) t1[p] = __ldg(tw1 + p);
+  for (int p = tid; p < N2; p += THREADS) t2[p] = __ldg(tw2 + p);
+  __syncthreads();   // twiddle tables
+  for (; sl < n_slabs; sl += ncl) {
   const int l = slabs[sl].l;
   float2 *P = psi + (int64_t)sl * g.npt;
   float ke1 = 0.0f, ke2 = 0.0f, ref = 0.0f;
-  float2 v[A];
 
   // ======== rows: thread j of row group q holds x[j + B1 m], m < A
   {
-    const int q = tid / B1, j = tid % B1;
-    const int r = c * RPC + q;
-    const float2 *src = P + (int64_t)r * N1 + j;
-#pragma unroll
-    for (int m = 0; m < A; m++) v[m] = __ldcs(src + B1 * m);
     if (lf.proR) {
       const float2 pr = __ldg(lf.pror + (int64_t)l * N2 + r);
 #pragma unroll
@@ -711,7 +718,6 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_fft_slab_se
         lift2(v[m].x, v[m].y, pr);
       }
     }
-    __syncthreads();   // twiddle tables
     float2 *G = Xr + q * RS;
     RegDFT<A, false>::run(v);
 #pragma unroll
@@ -753,6 +759,12 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_fft_slab_se
     for (int m = 0; m < A; m++) G[j + B1 * m] = v[m];
   }
   cluster.sync();   // every row of the slab is in its owner's shared memory
+  float2 vn[PIPE ? A : 1];
+  if (PIPE && sl + ncl < n_slabs) {   // the next slab's rows, in flight during the column phase
+    const float2 *src = psi + (int64_t)(sl + ncl) * g.npt + (int64_t)r * N1 + j;
+#pragma unroll
+    for (int m = 0; m < (PIPE ? A : 1); m++) vn[m] = __ldcs(src + B1 * m);
+  }
 
   // ======== columns: thread jc of column col holds x[r = jc + B2 m], m < A
   const int col = tid % CPC, jc = tid / CPC;
@@ -840,8 +852,13 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 3 : 1) k_fft_slab_se
     if (ke_part) ke_part[(int64_t)sl * C + c] = (double)ke;
     if (re_part) re_part[(int64_t)sl * C + c] = (double)re;
   }
-  // no CTA leaves while another may still read its rows
+  // no CTA leaves, or rewrites its rows, while another may still read them
   asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+  if (PIPE) {
+#pragma unroll
+    for (int m = 0; m < (PIPE ? A : 1); m++) v[m] = vn[m];
+  }
+  }
 }
 
 namespace {
@@ -849,18 +866,21 @@ namespace {
 // thread counts (and so cluster sizes, C = A B2 B1 / threads CTAs per slab) exist for the
 // production grids; the autotuner times them on the session's own slabs.
 struct SepShape {
-  int n1, n2, A, B1, B2, threads;
+  int n1, n2, A, B1, B2, threads, pipe;
 };
 constexpr SepShape kSepShapes[] = {
-    {256, 128, 16, 16, 8, 256},
-    {192, 96, 24, 8, 4, 96},
-    {64, 32, 8, 8, 4, 128},
-    {32, 16, 8, 4, 2, 32},
-    {16, 8, 4, 4, 2, 32},
-    {256, 128, 16, 16, 8, 512},
-    {256, 128, 16, 16, 8, 128},
-    {192, 96, 24, 8, 4, 192},
-    {192, 96, 24, 8, 4, 384},
+    {256, 128, 16, 16, 8, 256, 0},
+    {192, 96, 24, 8, 4, 96, 0},
+    {64, 32, 8, 8, 4, 128, 0},
+    {32, 16, 8, 4, 2, 32, 0},
+    {16, 8, 4, 4, 2, 32, 0},
+    {256, 128, 16, 16, 8, 512, 0},
+    {256, 128, 16, 16, 8, 128, 0},
+    {192, 96, 24, 8, 4, 192, 0},
+    {192, 96, 24, 8, 4, 384, 0},
+    {256, 128, 16, 16, 8, 256, 1},
+    {192, 96, 24, 8, 4, 192, 1},
+    {192, 96, 24, 8, 4, 96, 1},
 };
 constexpr int kNumSep = (int)(sizeof(kSepShapes) / sizeof(kSepShapes[0]));
 
@@ -874,15 +894,15 @@ int sep_cluster() {
   return A * B2 / (T / B1);
 }
 
-template <int A, int B1, int B2, int T>
+template <int A, int B1, int B2, int T, bool PIPE>
 void sep_set_attr() {
-  QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T, PIPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sep_smem_bytes<A, B1, B2, T>()));
   if (sep_cluster<A, B1, B2, T>() > 8)
-    QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T, PIPE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
 }
 
-template <int A, int B1, int B2, int T>
+template <int A, int B1, int B2, int T, bool PIPE>
 void sep_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, const SlabDesc *slabs, int n_slabs,
                 const FFTLift &lf, double *ke_part, double *re_part, float fscale, double scale, const int *status) {
   const int C = sep_cluster<A, B1, B2, T>();
@@ -898,32 +918,50 @@ void sep_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, 
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  QD_CUDA(cudaLaunchKernelEx(&cfg, k_fft_slab_sep<A, B1, B2, T>, psi_j, g, slabs, (const float2 *)p.tw1_f,
-                             (const float2 *)p.tw2_f, lf, ke_part, re_part, fscale, scale, status));
+  if (PIPE) {
+    // as many clusters as fit on the device at once (all of them resident: the slab loop
+    // needs no cluster to wait for another), at most one per slab
+    static int resident[64] = {};   // per instantiation, per device
+    int dev = 0;
+    QD_CUDA(cudaGetDevice(&dev));
+    int &n = resident[dev & 63];
+    if (n == 0) {
+      int k = 0;
+      n = cudaOccupancyMaxActiveClusters(&k, k_fft_slab_sep<A, B1, B2, T, PIPE>, &cfg) == cudaSuccess && k > 0 ? k : -1;
+      if (n < 0) cudaGetLastError();
+    }
+    if (n > 0) cfg.gridDim = dim3((unsigned)(std::min(n_slabs, n) * C));
+  }
+  QD_CUDA(cudaLaunchKernelEx(&cfg, k_fft_slab_sep<A, B1, B2, T, PIPE>, psi_j, g, slabs, n_slabs,
+                             (const float2 *)p.tw1_f, (const float2 *)p.tw2_f, lf, ke_part, re_part, fscale, scale,
+                             status));
 }
 
-#define QD_SEP_CASES(X)  \
-  X(0, 16, 16, 8, 256)   \
-  X(1, 24, 8, 4, 96)     \
-  X(2, 8, 8, 4, 128)     \
-  X(3, 8, 4, 2, 32)      \
-  X(4, 4, 4, 2, 32)      \
-  X(5, 16, 16, 8, 512)   \
-  X(6, 16, 16, 8, 128)   \
-  X(7, 24, 8, 4, 192)    \
-  X(8, 24, 8, 4, 384)
+#define QD_SEP_CASES(X)         \
+  X(0, 16, 16, 8, 256, false)   \
+  X(1, 24, 8, 4, 96, false)     \
+  X(2, 8, 8, 4, 128, false)     \
+  X(3, 8, 4, 2, 32, false)      \
+  X(4, 4, 4, 2, 32, false)      \
+  X(5, 16, 16, 8, 512, false)   \
+  X(6, 16, 16, 8, 128, false)   \
+  X(7, 24, 8, 4, 192, false)    \
+  X(8, 24, 8, 4, 384, false)    \
+  X(9, 16, 16, 8, 256, true)    \
+  X(10, 24, 8, 4, 192, true)    \
+  X(11, 24, 8, 4, 96, true)
 
 void sep_dispatch_attr(int id) {
   switch (id) {
-#define QD_X(i, a, b1, b2, t) \
-  case i: sep_set_attr<a, b1, b2, t>(); break;
+#define QD_X(i, a, b1, b2, t, pipe) \
+  case i: sep_set_attr<a, b1, b2, t, pipe>(); break;
     QD_SEP_CASES(QD_X)
 #undef QD_X
   }
 }
 int sep_dispatch_cluster(int id) {
   switch (id) {
-#define QD_X(i, a, b1, b2, t) \
+#define QD_X(i, a, b1, b2, t, pipe) \
   case i: return sep_cluster<a, b1, b2, t>();
     QD_SEP_CASES(QD_X)
 #undef QD_X
@@ -934,8 +972,10 @@ void sep_dispatch_launch(int id, cudaStream_t s, const Grid &g, const FFTPlan &p
                          const SlabDesc *slabs, int n_slabs, const FFTLift &lf, double *ke_part, double *re_part,
                          float fscale, double scale, const int *status) {
   switch (id) {
-#define QD_X(i, a, b1, b2, t) \
-  case i: sep_launch<a, b1, b2, t>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); break;
+#define QD_X(i, a, b1, b2, t, pipe)                                                                          \
+  case i:                                                                                                     \
+    sep_launch<a, b1, b2, t, pipe>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); \
+    break;
     QD_SEP_CASES(QD_X)
 #undef QD_X
   }
@@ -1038,7 +1078,8 @@ std::string fft_choice_name(int choice) {
   if (choice >= FFT_SEP0) {
     const SepShape &q = kSepShapes[choice - FFT_SEP0];
     name = "separable A=" + std::to_string(q.A) + " B1=" + std::to_string(q.B1) + " B2=" + std::to_string(q.B2) +
-           " threads=" + std::to_string(q.threads) + " cluster=" + std::to_string(sep_dispatch_cluster(choice - FFT_SEP0));
+           " threads=" + std::to_string(q.threads) + " cluster=" + std::to_string(sep_dispatch_cluster(choice - FFT_SEP0)) +
+           (q.pipe ? " persistent" : "");
   } else {
     name = choice == FFT_CLUSTER ? "cluster two-exchange" : "three-pass";
   }
