@@ -322,11 +322,12 @@ __global__ void __launch_bounds__(256) k_energy_finalize(FinalizeArgs a) {
   }
 }
 
-// Mixed form, one launch for the end of a step: CTAs [0, nfx) extract the flux
-// surface values (slot = the flux count before this step ends), CTAs
-// [nfx, nfx + n_blocks) finalise one Omega block each, and the last CTA to
+// Mixed form, one launch for the end of a step: CTAs [0, n_blocks) finalise one
+// Omega block each (first in the grid, so that their serial reductions overlap
+// the extraction), CTAs [n_blocks, n_blocks + nfx) extract the flux surface
+// values (slot = the flux count before this step ends), and the last CTA to
 // finish applies the norm guard and ends the step.
-__global__ void __launch_bounds__(256) k_step_tail_mixed(FinalizeArgs a, FluxTileArgs f, int nfx, int fx_tiles) {
+__global__ void __launch_bounds__(256) k_step_tail_mixed(FinalizeArgs a, FluxTileArgs f, int fx_tiles) {
   __shared__ double red[8][2];
   __shared__ float2 sD[FLUX_GY][FLUX_GX];
   __shared__ float2 sA[FLUX_GX];
@@ -335,12 +336,12 @@ __global__ void __launch_bounds__(256) k_step_tail_mixed(FinalizeArgs a, FluxTil
   const int tid = threadIdx.x;
   const int step = *a.d_step;
   const int fcount = a.tail.flux_count ? *a.tail.flux_count : 0;
-  if ((int)blockIdx.x < nfx) {
+  if ((int)blockIdx.x >= a.n_blocks) {
     // a full buffer is reported by the step end (QD_ERR_INVALID); nothing is written
-    if (fcount < a.tail.cap)
-      flux_extract_tile(f, fcount, blockIdx.x / fx_tiles, blockIdx.x % fx_tiles, tid, sD, sA);
+    const int x = blockIdx.x - a.n_blocks;
+    if (fcount < a.tail.cap) flux_extract_tile(f, fcount, x / fx_tiles, x % fx_tiles, tid, sD, sA);
   } else {
-    const int b = blockIdx.x - nfx;
+    const int b = blockIdx.x;
     finalize_reduce(a, b, red);
     if (tid == 0) finalize_write(a, b, step, red);
   }
@@ -375,7 +376,7 @@ void launch_energy_finalize2(cudaStream_t st, const Grid &g, const EnergyParts &
   if (fx) {
     const int fx_tiles = (int)(((int64_t)g.nth * g.n1 + FLUX_GX - 1) / FLUX_GX);
     const int nfx = fx_tiles * n_blocks;
-    k_step_tail_mixed<<<nfx + n_blocks, FLUX_GX * FLUX_GY, 0, st>>>(a, *fx, nfx, fx_tiles);
+    k_step_tail_mixed<<<nfx + n_blocks, FLUX_GX * FLUX_GY, 0, st>>>(a, *fx, fx_tiles);
   } else {
     k_energy_finalize<<<n_blocks, 256, 0, st>>>(a);
   }
