@@ -58,7 +58,9 @@ __global__ void __launch_bounds__(FLUX_GX *FLUX_GY) k_flux_extract_f32(FluxTileA
   if (status && *status) return;
   __shared__ float2 sD[FLUX_GY][FLUX_GX];
   __shared__ float2 sA[FLUX_GX];
-  flux_extract_tile(f, *slot_p, blockIdx.y, blockIdx.x, threadIdx.y * FLUX_GX + threadIdx.x, sD, sA);
+  __shared__ int slot;
+  if (threadIdx.x == 0 && threadIdx.y == 0) slot = *slot_p;
+  flux_extract_tile(f, &slot, blockIdx.y, blockIdx.x, threadIdx.y * FLUX_GX + threadIdx.x, sD, sA);
 }
 
 void launch_flux_extract_f32(cudaStream_t s, const Grid &g, const FluxConfig &f, const float2 *psi_th, int n_blocks,

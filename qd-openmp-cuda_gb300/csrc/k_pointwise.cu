@@ -298,17 +298,26 @@ template void launch_rot_energy<float2>(cudaStream_t, const Grid &, const float2
 // Coupling-energy partials are laid out [group][ce_n][tiles]; a block collects
 // them from every group (one per l) of its problem that contains its Omega.
 __global__ void __launch_bounds__(256) k_energy_finalize(FinalizeArgs a) {
-  __shared__ double red[8][2];
+  __shared__ double red[5][FIN_THREADS];
+  __shared__ double tot[5];
   __shared__ bool last;
+  __shared__ int hdr[3];
   const int tid = threadIdx.x;
-  // everything this launch reads is loaded up front
-  const int st0 = *a.status;
-  const int step = *a.d_step;   // advanced only at the very end, after every CTA has read it
-  const int fcount = (tid == 0 && a.tail.flux_count) ? *a.tail.flux_count : 0;
-  finalize_reduce(a, blockIdx.x, red);
+  // everything this launch reads is loaded up front, once per CTA (the status words
+  // share one L2 line), issued together with the partial sums; finalize_reduce's
+  // barrier publishes them
+  double eprev[6];
+  if (tid == 0) {
+    hdr[0] = *a.status;
+    hdr[1] = *a.d_step;   // advanced only at the very end, after every CTA has read it
+    hdr[2] = a.tail.flux_count ? *a.tail.flux_count : 0;
+    for (int q = 0; q < 6; q++) eprev[q] = a.energies[blockIdx.x * 6 + q];
+  }
+  finalize_reduce(a, blockIdx.x, red, tot);
+  const int st0 = hdr[0], step = hdr[1], fcount = tid == 0 ? hdr[2] : 0;
   if (st0) return;   // set before this launch: nothing is written, the counter is untouched
   double mod = 0.0;
-  if (tid == 0) mod = finalize_write(a, blockIdx.x, step, red);
+  if (tid == 0) mod = finalize_write(a, blockIdx.x, step, tot, eprev);
   if (gridDim.x == 1) {
     if (tid != 0) return;
     bool bad = false;
@@ -328,23 +337,35 @@ __global__ void __launch_bounds__(256) k_energy_finalize(FinalizeArgs a) {
 // values (slot = the flux count before this step ends), and the last CTA to
 // finish applies the norm guard and ends the step.
 __global__ void __launch_bounds__(256) k_step_tail_mixed(FinalizeArgs a, FluxTileArgs f, int fx_tiles) {
-  __shared__ double red[8][2];
+  __shared__ double red[5][FIN_THREADS];
+  __shared__ double tot[5];
   __shared__ float2 sD[FLUX_GY][FLUX_GX];
   __shared__ float2 sA[FLUX_GX];
   __shared__ bool last;
-  if (*a.status) return;   // set before this launch: uniform, the counter is untouched
+  __shared__ int hdr[4];
   const int tid = threadIdx.x;
-  const int step = *a.d_step;
-  const int fcount = a.tail.flux_count ? *a.tail.flux_count : 0;
-  if ((int)blockIdx.x >= a.n_blocks) {
-    // a full buffer is reported by the step end (QD_ERR_INVALID); nothing is written
-    const int x = blockIdx.x - a.n_blocks;
-    if (fcount < a.tail.cap) flux_extract_tile(f, fcount, x / fx_tiles, x % fx_tiles, tid, sD, sA);
-  } else {
-    const int b = blockIdx.x;
-    finalize_reduce(a, b, red);
-    if (tid == 0) finalize_write(a, b, step, red);
+  // the status words are read once per CTA (they share one L2 line) and in flight
+  // together with the tile's own loads; the barrier inside the extraction or the
+  // reduction publishes them, and nothing is written before they are checked
+  double eprev[6];
+  if (tid == 0) {
+    hdr[0] = *a.status;
+    hdr[1] = *a.d_step;
+    hdr[2] = a.tail.flux_count ? *a.tail.flux_count : 0;
+    // the flux slot, or -1: status already set, or the buffer is full (reported by the step end)
+    hdr[3] = (hdr[0] == 0 && hdr[2] < a.tail.cap) ? hdr[2] : -1;
+    if ((int)blockIdx.x < a.n_blocks)
+      for (int q = 0; q < 6; q++) eprev[q] = a.energies[blockIdx.x * 6 + q];
   }
+  if ((int)blockIdx.x >= a.n_blocks) {
+    const int x = blockIdx.x - a.n_blocks;
+    flux_extract_tile(f, &hdr[3], x / fx_tiles, x % fx_tiles, tid, sD, sA);
+  } else {
+    finalize_reduce(a, blockIdx.x, red, tot);
+  }
+  if (hdr[0]) return;   // set before this launch: uniform, the counter is untouched
+  const int step = hdr[1], fcount = hdr[2];
+  if ((int)blockIdx.x < a.n_blocks && tid == 0) finalize_write(a, blockIdx.x, step, tot, eprev);
   finalize_last_cta(a, step, fcount, &last);
 }
 

@@ -46,13 +46,15 @@ inline FluxTileArgs flux_tile_args(const Grid &g, const FluxConfig &fc, const fl
   f.buf = buf;
   return f;
 }
-__device__ inline void flux_extract_tile(const FluxTileArgs &f, int slot, int b, int xtile, int tid,
+// slot_sh: shared word written by thread 0 before the call and read only after
+// the tile's barrier (so its global source need not be waited for first); a
+// negative slot writes nothing.
+__device__ inline void flux_extract_tile(const FluxTileArgs &f, const int *slot_sh, int b, int xtile, int tid,
                                          float2 (*sD)[FLUX_GX], float2 *sA) {
   const Grid &g = f.g;
   const int tx = tid % FLUX_GX, ty = tid / FLUX_GX;
   const int h = (f.n_grad - 1) / 2;
   const int64_t ns = (int64_t)g.nth * g.n1;
-  float2 *out = f.buf + ((int64_t)slot * f.n_blocks + b) * 2 * ns;
   const float2 *p = f.psi_th + (int64_t)b * g.nth * g.npt;
   const int64_t q = (int64_t)xtile * FLUX_GX + tx;
   float Dx = 0.0f, Dy = 0.0f;
@@ -83,7 +85,9 @@ __device__ inline void flux_extract_tile(const FluxTileArgs &f, int slot, int b,
   }
   sD[ty][tx] = make_float2(Dx, Dy);
   __syncthreads();
-  if (ty == 0 && q < ns) {
+  const int slot = *slot_sh;
+  if (ty == 0 && q < ns && slot >= 0) {
+    float2 *out = f.buf + ((int64_t)slot * f.n_blocks + b) * 2 * ns;
     float2 D = sD[0][tx];
 #pragma unroll
     for (int y = 1; y < FLUX_GY; y++) {
@@ -114,9 +118,15 @@ struct FinalizeArgs {
   unsigned *done;
 };
 
-// All partials of block b, 256 threads (two warps per quantity: module/potential,
-// kinetic, rotational, Coriolis), reduced in a fixed order into red[8][2].
-__device__ inline void finalize_reduce(const FinalizeArgs &a, int b, double (*red)[2]) {
+// All partials of block b, summed by the CTA's 256 threads into tot[5] (module,
+// potential, kinetic, rotational, Coriolis), deterministically: thread t loads
+// elements t, t + 256, ... of every partial array (a chunk's loads in flight
+// together) and adds the ones that exist; warp q then sums quantity q's 256
+// per-thread values from shared memory in a fixed order.  The FP64 pipe runs
+// at 1/64 of FP32 on this part, so the CTA adds each value once: no zero
+// padding and no all-lane shuffle trees over the 256 threads.
+constexpr int FIN_THREADS = 256;
+__device__ inline void finalize_reduce(const FinalizeArgs &a, int b, double (*red)[FIN_THREADS], double *tot) {
   const int tid = threadIdx.x;
   const EnergyParts &ep = a.ep;
   const BlockDesc bd = a.blocks[b];
@@ -129,56 +139,64 @@ __device__ inline void finalize_reduce(const FinalizeArgs &a, int b, double (*re
   const double2 *mp = reinterpret_cast<const double2 *>(ep.mod_pe) + (int64_t)b * ep.mod_pe_tiles;
   const double *kp = ep.ke + (int64_t)bd.slab0 * ep.ke_tiles;
   const double *rp = ep.re + (int64_t)bd.slab0 * ep.re_tiles;
-  // warp-uniform branches, no divergence inside a loop: each lane's loads issue together
+  constexpr int T = FIN_THREADS, U = 4;
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  const int wq = tid >> 6, l64 = tid & 63;
-  if (wq == 0) {
-#pragma unroll 8
-    for (int t = l64; t < n0; t += 64) {
-      const double2 v = mp[t];
-      acc[0] += v.x;
-      acc[1] += v.y;
+  const int nmax = max(max(n0, n1), max(n2, n3));
+  for (int t0 = tid; t0 < nmax; t0 += T * U) {
+    double2 vm[U];
+    double vk[U], vr[U], vc[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int t = t0 + u * T;
+      vm[u] = t < n0 ? mp[t] : make_double2(0.0, 0.0);
+      vk[u] = t < n1 ? kp[t] : 0.0;
+      vr[u] = t < n2 ? rp[t] : 0.0;
+      vc[u] = 0.0;
+      if (t < n3) {
+        const int gi = g_lo + t / ep.ce_tiles, tt = t - (t / ep.ce_tiles) * ep.ce_tiles;
+        const int o = bd.omega - a.groups[gi].omega_lo;
+        if (o >= 0 && o < a.groups[gi].n) vc[u] = ep.ce[((int64_t)gi * a.ce_n + o) * ep.ce_tiles + tt];
+      }
     }
-  } else if (wq == 1) {
-#pragma unroll 8
-    for (int t = l64; t < n1; t += 64) acc[2] += kp[t];
-  } else if (wq == 2) {
-#pragma unroll 8
-    for (int t = l64; t < n2; t += 64) acc[3] += rp[t];
-  } else {
-#pragma unroll 4
-    for (int q = l64; q < n3; q += 64) {
-      const int gi = g_lo + q / ep.ce_tiles, tt = q - (q / ep.ce_tiles) * ep.ce_tiles;
-      const int o = bd.omega - a.groups[gi].omega_lo;
-      if (o >= 0 && o < a.groups[gi].n) acc[4] += ep.ce[((int64_t)gi * a.ce_n + o) * ep.ce_tiles + tt];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int t = t0 + u * T;
+      if (t < n0) {
+        acc[0] += vm[u].x;
+        acc[1] += vm[u].y;
+      }
+      if (t < n1) acc[2] += vk[u];
+      if (t < n2) acc[3] += vr[u];
+      if (t < n3) acc[4] += vc[u];
     }
   }
-  // each warp reduces only its own quantity; thread 0 later adds the two warps of each
-  double v0 = wq == 0 ? acc[0] : acc[1 + wq], v1 = acc[1];
-  for (int o = 16; o > 0; o >>= 1) {
-    v0 += __shfl_down_sync(0xffffffffu, v0, o);
-    if (wq == 0) v1 += __shfl_down_sync(0xffffffffu, v1, o);
-  }
-  if ((tid & 31) == 0) {
-    red[tid >> 5][0] = v0;
-    red[tid >> 5][1] = v1;
+#pragma unroll
+  for (int q = 0; q < 5; q++) red[q][tid] = acc[q];
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  if (warp < 5) {
+    double v = 0.0;
+#pragma unroll
+    for (int i = 0; i < T / 32; i++) v += red[warp][lane + 32 * i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) tot[warp] = v;
   }
   __syncthreads();
 }
 
 // Thread 0: energies[b] (totals included) and the step record; returns the module.
-__device__ inline double finalize_write(const FinalizeArgs &a, int b, int step, const double (*red)[2]) {
+// eprev: energies[b] as loaded at the start (kept for quantities not computed here).
+__device__ inline double finalize_write(const FinalizeArgs &a, int b, int step, const double *tot,
+                                        const double *eprev) {
   const EnergyParts &ep = a.ep;
-  const double tot[5] = {red[0][0] + red[1][0], red[0][1] + red[1][1], red[2][0] + red[3][0],
-                         red[4][0] + red[5][0], red[6][0] + red[7][0]};
   const double dV = a.g.dr1 * a.g.dr2;
   double *e = a.energies + b * 6;
   double ev[6];
-  ev[E_MODULE] = ep.have_mod ? tot[0] * dV : e[E_MODULE];
-  ev[E_POTENTIAL] = ep.have_mod ? tot[1] * dV : e[E_POTENTIAL];
-  ev[E_KINETIC] = ep.have_ke ? tot[2] * ep.ke_scale : e[E_KINETIC];
-  ev[E_ROTATIONAL] = ep.have_re ? tot[3] * dV : e[E_ROTATIONAL];
-  ev[E_CORIOLIS] = ep.have_ce ? tot[4] * dV : e[E_CORIOLIS];
+  ev[E_MODULE] = ep.have_mod ? tot[0] * dV : eprev[E_MODULE];
+  ev[E_POTENTIAL] = ep.have_mod ? tot[1] * dV : eprev[E_POTENTIAL];
+  ev[E_KINETIC] = ep.have_ke ? tot[2] * ep.ke_scale : eprev[E_KINETIC];
+  ev[E_ROTATIONAL] = ep.have_re ? tot[3] * dV : eprev[E_ROTATIONAL];
+  ev[E_CORIOLIS] = ep.have_ce ? tot[4] * dV : eprev[E_CORIOLIS];
   ev[E_TOTAL] = ev[E_POTENTIAL] + ev[E_KINETIC] + ev[E_ROTATIONAL] + ev[E_CORIOLIS];
   for (int q = 0; q < 6; q++) e[q] = ev[q];
   const int slot = step - a.rec_base;
