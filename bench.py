@@ -386,8 +386,16 @@ def pe_gate(qd, steps: int):
             "note": "mixed vs FP64 form of this library on this GPU, same inputs, qd_evolve"}
 
 
-def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 3):
-    cfg = qd.inputs.CONFIGS[WORKLOAD]
+def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 3, workload: str = WORKLOAD):
+    """The FP64 oracle on the host cores, a bounded sample of ``workload``: its single
+    problem, or for the batched partial waves one of its problems (J = 20, 21 Omega
+    blocks), in Omega-block steps per second."""
+    if workload.startswith("fh2_batched"):
+        cfg = [c for c in qd.inputs.batched_partial_waves() if c.J == 20][0]
+        what = f"the J = 20 problem (21 Omega blocks, 192x96x80) of the {workload} workload"
+    else:
+        cfg = qd.inputs.CONFIGS[workload]
+        what = f"the {workload} workload"
     d = qd.inputs.build_fh2data(cfg)
     o = oracle.Oracle(d)
     for _ in range(warm):
@@ -398,8 +406,8 @@ def cpu_baseline(qd, oracle, n_steps: int = 8, warm: int = 3):
     sec = time.perf_counter() - t0
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     return {"value": n_steps * len(o.omegas) / sec, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{n_steps} FP64 oracle steps (numpy/scipy, pocketfft + OpenBLAS) of the "
-                      f"{WORKLOAD} workload after {warm} warm-up step{'s' if warm != 1 else ''}"}
+            "sample": f"{n_steps} FP64 oracle steps (numpy/scipy, pocketfft + OpenBLAS) of {what} "
+                      f"after {warm} warm-up step{'s' if warm != 1 else ''}"}
 
 
 def accuracy(qd, total: int, checkpoints=(10, 40, 160, 640, 2560, 10240, 20000)):
@@ -510,6 +518,9 @@ def main():
     if args.workload:
         line = workload_mode(qd, args.workload, prec, args.steps, args.warmup, rank, world)
         if rank == 0:
+            if world == 1 and not args.no_cpu_baseline:
+                line["cpu_baseline"] = cpu_baseline(qd, entry.load_oracle(), n_steps=2, warm=1,
+                                                    workload=args.workload)
             print(json.dumps(line), flush=True)
         return
     gpu_index = local
