@@ -88,6 +88,31 @@ namespace {
 constexpr int FLUX_EB = 8;        // energies per thread
 constexpr int FLUX_THREADS = 128; // surface points per CTA
 constexpr int FLUX_MAXC = 64;     // maximum chunk length
+
+// dst[e ns] += v[e] for e < ne (FP64 accumulators; FP32 partial sums widened
+// exactly with integer instructions).  The loads of a chunk of up to 16 energies
+// issue together before their adds: one memory round trip per chunk, not one per
+// energy.
+__device__ inline double2 widen(float2 v) { return make_double2(f2d(v.x), f2d(v.y)); }
+__device__ inline double2 widen(double2 v) { return v; }
+template <int EB, typename T>
+__device__ inline void flux_acc_add(double2 *__restrict__ dst, int64_t ns, int ne, const T *v) {
+  constexpr int CH = EB < 8 ? EB : 8;
+#pragma unroll
+  for (int e1 = 0; e1 < EB; e1 += CH) {
+    double2 old[CH];
+#pragma unroll
+    for (int u = 0; u < CH; u++) old[u] = e1 + u < ne ? dst[(int64_t)(e1 + u) * ns] : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int u = 0; u < CH; u++)
+      if (e1 + u < ne) {
+        const double2 w = widen(v[e1 + u]);
+        old[u].x += w.x;
+        old[u].y += w.y;
+        dst[(int64_t)(e1 + u) * ns] = old[u];
+      }
+  }
+}
 }
 
 // acc[b][c][E][k][i] += sum_n phase[n][E] buf[n][b][c][k][i]
@@ -121,15 +146,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft(int64_t ns2, int nE, 
   const int64_t ns = ns2 / 2;
   const int c = (int)(s / ns);
   const int64_t kq = s % ns;
-#pragma unroll
-  for (int e = 0; e < FLUX_EB; e++) {
-    if (e0 + e >= nE) break;
-    double2 *dst = acc + (((int64_t)b * 2 + c) * nE + e0 + e) * ns + kq;
-    double2 v = *dst;
-    v.x += a[e].x;
-    v.y += a[e].y;
-    *dst = v;
-  }
+  flux_acc_add<FLUX_EB>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB, nE - e0), a);
 }
 
 void launch_flux_dft(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_blocks, const double2 *buf, int count,
@@ -180,25 +197,21 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_dev(int64_t ns2, int 
   const int64_t ns = ns2 / 2;
   const int c = (int)(s / ns);
   const int64_t kq = s % ns;
-#pragma unroll
-  for (int e = 0; e < FLUX_EB; e++) {
-    if (e0 + e >= nE) break;
-    double2 *dst = acc + (((int64_t)b * 2 + c) * nE + e0 + e) * ns + kq;
-    double2 v = *dst;
-    v.x += a[e].x;
-    v.y += a[e].y;
-    *dst = v;
-  }
+  flux_acc_add<FLUX_EB>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB, nE - e0), a);
 }
 
-// Mixed form of the transform: products and the 32-step partial sums in FP32
+// Mixed form of the transform: products and the chunk's partial sums in FP32
 // (phases computed in FP64 and rounded once, surface values converted with
 // integer instructions), each chunk's sum added into the FP64 accumulators.
+// Eight energies per thread: the accumulator update is one round of eight
+// loads per thread, and the grid (ns2 / 128 x nE / 8 CTAs of 80 registers, six
+// per SM) keeps enough loads in flight; the kernel is bound by the latency of
+// the 630 MB of FP64 accumulators it reads and writes per flush.
 namespace {
-constexpr int FLUX_EB32 = 32;
+constexpr int FLUX_EB32 = 8;
 }
 
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_f32(int64_t ns2, int nE, int n_blocks, const int *count_p,
+__global__ void __launch_bounds__(FLUX_THREADS, 6) k_flux_dft_f32(int64_t ns2, int nE, int n_blocks, const int *count_p,
                                                                int cap, const float2 *__restrict__ buf,
                                                                const double2 *__restrict__ phase,
                                                                double2 *__restrict__ acc, const int *status) {
@@ -220,7 +233,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_f32(int64_t ns2, int 
 #pragma unroll
   for (int e = 0; e < FLUX_EB32; e++) a[e] = make_float2(0.0f, 0.0f);
   // unrolled so that several steps' surface values are loaded ahead of their use
-#pragma unroll 4
+#pragma unroll 8
   for (int n = 0; n < count; n++) {
     const float2 vd = buf[((int64_t)n * n_blocks + b) * ns2 + s];
     const float vx = vd.x, vy = vd.y;
@@ -234,15 +247,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_f32(int64_t ns2, int 
   const int64_t ns = ns2 / 2;
   const int c = (int)(s / ns);
   const int64_t kq = s % ns;
-#pragma unroll
-  for (int e = 0; e < FLUX_EB32; e++) {
-    if (e0 + e >= nE) break;
-    double2 *dst = acc + (((int64_t)b * 2 + c) * nE + e0 + e) * ns + kq;
-    double2 v = *dst;
-    v.x += f2d(a[e].x);
-    v.y += f2d(a[e].y);
-    *dst = v;
-  }
+  flux_acc_add<FLUX_EB32>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB32, nE - e0), a);
 }
 
 void launch_flux_dft_f32(cudaStream_t s, int64_t ns2, int nE, int n_blocks, const int *count_p, int cap,
