@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         const int64_t p = p0 + pl;
         float msk = 1.0f;
         if (FWD && P.d1 && p < g.npt) msk = P.d1[(int)(p % g.n1)] * P.d2[(int)(p / g.n1)];
-        constexpr int U = FWD ? 16 : 24;
+        constexpr int U = 24;   // all of a 96-row tile's loads (and shears) in flight in one batch
         const int nk = T.Kp / 4;   // this thread's k values: tid/64 + 4u
         for (int u0 = 0; u0 < nk; u0 += U) {
           float2 v[U];
