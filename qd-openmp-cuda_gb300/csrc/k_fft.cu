@@ -640,10 +640,9 @@ template <bool INV> struct RegDFT<4, INV> {
   static __device__ __forceinline__ void run(float2 *v) { dft<float, 4>(v, INV); }
 };
 
-// v *= W_n^(+-e) from the shared twiddle table (three shears, see fft_stage)
-__device__ __forceinline__ void tw_apply(float2 &v, const float2 *tab, int e, int n, bool inv) {
+// v *= W_n^(+-e) given its table entry w (three shears, see fft_stage)
+__device__ __forceinline__ void tw_rotate(float2 &v, float2 w, int e, int n, bool inv) {
   if (e == 0) return;
-  const float2 w = tab[e];
   const float tt = inv ? -w.x : w.x, ss = inv ? -w.y : w.y;
   float x = v.x, y = v.y;
   if (4 * e > n && 4 * e < 3 * n) {
@@ -655,6 +654,10 @@ __device__ __forceinline__ void tw_apply(float2 &v, const float2 *tab, int e, in
   x = fmaf(tt, y, x);
   v.x = x;
   v.y = y;
+}
+// v *= W_n^(+-e) from the shared twiddle table indexed by e
+__device__ __forceinline__ void tw_apply(float2 &v, const float2 *tab, int e, int n, bool inv) {
+  if (e != 0) tw_rotate(v, tab[e], e, n, inv);
 }
 }  // namespace
 
@@ -861,12 +864,234 @@ __global__ void __launch_bounds__(THREADS, PIPE ? 2 : (THREADS <= 256 ? 3 : 1))
   }
 }
 
+// ---------------------------------------------------------- two-pass form
+// The separable transform as two independent passes with no cluster: a row pass
+// (rotational phase before the transform, forward row FFT, kinetic phase along R and
+// its energy, inverse) writes each slab back in natural order, where it stays in L2,
+// and a column pass (forward column FFT, kinetic phase along r and its energy,
+// inverse, scale, epilogue phase, rotational energy) finishes it.  Same arithmetic as
+// k_fft_slab_sep; what changes is that no CTA waits for another (no cluster barrier,
+// no distributed-shared-memory gather), and every per-l table a CTA needs is fetched
+// into shared memory right at its start, beside the slab's own loads.
+//
+// Row transposition buffer: element (a, b), a < A, b < B1, of a row at a B1 + (b ^ (a mod
+// B1)) (an XOR swizzle instead of padding), rows RS apart; the twiddle table W^(a b)
+// uses the same swizzle, so the forward (a uniform in a half-warp) and inverse (b
+// uniform) lookups are both free of bank conflicts.
+template <int A, int B1>
+constexpr int split_row_stride() {
+  return A * B1 + (B1 == 16 ? 0 : B1);
+}
+// W resident warps per SM (24: about 80 registers a thread, 32: 64)
+template <int A, int B1, int B2, int T, int W>
+__global__ void __launch_bounds__(T, W * 32 / T)
+    k_fft_split_rows(float2 *__restrict__ psi, Grid g, const SlabDesc *__restrict__ slabs,
+                     const float2 *__restrict__ tw1, FFTLift lf, double *__restrict__ ke_part, int ke_tiles,
+                     const int *status) {
+  constexpr int N1 = A * B1, N2 = A * B2;
+  constexpr int RPC = T / B1;   // rows per CTA
+  constexpr int CR = N2 / RPC;  // CTAs per slab
+  constexpr int RS = split_row_stride<A, B1>();
+  static_assert(T % B1 == 0 && N2 % RPC == 0 && A % B1 == 0 && 32 % B1 == 0 && N1 % 16 == 0, "row tiling");
+  if (status && *status) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ float red[T / 32];
+  float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+  float2 *X = tw + N1;
+  float2 *pro = X + RPC * RS;
+  const int tid = threadIdx.x;
+  const int sl = blockIdx.x / CR, c = blockIdx.x % CR;
+  const int l = __ldg(&slabs[sl].l);
+  const int q = tid / B1, j = tid % B1;
+  const int r = c * RPC + q;
+  float2 *row = psi + (int64_t)sl * g.npt + (int64_t)r * N1;
+  float2 v[A];
+#pragma unroll
+  for (int m = 0; m < A; m++) v[m] = __ldcs(row + j + B1 * m);
+  for (int p = tid; p < N1; p += T) {
+    const int a = p / B1, b = (p % B1) ^ (a % B1);
+    tw[p] = __ldg(tw1 + a * b);
+    if (lf.proR) pro[p] = __ldg(lf.proR + (int64_t)l * N1 + p);
+  }
+  const float2 pr = lf.proR ? __ldg(lf.pror + (int64_t)l * N2 + r) : make_float2(0.0f, 0.0f);
+  __syncthreads();
+
+  if (lf.proR) {
+#pragma unroll
+    for (int m = 0; m < A; m++) {
+      lift2(v[m].x, v[m].y, pro[j + B1 * m]);
+      lift2(v[m].x, v[m].y, pr);
+    }
+  }
+  float2 *G = X + q * RS;
+  float ke1 = 0.0f;
+  RegDFT<A, false>::run(v);
+#pragma unroll
+  for (int k1 = 1; k1 < A; k1++) tw_rotate(v[k1], tw[k1 * B1 + (j ^ (k1 % B1))], j * k1, N1, false);
+#pragma unroll
+  for (int k1 = 0; k1 < A; k1++) G[k1 * B1 + (j ^ (k1 % B1))] = v[k1];
+  __syncwarp();
+  float2 w[A];
+#pragma unroll
+  for (int h = 0; h < A / B1; h++)
+#pragma unroll
+    for (int jj = 0; jj < B1; jj++) w[h * B1 + jj] = G[(j + B1 * h) * B1 + (jj ^ j)];
+#pragma unroll
+  for (int h = 0; h < A / B1; h++) {
+    RegDFT<B1, false>::run(w + h * B1);
+#pragma unroll
+    for (int k2 = 0; k2 < B1; k2++) {   // frequency kR = k1 + A k2
+      const int kR = j + B1 * h + A * k2;
+      float2 &z = w[h * B1 + k2];
+      ke1 = fmaf(__ldg(lf.T1f + kR), z.x * z.x + z.y * z.y, ke1);
+      lift2(z.x, z.y, __ldg(lf.kinR + kR));
+    }
+    RegDFT<B1, true>::run(w + h * B1);
+#pragma unroll
+    for (int jj = 1; jj < B1; jj++) {
+      const int a = j + B1 * h;
+      tw_rotate(w[h * B1 + jj], tw[a * B1 + (jj ^ j)], a * jj, N1, true);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int h = 0; h < A / B1; h++)
+#pragma unroll
+    for (int jj = 0; jj < B1; jj++) G[(j + B1 * h) * B1 + (jj ^ j)] = w[h * B1 + jj];
+  __syncwarp();
+#pragma unroll
+  for (int k1 = 0; k1 < A; k1++) v[k1] = G[k1 * B1 + (j ^ (k1 % B1))];
+  RegDFT<A, true>::run(v);
+#pragma unroll
+  for (int m = 0; m < A; m++) row[j + B1 * m] = v[m];   // natural order; read back by the column pass
+
+  float kew = (float)N2 * ke1;
+  for (int o = 16; o > 0; o >>= 1) kew += __shfl_down_sync(0xffffffffu, kew, o);
+  if ((tid & 31) == 0) red[tid >> 5] = kew;
+  __syncthreads();
+  if (tid == 0) {   // FP32 over the warps, in a fixed order
+    float ke = 0.0f;
+    for (int wi = 0; wi < T / 32; wi++) ke += red[wi];
+    if (ke_part) ke_part[(int64_t)sl * ke_tiles + c] = (double)ke;
+  }
+}
+
+template <int A, int B1, int B2, int T, int W>
+__global__ void __launch_bounds__(T, W * 32 / T)
+    k_fft_split_cols(float2 *__restrict__ psi, Grid g, const SlabDesc *__restrict__ slabs,
+                     const float2 *__restrict__ tw2, FFTLift lf, double *__restrict__ ke_part, int ke_tiles,
+                     double *__restrict__ re_part, int re_tiles, float fscale, double scale, const int *status) {
+  constexpr int N1 = A * B1, N2 = A * B2;
+  constexpr int CPC = T / B2;        // columns per CTA
+  constexpr int CC = N1 / CPC;       // CTAs per slab
+  constexpr int CR = N2 / (T / B1);  // row-pass CTAs per slab: their kinetic partials come first
+  static_assert(T % B2 == 0 && N1 % CPC == 0 && A % B2 == 0, "column tiling");
+  if (status && *status) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ float2 red[T / 32];
+  float2 *t2 = reinterpret_cast<float2 *>(smem_raw);
+  float2 *Sc = t2 + N2;
+  float2 *epi = Sc + A * B2 * CPC;
+  float *i2 = reinterpret_cast<float *>(epi + N2);
+  const int tid = threadIdx.x;
+  const int sl = blockIdx.x / CC, c = blockIdx.x % CC;
+  const int l = __ldg(&slabs[sl].l);
+  const int col = tid % CPC, jc = tid / CPC;
+  const int R = c * CPC + col;
+  float2 *P = psi + (int64_t)sl * g.npt;
+  for (int p = tid; p < N2; p += T) {
+    t2[p] = __ldg(tw2 + p);
+    if (lf.epiR) epi[p] = __ldg(lf.epir + (int64_t)l * N2 + p);
+    if (re_part) i2[p] = __ldg(lf.I2f + p);
+  }
+  const float2 eR = lf.epiR ? __ldg(lf.epiR + (int64_t)l * N1 + R) : make_float2(0.0f, 0.0f);
+  const float I1 = re_part ? __ldg(lf.I1f + R) : 0.0f;
+  float2 v[A];
+#pragma unroll
+  for (int m = 0; m < A; m++) v[m] = __ldcs(P + (int64_t)(jc + B2 * m) * N1 + R);
+  __syncthreads();
+
+  float ke2 = 0.0f, ref = 0.0f;
+  RegDFT<A, false>::run(v);
+#pragma unroll
+  for (int k1 = 1; k1 < A; k1++) tw_apply(v[k1], t2, jc * k1, N2, false);
+#pragma unroll
+  for (int k1 = 0; k1 < A; k1++) Sc[(k1 * B2 + jc) * CPC + col] = v[k1];
+  __syncthreads();
+  {
+    float2 w[A];
+#pragma unroll
+    for (int h = 0; h < A / B2; h++)
+#pragma unroll
+      for (int jj = 0; jj < B2; jj++) w[h * B2 + jj] = Sc[((jc + B2 * h) * B2 + jj) * CPC + col];
+#pragma unroll
+    for (int h = 0; h < A / B2; h++) {
+      RegDFT<B2, false>::run(w + h * B2);
+#pragma unroll
+      for (int k2 = 0; k2 < B2; k2++) {   // frequency kr = k1 + A k2
+        const int kr = jc + B2 * h + A * k2;
+        float2 &z = w[h * B2 + k2];
+        ke2 = fmaf(__ldg(lf.T2f + kr), z.x * z.x + z.y * z.y, ke2);
+        lift2(z.x, z.y, __ldg(lf.kinr + kr));
+      }
+      RegDFT<B2, true>::run(w + h * B2);
+#pragma unroll
+      for (int jj = 1; jj < B2; jj++) tw_apply(w[h * B2 + jj], t2, jj * (jc + B2 * h), N2, true);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < A / B2; h++)
+#pragma unroll
+      for (int jj = 0; jj < B2; jj++) Sc[((jc + B2 * h) * B2 + jj) * CPC + col] = w[h * B2 + jj];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k1 = 0; k1 < A; k1++) v[k1] = Sc[(k1 * B2 + jc) * CPC + col];
+  RegDFT<A, true>::run(v);
+
+  // scale, rotational phase after the inverse transform, rotational energy, store
+  const float lls2 = (float)l * (float)(l + 1) * (fscale != 0.0f ? 1.0f : (float)(scale * scale));
+#pragma unroll
+  for (int m = 0; m < A; m++) {
+    const int rr = jc + B2 * m;
+    float x = v[m].x, y = v[m].y;
+    if (fscale != 0.0f) {
+      x *= fscale;
+      y *= fscale;
+    }
+    if (lf.epiR) {
+      lift2(x, y, eR);
+      lift2(x, y, epi[rr]);
+    }
+    if (re_part) ref = fmaf(lls2 * (I1 + i2[rr]), x * x + y * y, ref);
+    __stcs(P + (int64_t)rr * N1 + R, fscale != 0.0f ? make_float2(x, y) : scaled_c64(x, y, 0.0f, scale));
+  }
+  float kew = ke2 * (1.0f / (float)N1), rew = ref;
+  for (int o = 16; o > 0; o >>= 1) {
+    kew += __shfl_down_sync(0xffffffffu, kew, o);
+    rew += __shfl_down_sync(0xffffffffu, rew, o);
+  }
+  if ((tid & 31) == 0) red[tid >> 5] = make_float2(kew, rew);
+  __syncthreads();
+  if (tid == 0) {
+    float ke = 0.0f, re = 0.0f;
+    for (int wi = 0; wi < T / 32; wi++) {
+      ke += red[wi].x;
+      re += red[wi].y;
+    }
+    if (ke_part) ke_part[(int64_t)sl * ke_tiles + CR + c] = (double)ke;
+    if (re_part) re_part[(int64_t)sl * re_tiles + c] = (double)re;
+  }
+}
+
 namespace {
-// instantiations of the separable slab FFT: (n1, n2) -> (A, B1, B2, threads).  Several
-// thread counts (and so cluster sizes, C = A B2 B1 / threads CTAs per slab) exist for the
-// production grids; the autotuner times them on the session's own slabs.
+// instantiations of the separable slab FFT: (n1, n2) -> (A, B1, B2, threads, mode).  Mode 0:
+// one cluster per slab (C = A B2 B1 / threads CTAs); 1: a persistent grid of such clusters;
+// 2 and 3: the two-pass form (row pass, then column pass, no cluster) built for 24 and 32
+// resident warps per SM.  Several thread counts exist for the production grids; the
+// autotuner times them on the session's own slabs.
 struct SepShape {
-  int n1, n2, A, B1, B2, threads, pipe;
+  int n1, n2, A, B1, B2, threads, mode;
 };
 constexpr SepShape kSepShapes[] = {
     {256, 128, 16, 16, 8, 256, 0},
@@ -881,6 +1106,12 @@ constexpr SepShape kSepShapes[] = {
     {256, 128, 16, 16, 8, 256, 1},
     {192, 96, 24, 8, 4, 192, 1},
     {192, 96, 24, 8, 4, 96, 1},
+    {256, 128, 16, 16, 8, 256, 2},
+    {256, 128, 16, 16, 8, 256, 3},
+    {256, 128, 16, 16, 8, 128, 3},
+    {192, 96, 24, 8, 4, 192, 2},
+    {192, 96, 24, 8, 4, 96, 2},
+    {192, 96, 24, 8, 4, 192, 3},
 };
 constexpr int kNumSep = (int)(sizeof(kSepShapes) / sizeof(kSepShapes[0]));
 
@@ -893,13 +1124,57 @@ template <int A, int B1, int B2, int T>
 int sep_cluster() {
   return A * B2 / (T / B1);
 }
+// two-pass form: shared memory of each pass, CTAs per slab of each pass
+template <int A, int B1, int B2, int T>
+size_t split_rows_smem() {
+  return (size_t)A * B1 * sizeof(float2) + ((size_t)(T / B1) * split_row_stride<A, B1>() + A * B1) * sizeof(float2);
+}
+template <int A, int B1, int B2, int T>
+size_t split_cols_smem() {
+  return (size_t)A * B2 * sizeof(float2) + ((size_t)A * B2 * (T / B2) + A * B2) * sizeof(float2) +
+         (size_t)A * B2 * sizeof(float);
+}
+template <int A, int B1, int B2, int T>
+constexpr int split_row_ctas() {
+  return A * B2 / (T / B1);
+}
+template <int A, int B1, int B2, int T>
+constexpr int split_col_ctas() {
+  return A * B1 / (T / B2);
+}
 
-template <int A, int B1, int B2, int T, bool PIPE>
+// kinetic-energy and rotational-energy partials per slab: one per CTA of the cluster, or
+// the row pass's CTAs then the column pass's (kinetic) and the column pass's (rotational)
+template <int A, int B1, int B2, int T, int MODE>
+int shape_ke_tiles() {
+  if constexpr (MODE >= 2)
+    return split_row_ctas<A, B1, B2, T>() + split_col_ctas<A, B1, B2, T>();
+  else
+    return sep_cluster<A, B1, B2, T>();
+}
+template <int A, int B1, int B2, int T, int MODE>
+int shape_re_tiles() {
+  if constexpr (MODE >= 2)
+    return split_col_ctas<A, B1, B2, T>();
+  else
+    return sep_cluster<A, B1, B2, T>();
+}
+
+template <int A, int B1, int B2, int T, int MODE>
 void sep_set_attr() {
-  QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T, PIPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)sep_smem_bytes<A, B1, B2, T>()));
-  if (sep_cluster<A, B1, B2, T>() > 8)
-    QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T, PIPE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  if constexpr (MODE >= 2) {
+    constexpr int W = MODE == 2 ? 24 : 32;
+    QD_CUDA(cudaFuncSetAttribute(k_fft_split_rows<A, B1, B2, T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)split_rows_smem<A, B1, B2, T>()));
+    QD_CUDA(cudaFuncSetAttribute(k_fft_split_cols<A, B1, B2, T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)split_cols_smem<A, B1, B2, T>()));
+  } else {
+    QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T, MODE == 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sep_smem_bytes<A, B1, B2, T>()));
+    if (sep_cluster<A, B1, B2, T>() > 8)
+      QD_CUDA(cudaFuncSetAttribute(k_fft_slab_sep<A, B1, B2, T, MODE == 1>,
+                                   cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  }
 }
 
 template <int A, int B1, int B2, int T, bool PIPE>
@@ -937,32 +1212,61 @@ void sep_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, 
                              status));
 }
 
-#define QD_SEP_CASES(X)         \
-  X(0, 16, 16, 8, 256, false)   \
-  X(1, 24, 8, 4, 96, false)     \
-  X(2, 8, 8, 4, 128, false)     \
-  X(3, 8, 4, 2, 32, false)      \
-  X(4, 4, 4, 2, 32, false)      \
-  X(5, 16, 16, 8, 512, false)   \
-  X(6, 16, 16, 8, 128, false)   \
-  X(7, 24, 8, 4, 192, false)    \
-  X(8, 24, 8, 4, 384, false)    \
-  X(9, 16, 16, 8, 256, true)    \
-  X(10, 24, 8, 4, 192, true)    \
-  X(11, 24, 8, 4, 96, true)
+template <int A, int B1, int B2, int T, int W>
+void split_launch(cudaStream_t s, const Grid &g, const FFTPlan &p, float2 *psi_j, const SlabDesc *slabs, int n_slabs,
+                  const FFTLift &lf, double *ke_part, double *re_part, float fscale, double scale, const int *status) {
+  const int ke_tiles = shape_ke_tiles<A, B1, B2, T, 2>(), re_tiles = shape_re_tiles<A, B1, B2, T, 2>();
+  k_fft_split_rows<A, B1, B2, T, W>
+      <<<(unsigned)(n_slabs * split_row_ctas<A, B1, B2, T>()), T, split_rows_smem<A, B1, B2, T>(), s>>>(
+          psi_j, g, slabs, (const float2 *)p.tw1_f, lf, ke_part, ke_tiles, status);
+  QD_CUDA(cudaGetLastError());
+  k_fft_split_cols<A, B1, B2, T, W>
+      <<<(unsigned)(n_slabs * split_col_ctas<A, B1, B2, T>()), T, split_cols_smem<A, B1, B2, T>(), s>>>(
+          psi_j, g, slabs, (const float2 *)p.tw2_f, lf, ke_part, ke_tiles, re_part, re_tiles, fscale, scale, status);
+  QD_CUDA(cudaGetLastError());
+}
+
+#define QD_SEP_CASES(X)     \
+  X(0, 16, 16, 8, 256, 0)   \
+  X(1, 24, 8, 4, 96, 0)     \
+  X(2, 8, 8, 4, 128, 0)     \
+  X(3, 8, 4, 2, 32, 0)      \
+  X(4, 4, 4, 2, 32, 0)      \
+  X(5, 16, 16, 8, 512, 0)   \
+  X(6, 16, 16, 8, 128, 0)   \
+  X(7, 24, 8, 4, 192, 0)    \
+  X(8, 24, 8, 4, 384, 0)    \
+  X(9, 16, 16, 8, 256, 1)   \
+  X(10, 24, 8, 4, 192, 1)   \
+  X(11, 24, 8, 4, 96, 1)    \
+  X(12, 16, 16, 8, 256, 2)  \
+  X(13, 16, 16, 8, 256, 3)  \
+  X(14, 16, 16, 8, 128, 3)  \
+  X(15, 24, 8, 4, 192, 2)   \
+  X(16, 24, 8, 4, 96, 2)    \
+  X(17, 24, 8, 4, 192, 3)
 
 void sep_dispatch_attr(int id) {
   switch (id) {
-#define QD_X(i, a, b1, b2, t, pipe) \
-  case i: sep_set_attr<a, b1, b2, t, pipe>(); break;
+#define QD_X(i, a, b1, b2, t, mode) \
+  case i: sep_set_attr<a, b1, b2, t, mode>(); break;
     QD_SEP_CASES(QD_X)
 #undef QD_X
   }
 }
-int sep_dispatch_cluster(int id) {
+int sep_dispatch_ke_tiles(int id) {
   switch (id) {
-#define QD_X(i, a, b1, b2, t, pipe) \
-  case i: return sep_cluster<a, b1, b2, t>();
+#define QD_X(i, a, b1, b2, t, mode) \
+  case i: return shape_ke_tiles<a, b1, b2, t, mode>();
+    QD_SEP_CASES(QD_X)
+#undef QD_X
+  }
+  return 0;
+}
+int sep_dispatch_re_tiles(int id) {
+  switch (id) {
+#define QD_X(i, a, b1, b2, t, mode) \
+  case i: return shape_re_tiles<a, b1, b2, t, mode>();
     QD_SEP_CASES(QD_X)
 #undef QD_X
   }
@@ -972,9 +1276,14 @@ void sep_dispatch_launch(int id, cudaStream_t s, const Grid &g, const FFTPlan &p
                          const SlabDesc *slabs, int n_slabs, const FFTLift &lf, double *ke_part, double *re_part,
                          float fscale, double scale, const int *status) {
   switch (id) {
-#define QD_X(i, a, b1, b2, t, pipe)                                                                          \
-  case i:                                                                                                     \
-    sep_launch<a, b1, b2, t, pipe>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale, status); \
+#define QD_X(i, a, b1, b2, t, mode)                                                                               \
+  case i:                                                                                                          \
+    if constexpr (mode >= 2)                                                                                       \
+      split_launch<a, b1, b2, t, mode == 2 ? 24 : 32>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, \
+                                                      scale, status);                                              \
+    else                                                                                                           \
+      sep_launch<a, b1, b2, t, mode == 1>(s, g, p, psi_j, slabs, n_slabs, lf, ke_part, re_part, fscale, scale,    \
+                                          status);                                                                 \
     break;
     QD_SEP_CASES(QD_X)
 #undef QD_X
@@ -1022,7 +1331,7 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
     throw Error{QD_ERR_UNSUPPORTED, "FFT grid size above 4096"};
   p.cluster = choose_cluster(n1, n2);
   p.sep = -1;
-  p.sep_cluster = 0;
+  p.sep_ke_tiles = p.sep_re_tiles = 0;
   // mixed-form candidates in order of preference without timing: separable shapes
   // (first instantiated first), the two-exchange cluster kernel, the three-pass kernels
   p.n_cand = 0;
@@ -1069,7 +1378,8 @@ void fft_plan_init(FFTPlan &p, int n1, int n2) {
 void fft_plan_choose(FFTPlan &p, int choice) {
   p.choice = choice;
   p.sep = choice >= FFT_SEP0 ? choice - FFT_SEP0 : -1;
-  p.sep_cluster = p.sep >= 0 ? sep_dispatch_cluster(p.sep) : 0;
+  p.sep_ke_tiles = p.sep >= 0 ? sep_dispatch_ke_tiles(p.sep) : 0;
+  p.sep_re_tiles = p.sep >= 0 ? sep_dispatch_re_tiles(p.sep) : 0;
   p.use_cluster = choice == FFT_CLUSTER;
 }
 
@@ -1078,8 +1388,10 @@ std::string fft_choice_name(int choice) {
   if (choice >= FFT_SEP0) {
     const SepShape &q = kSepShapes[choice - FFT_SEP0];
     name = "separable A=" + std::to_string(q.A) + " B1=" + std::to_string(q.B1) + " B2=" + std::to_string(q.B2) +
-           " threads=" + std::to_string(q.threads) + " cluster=" + std::to_string(sep_dispatch_cluster(choice - FFT_SEP0)) +
-           (q.pipe ? " persistent" : "");
+           " threads=" + std::to_string(q.threads) +
+           (q.mode >= 2 ? std::string(q.mode == 2 ? " two-pass 24 warps/SM" : " two-pass 32 warps/SM")
+                        : " cluster=" + std::to_string(sep_dispatch_ke_tiles(choice - FFT_SEP0)) +
+                              (q.mode == 1 ? " persistent" : ""));
   } else {
     name = choice == FFT_CLUSTER ? "cluster two-exchange" : "three-pass";
   }
@@ -1096,20 +1408,21 @@ void fft_plan_free(FFTPlan &p) {
 }
 
 // partial-sum tiles per slab: the single-pass FP32 form writes one per CTA of
-// the cluster, the three-pass forms one per column / row tile
+// the cluster, the two-pass form one per CTA of each pass (kinetic) and of the
+// column pass (rotational), the three-pass forms one per column / row tile
 int fft_col_tiles(const FFTPlan &p, int precision) {
-  if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_cluster;
+  if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_ke_tiles;
   return (precision == QD_PRECISION_MIXED && p.use_cluster) ? p.cluster : p.n1 / p.cols_per_cta;
 }
 int fft_row_tiles(const FFTPlan &p, int precision) {
-  if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_cluster;
+  if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_re_tiles;
   return (precision == QD_PRECISION_MIXED && p.use_cluster) ? p.cluster : p.n2 / p.rows_per_cta;
 }
 // partial-sum tiles per slab of any mixed-form candidate (buffers sized for tuning)
 int fft_max_tiles(const FFTPlan &p) {
   int t = std::max(p.n1 / p.cols_per_cta, p.n2 / p.rows_per_cta);
   for (int q = 0; q < p.n_cand; q++) {
-    if (p.cand[q] >= FFT_SEP0) t = std::max(t, sep_dispatch_cluster(p.cand[q] - FFT_SEP0));
+    if (p.cand[q] >= FFT_SEP0) t = std::max(t, sep_dispatch_ke_tiles(p.cand[q] - FFT_SEP0));
     if (p.cand[q] == FFT_CLUSTER) t = std::max(t, p.cluster);
   }
   return t;

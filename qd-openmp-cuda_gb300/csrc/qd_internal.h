@@ -128,7 +128,8 @@ struct FFTPlan {
   int cols_per_cta;
   int cluster;   // CTAs per slab of the single-pass FP32 FFT (0: three-pass form)
   int sep;           // shape index of the separable single-pass FP32 FFT, -1: none
-  int sep_cluster;   // its CTAs per slab
+  int sep_ke_tiles;  // its kinetic-energy partials per slab
+  int sep_re_tiles;  // its rotational-energy partials per slab
   int use_cluster;   // the two-exchange cluster kernel is the mixed form's FFT
   // mixed-form FFT kernels that fit this grid (FFT_SEP0 + shape, FFT_CLUSTER,
   // FFT_THREE_PASS) and the one in use (fft_plan_choose; the autotuner times them)
