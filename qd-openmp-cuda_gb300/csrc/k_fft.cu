@@ -984,8 +984,8 @@ __global__ void __launch_bounds__(T, W * 32 / T)
   constexpr int N1 = A * B1, N2 = A * B2;
   constexpr int CPC = T / B2;        // columns per CTA
   constexpr int CC = N1 / CPC;       // CTAs per slab
-  constexpr int CR = N2 / (T / B1);  // row-pass CTAs per slab: their kinetic partials come first
   static_assert(T % B2 == 0 && N1 % CPC == 0 && A % B2 == 0, "column tiling");
+  static_assert(N2 / (T / B1) == CC, "both passes have A B1 B2 / T CTAs per slab");
   if (status && *status) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float2 red[T / 32];
@@ -1079,7 +1079,8 @@ __global__ void __launch_bounds__(T, W * 32 / T)
       ke += red[wi].x;
       re += red[wi].y;
     }
-    if (ke_part) ke_part[(int64_t)sl * ke_tiles + CR + c] = (double)ke;
+    // the row pass's CTA c left its kinetic partial in this slot: one partial per CTA pair
+    if (ke_part) ke_part[(int64_t)sl * ke_tiles + c] += (double)ke;
     if (re_part) re_part[(int64_t)sl * re_tiles + c] = (double)re;
   }
 }
@@ -1143,12 +1144,12 @@ constexpr int split_col_ctas() {
   return A * B1 / (T / B2);
 }
 
-// kinetic-energy and rotational-energy partials per slab: one per CTA of the cluster, or
-// the row pass's CTAs then the column pass's (kinetic) and the column pass's (rotational)
+// kinetic-energy and rotational-energy partials per slab: one per CTA of the cluster, or one
+// per CTA of the column pass (its CTA c adds the row pass's CTA c to its own kinetic partial)
 template <int A, int B1, int B2, int T, int MODE>
 int shape_ke_tiles() {
   if constexpr (MODE >= 2)
-    return split_row_ctas<A, B1, B2, T>() + split_col_ctas<A, B1, B2, T>();
+    return split_col_ctas<A, B1, B2, T>();
   else
     return sep_cluster<A, B1, B2, T>();
 }
@@ -1408,8 +1409,8 @@ void fft_plan_free(FFTPlan &p) {
 }
 
 // partial-sum tiles per slab: the single-pass FP32 form writes one per CTA of
-// the cluster, the two-pass form one per CTA of each pass (kinetic) and of the
-// column pass (rotational), the three-pass forms one per column / row tile
+// the cluster, the two-pass form one per CTA of the column pass, the three-pass
+// forms one per column / row tile
 int fft_col_tiles(const FFTPlan &p, int precision) {
   if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_ke_tiles;
   return (precision == QD_PRECISION_MIXED && p.use_cluster) ? p.cluster : p.n1 / p.cols_per_cta;
