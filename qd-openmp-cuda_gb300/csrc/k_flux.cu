@@ -95,14 +95,17 @@ constexpr int FLUX_MAXC = 64;     // maximum chunk length
 // energy.
 __device__ inline double2 widen(float2 v) { return make_double2(f2d(v.x), f2d(v.y)); }
 __device__ inline double2 widen(double2 v) { return v; }
+// fresh: the accumulators hold no earlier sum yet (first transform of a call), so they are
+// written without being read
 template <int EB, typename T>
-__device__ inline void flux_acc_add(double2 *__restrict__ dst, int64_t ns, int ne, const T *v) {
+__device__ inline void flux_acc_add(double2 *__restrict__ dst, int64_t ns, int ne, const T *v, bool fresh) {
   constexpr int CH = EB < 8 ? EB : 8;
 #pragma unroll
   for (int e1 = 0; e1 < EB; e1 += CH) {
     double2 old[CH];
 #pragma unroll
-    for (int u = 0; u < CH; u++) old[u] = e1 + u < ne ? dst[(int64_t)(e1 + u) * ns] : make_double2(0.0, 0.0);
+    for (int u = 0; u < CH; u++)
+      old[u] = e1 + u < ne && !fresh ? dst[(int64_t)(e1 + u) * ns] : make_double2(0.0, 0.0);
 #pragma unroll
     for (int u = 0; u < CH; u++)
       if (e1 + u < ne) {
@@ -146,7 +149,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft(int64_t ns2, int nE, 
   const int64_t ns = ns2 / 2;
   const int c = (int)(s / ns);
   const int64_t kq = s % ns;
-  flux_acc_add<FLUX_EB>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB, nE - e0), a);
+  flux_acc_add<FLUX_EB>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB, nE - e0), a, false);
 }
 
 void launch_flux_dft(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_blocks, const double2 *buf, int count,
@@ -168,8 +171,10 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_dev(int64_t ns2, int 
                                                                int cap,
                                                                const double2 *__restrict__ buf,
                                                                const double2 *__restrict__ phase,
-                                                               double2 *__restrict__ acc, const int *status) {
+                                                               double2 *__restrict__ acc, const int *status,
+                                                               const int *fresh) {
   if (status && *status) return;
+  const bool fr = fresh && *fresh;
   const int count = min(min(*count_p, cap), FLUX_MAXC);
   if (count <= 0) return;
   __shared__ double2 ph[FLUX_MAXC][FLUX_EB];
@@ -197,7 +202,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_dft_dev(int64_t ns2, int 
   const int64_t ns = ns2 / 2;
   const int c = (int)(s / ns);
   const int64_t kq = s % ns;
-  flux_acc_add<FLUX_EB>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB, nE - e0), a);
+  flux_acc_add<FLUX_EB>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB, nE - e0), a, fr);
 }
 
 // Mixed form of the transform: products and the chunk's partial sums in FP32
@@ -214,8 +219,10 @@ constexpr int FLUX_EB32 = 8;
 __global__ void __launch_bounds__(FLUX_THREADS, 6) k_flux_dft_f32(int64_t ns2, int nE, int n_blocks, const int *count_p,
                                                                int cap, const float2 *__restrict__ buf,
                                                                const double2 *__restrict__ phase,
-                                                               double2 *__restrict__ acc, const int *status) {
+                                                               double2 *__restrict__ acc, const int *status,
+                                                               const int *fresh) {
   if (status && *status) return;
+  const bool fr = fresh && *fresh;
   const int count = min(min(*count_p, cap), FLUX_MAXC);
   if (count <= 0) return;
   __shared__ float2 ph[FLUX_MAXC][FLUX_EB32];
@@ -247,24 +254,26 @@ __global__ void __launch_bounds__(FLUX_THREADS, 6) k_flux_dft_f32(int64_t ns2, i
   const int64_t ns = ns2 / 2;
   const int c = (int)(s / ns);
   const int64_t kq = s % ns;
-  flux_acc_add<FLUX_EB32>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB32, nE - e0), a);
+  flux_acc_add<FLUX_EB32>(acc + (((int64_t)b * 2 + c) * nE + e0) * ns + kq, ns, min(FLUX_EB32, nE - e0), a, fr);
 }
 
 void launch_flux_dft_f32(cudaStream_t s, int64_t ns2, int nE, int n_blocks, const int *count_p, int cap,
-                         const float2 *buf, const double2 *phase, double2 *acc, const int *status) {
+                         const float2 *buf, const double2 *phase, double2 *acc, const int *status, const int *fresh) {
   dim3 grid((unsigned)((ns2 + FLUX_THREADS - 1) / FLUX_THREADS), (unsigned)((nE + FLUX_EB32 - 1) / FLUX_EB32),
             (unsigned)n_blocks);
-  k_flux_dft_f32<<<grid, FLUX_THREADS, 0, s>>>(ns2, nE, n_blocks, count_p, cap, buf, phase, acc, status);
+  k_flux_dft_f32<<<grid, FLUX_THREADS, 0, s>>>(ns2, nE, n_blocks, count_p, cap, buf, phase, acc, status, fresh);
 }
 
-// P(E) per problem: one CTA per (E, problem)
+// P(E) per problem: one CTA per (E, problem); accumulators still marked fresh hold
+// no transform yet and count as zero
 __global__ void k_flux_crp(Grid g, int nE, const int *__restrict__ pblock0, const double2 *__restrict__ acc,
-                           const double *__restrict__ w, const double *__restrict__ eta_sq, double *__restrict__ crp) {
+                           const double *__restrict__ w, const double *__restrict__ eta_sq, double *__restrict__ crp,
+                           const int *fresh) {
   __shared__ double red[32];
   const int e = blockIdx.x, pr = blockIdx.y;
   const int64_t ns = (int64_t)g.nth * g.n1;
   double s = 0.0;
-  for (int b = pblock0[pr]; b < pblock0[pr + 1]; b++) {
+  for (int b = pblock0[pr]; b < pblock0[pr + 1] && !(fresh && *fresh); b++) {
     const double2 *A = acc + (((int64_t)b * 2 + 0) * nE + e) * ns;
     const double2 *D = acc + (((int64_t)b * 2 + 1) * nE + e) * ns;
     for (int64_t q = threadIdx.x; q < ns; q += blockDim.x) {
@@ -279,9 +288,9 @@ __global__ void k_flux_crp(Grid g, int nE, const int *__restrict__ pblock0, cons
 }
 
 void launch_flux_crp(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_problems, const int *block0_of_problem,
-                     const double2 *acc, const double *w, const double *eta_sq, double *crp) {
+                     const double2 *acc, const double *w, const double *eta_sq, double *crp, const int *fresh) {
   dim3 grid((unsigned)f.n_energies, (unsigned)n_problems);
-  k_flux_crp<<<grid, 256, 0, s>>>(g, f.n_energies, block0_of_problem, acc, w, eta_sq, crp);
+  k_flux_crp<<<grid, 256, 0, s>>>(g, f.n_energies, block0_of_problem, acc, w, eta_sq, crp, fresh);
 }
 
 }  // namespace qd

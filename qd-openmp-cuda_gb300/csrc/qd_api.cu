@@ -331,6 +331,7 @@ struct qd_session {
   float2 *flux_buf_f = nullptr;   // mixed form: surface buffer in c64 (FP32 values)
   double *fd = nullptr, *flux_E = nullptr, *flux_eta = nullptr, *crp = nullptr, *flux_t0 = nullptr;
   int *flux_count = nullptr, *flux_slot = nullptr;
+  int *flux_fresh = nullptr;   // nonzero: the accumulators hold no transform of this call yet
   unsigned *step_done = nullptr;
   float2 *half_v_lift = nullptr;
   float *fdf = nullptr;
@@ -346,6 +347,12 @@ struct qd_session {
   float *I1f = nullptr, *I2f = nullptr;
   int steps = 0;   // host mirror of time.steps
   int launches_per_step = 0;
+  // end of a call: the download stream (psi beside the flux transform), the event that
+  // ends the steps (also: the potential comparison at the start), and the status words and
+  // the comparison flag read back through pinned memory
+  cudaStream_t stream_dl = nullptr;
+  cudaEvent_t ev_steps = nullptr;
+  int *h_status = nullptr;   // [status, status step, potential differs]
   cudaGraphExec_t graph_chunk = nullptr;
   int graph_steps = 0;
   // reuse across qd_evolve calls of the same shape: the key, host copies of the
@@ -447,7 +454,11 @@ __global__ void k_flux_phase_dev(const double *__restrict__ E, int nE, int cap, 
   phase[q] = make_double2(dt * c, dt * s);
 }
 
-__global__ void k_flux_reset(int *count) { *count = 0; }
+// after a transform: the buffer is empty, and the accumulators hold a sum (when it ran)
+__global__ void k_flux_reset(int *count, int *fresh, const int *status) {
+  if (*count > 0 && !*status) *fresh = 0;
+  *count = 0;
+}
 
 }  // namespace qd
 
@@ -458,6 +469,12 @@ qd_session::~qd_session() {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
   }
+  if (stream_dl) {
+    cudaStreamSynchronize(stream_dl);
+    cudaStreamDestroy(stream_dl);
+  }
+  if (ev_steps) cudaEventDestroy(ev_steps);
+  if (h_status) cudaFreeHost(h_status);
   // the arena's chunks are released by its destructor
 }
 
@@ -466,7 +483,7 @@ namespace qd {
 // flux DFT reading count/t0 from the device (graph friendly)
 __global__ void k_flux_dft_dev(int64_t ns2, int nE, int n_blocks, const int *count_p, int cap,
                                const double2 *__restrict__ buf, const double2 *__restrict__ phase,
-                               double2 *__restrict__ acc, const int *status);
+                               double2 *__restrict__ acc, const int *status, const int *fresh);
 
 static void enqueue_flux_dft(qd_session *s) {
   const int nE = s->flux.n_energies;
@@ -477,14 +494,14 @@ static void enqueue_flux_dft(qd_session *s) {
   const int64_t ns2 = 2LL * s->g.nth * s->g.n1;
   if (s->precision == QD_PRECISION_MIXED) {
     launch_flux_dft_f32(s->stream, ns2, nE, s->n_blocks, s->flux_count, cap, s->flux_buf_f, s->flux_phase,
-                        s->flux_acc, s->status);
+                        s->flux_acc, s->status, s->flux_fresh);
   } else {
     dim3 grid((unsigned)((ns2 + 127) / 128), (unsigned)((nE + 7) / 8), (unsigned)s->n_blocks);
     k_flux_dft_dev<<<grid, 128, 0, s->stream>>>(ns2, nE, s->n_blocks, s->flux_count, cap, s->flux_buf,
-                                                 s->flux_phase, s->flux_acc, s->status);
+                                                 s->flux_phase, s->flux_acc, s->status, s->flux_fresh);
   }
   prof_mark(s->stream, "flux_dft");
-  k_flux_reset<<<1, 1, 0, s->stream>>>(s->flux_count);
+  k_flux_reset<<<1, 1, 0, s->stream>>>(s->flux_count, s->flux_fresh, s->status);
   prof_mark(s->stream, "flux_reset");
 }
 
@@ -661,8 +678,7 @@ static void theta_from_host(qd_session *s, int64_t off, int64_t n, const double 
     launch_narrow(st, s->xfer, s->psi_thf + off + q, m);
   }
 }
-static void theta_to_host(qd_session *s, int64_t off, int64_t n, double *host) {
-  cudaStream_t st = s->stream;
+static void theta_to_host(qd_session *s, int64_t off, int64_t n, double *host, cudaStream_t st) {
   if (!s->psi_thf) {
     QD_CUDA(cudaMemcpyAsync(host, s->psi_th + off, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     return;
@@ -849,6 +865,9 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     throw Error{QD_ERR_NO_DEVICE, "no CUDA device"};
   QD_CUDA(cudaGetDevice(&s->device));
   QD_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  QD_CUDA(cudaStreamCreateWithFlags(&s->stream_dl, cudaStreamNonBlocking));
+  QD_CUDA(cudaEventCreateWithFlags(&s->ev_steps, cudaEventDisableTiming));
+  QD_CUDA(cudaMallocHost(&s->h_status, 3 * sizeof(int)));
   s->key = session_key(problems, n_problems);
   cudaStream_t st = s->stream;
   const qd_fh2data *d0 = problems[0];
@@ -1118,6 +1137,7 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
     else
       s->flux_buf = s->alloc<double2>((size_t)s->flux.chunk * s->n_blocks * 2 * ns);
     s->flux_acc = s->alloc<double2>((size_t)s->n_blocks * 2 * c.n_energies * ns);
+    s->flux_fresh = s->alloc<int>(1);
     s->flux_phase = s->alloc<double2>((size_t)s->flux.chunk * c.n_energies);
     s->half_v = s->alloc<double2>((size_t)g.nth * c.n_gradient_points * g.n1);
     std::vector<double> fdw = fd_weights(c.n_gradient_points);
@@ -1160,6 +1180,9 @@ static void session_load(qd_session *s, qd_fh2data *const *problems, int n_probl
     QD_CUDA(cudaMemcpyAsync(s->pot_stage, d0->pot, (size_t)nth_pt * sizeof(double), cudaMemcpyHostToDevice, st));
     QD_CUDA(cudaMemsetAsync(s->d_flag, 0, sizeof(int), st));
     k_differs<<<grid_for(nth_pt, 256, 152 * 8), 256, 0, st>>>(s->pot_stage, s->pot, nth_pt, s->d_flag);
+    // the flag is read as soon as the comparison ends, while the wave packets upload
+    QD_CUDA(cudaMemcpyAsync(s->h_status + 2, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    QD_CUDA(cudaEventRecord(s->ev_steps, st));
   } else {
     QD_CUDA(cudaMemcpyAsync(s->pot, d0->pot, (size_t)nth_pt * sizeof(double), cudaMemcpyHostToDevice, st));
   }
@@ -1212,10 +1235,8 @@ static void session_load(qd_session *s, qd_fh2data *const *problems, int n_probl
     }
   }
   if (reuse) {
-    int flag = 0;
-    QD_CUDA(cudaMemcpyAsync(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
-    QD_CUDA(cudaStreamSynchronize(st));
-    if (flag) {
+    QD_CUDA(cudaEventSynchronize(s->ev_steps));
+    if (s->h_status[2]) {
       pot_changed = true;
       QD_CUDA(cudaMemcpyAsync(s->pot, s->pot_stage, (size_t)nth_pt * sizeof(double), cudaMemcpyDeviceToDevice, st));
     }
@@ -1255,14 +1276,22 @@ static void session_load(qd_session *s, qd_fh2data *const *problems, int n_probl
       launch_build_half_v(st, g, s->flux, s->pot, s->dt, s->half_v);
       if (s->half_v_lift) launch_build_half_v_lift(st, g, s->flux, s->pot, s->dt, s->half_v_lift);
     }
+    // accumulators: the caller's sums, or none (the first transform writes them, P(E)
+    // before it is zero); all problems of a batch either pass theirs or none
+    bool any_acc = false, all_acc = true;
     for (int p = 0; p < n_problems; p++) {
+      any_acc = any_acc || problems[p]->CRP.accumulators;
+      all_acc = all_acc && problems[p]->CRP.accumulators;
+    }
+    for (int p = 0; p < n_problems && any_acc; p++) {
       double2 *dst = s->flux_acc + (int64_t)s->h_pblock0[p] * 2 * c.n_energies * ns;
       const size_t bytes = (size_t)s->probs[p].n_omegas * 2 * c.n_energies * ns * sizeof(double2);
       if (problems[p]->CRP.accumulators)
         QD_CUDA(cudaMemcpyAsync(dst, problems[p]->CRP.accumulators, bytes, cudaMemcpyHostToDevice, st));
-      else
+      else if (!all_acc)
         QD_CUDA(cudaMemsetAsync(dst, 0, bytes, st));
     }
+    QD_CUDA(cudaMemsetAsync(s->flux_fresh, any_acc ? 0 : 1, sizeof(int), st));
   }
   QD_CUDA(cudaGetLastError());
 }
@@ -1275,20 +1304,22 @@ static void session_create(qd_session *s, qd_fh2data *const *problems, int n_pro
 }
 
 // -------------------------------------------------------------- running
+static void throw_status(int st, int stp) {
+  if (st == QD_ERR_NORM)
+    throw Error{st, "Total module error: norm above 1 at step " + std::to_string(stp) +
+                        " (print_energies, cudaOpenMP2.cu:437-440)"};
+  if (st == QD_ERR_TIMEOUT)
+    throw Error{st, "a device-side wait gave up after 1 s: a tensor-core contraction's pipeline stalled"};
+  if (st == QD_ERR_INVALID) throw Error{st, "flux surface buffer full (more steps buffered than its capacity)"};
+  if (st) throw Error{st, "device status " + std::to_string(st)};
+}
 static void check_status(qd_session *s) {
   QD_CUDA(cudaStreamSynchronize(s->stream));
   QD_CUDA(cudaGetLastError());
   int st = 0, stp = 0;
   QD_CUDA(cudaMemcpy(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost));
-  if (st == QD_ERR_NORM) {
-    QD_CUDA(cudaMemcpy(&stp, s->status_step, sizeof(int), cudaMemcpyDeviceToHost));
-    throw Error{st, "Total module error: norm above 1 at step " + std::to_string(stp) +
-                        " (print_energies, cudaOpenMP2.cu:437-440)"};
-  }
-  if (st == QD_ERR_TIMEOUT)
-    throw Error{st, "a device-side wait gave up after 1 s: a tensor-core contraction's pipeline stalled"};
-  if (st == QD_ERR_INVALID) throw Error{st, "flux surface buffer full (more steps buffered than its capacity)"};
-  if (st) throw Error{st, "device status " + std::to_string(st)};
+  if (st == QD_ERR_NORM) QD_CUDA(cudaMemcpy(&stp, s->status_step, sizeof(int), cudaMemcpyDeviceToHost));
+  throw_status(st, stp);
 }
 
 static void flush_flux(qd_session *s) {
@@ -1350,18 +1381,17 @@ static void run_steps(qd_session *s, int n) {
   }
 }
 
-static void download_psi(qd_session *s, qd_fh2data *const *problems, int n) {
+static void download_psi(qd_session *s, qd_fh2data *const *problems, int n, cudaStream_t st) {
   const int64_t nth_pt = s->g.npt * s->g.nth;
   for (int p = 0; p < n; p++)
     theta_to_host(s, (int64_t)s->h_pblock0[p] * nth_pt, (int64_t)s->probs[p].n_omegas * nth_pt,
-                  problems[p]->OmegaStates.wave_packets);
-  QD_CUDA(cudaStreamSynchronize(s->stream));
+                  problems[p]->OmegaStates.wave_packets, st);
+  QD_CUDA(cudaStreamSynchronize(st));
 }
 
+// P(E) of the accumulators (the flux transform of the buffered steps is already enqueued)
 static void download_crp(qd_session *s, qd_fh2data *const *problems, int n) {
   if (!s->flux.enabled) return;
-  flush_flux(s);
-  launch_flux_crp(s->stream, s->g, s->flux, s->n_problems, s->d_pblock0, s->flux_acc, s->w, s->flux_eta, s->crp);
   const int nE = s->flux.n_energies;
   const int64_t ns = (int64_t)s->g.nth * s->g.n1;
   for (int p = 0; p < n; p++) {
@@ -1490,16 +1520,18 @@ static void evolve(qd_fh2data *const *problems, int n, qd_callback cb, void *use
     const int before = s->steps;
     run_steps(s.get(), seg);
     done += seg;
-    check_status(s.get());
+    const int last = s->steps - 1;   // counter value of the last completed step
+    const bool cb_now = every > 0 && last >= before && last % every == 0;
+    // the status of the last segment is read by the end of the call, beside the downloads
+    if (done < total || op.print_energies || cb_now) check_status(s.get());
     if (op.print_energies) {
       std::vector<double> e((size_t)s->n_blocks * 6);
       QD_CUDA(cudaMemcpy(e.data(), s->energies, e.size() * sizeof(double), cudaMemcpyDeviceToHost));
       std::printf("\n Step: %d\n", s->steps - 1);
       print_energies(s.get(), e);
     }
-    const int last = s->steps - 1;   // counter value of the last completed step
-    if (every > 0 && last >= before && last % every == 0) {
-      download_psi(s.get(), problems, n);
+    if (cb_now) {
+      download_psi(s.get(), problems, n, s->stream);
       for (int p = 0; p < n; p++) problems[p]->time.steps = last;
       if (cb) {
         for (int p = 0; p < n; p++)
@@ -1507,8 +1539,25 @@ static void evolve(qd_fh2data *const *problems, int n, qd_callback cb, void *use
       }
     }
   }
-  check_status(s.get());
-  download_psi(s.get(), problems, n);
+  // End of the call.  The download stream reads the status words once the steps are
+  // done, while the main stream runs the flux transform of the buffered steps and
+  // P(E); psi is copied out only when the status is clean, beside that transform.
+  QD_CUDA(cudaEventRecord(s->ev_steps, s->stream));
+  QD_CUDA(cudaStreamWaitEvent(s->stream_dl, s->ev_steps, 0));
+  QD_CUDA(cudaMemcpyAsync(s->h_status, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream_dl));
+  QD_CUDA(cudaMemcpyAsync(s->h_status + 1, s->status_step, sizeof(int), cudaMemcpyDeviceToHost, s->stream_dl));
+  if (s->flux.enabled) {
+    flush_flux(s.get());
+    launch_flux_crp(s->stream, s->g, s->flux, s->n_problems, s->d_pblock0, s->flux_acc, s->w, s->flux_eta, s->crp,
+                    s->flux_fresh);
+  }
+  QD_CUDA(cudaStreamSynchronize(s->stream_dl));
+  QD_CUDA(cudaGetLastError());
+  if (s->h_status[0]) {
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    throw_status(s->h_status[0], s->h_status[1]);
+  }
+  download_psi(s.get(), problems, n, s->stream_dl);
   download_crp(s.get(), problems, n);
   for (int p = 0; p < n; p++) problems[p]->time.steps = s->steps;
   if (want_rec && total > 0) {
@@ -1602,7 +1651,12 @@ int qd_session_download(qd_session *s, qd_fh2data *const *problems, int32_t n_pr
   QD_GUARD({
     QD_REQUIRE(s && problems && n_problems == s->n_problems, "session download: same problem count");
     check_status(s);
-    download_psi(s, problems, n_problems);
+    download_psi(s, problems, n_problems, s->stream);
+    if (s->flux.enabled) {
+      flush_flux(s);
+      launch_flux_crp(s->stream, s->g, s->flux, s->n_problems, s->d_pblock0, s->flux_acc, s->w, s->flux_eta, s->crp,
+                    s->flux_fresh);
+    }
     download_crp(s, problems, n_problems);
     for (int p = 0; p < n_problems; p++) problems[p]->time.steps = s->steps;
   })
@@ -1795,7 +1849,7 @@ int qd_session_get_psi(qd_session *s, int32_t which, int32_t block, double *host
     QD_REQUIRE(n_doubles == 2 * n, "buffer size");
     QD_CUDA(cudaStreamSynchronize(s->stream));
     if (which == 0) {
-      theta_to_host(s, (int64_t)block * n, (int64_t)n, host_out);
+      theta_to_host(s, (int64_t)block * n, (int64_t)n, host_out, s->stream);
       QD_CUDA(cudaStreamSynchronize(s->stream));
     } else if (s->psi_jf) {   // mixed form: c64 pool, widened exactly
       std::vector<float2> tmp(n);

@@ -250,10 +250,10 @@ void launch_flux_dft(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_b
                      int count, const double *energies, double t0, double dt, double2 *phase_scratch,
                      double2 *acc, const int *status);
 void launch_flux_dft_f32(cudaStream_t s, int64_t ns2, int nE, int n_blocks, const int *count_p, int cap,
-                         const float2 *buf, const double2 *phase, double2 *acc, const int *status);
+                         const float2 *buf, const double2 *phase, double2 *acc, const int *status, const int *fresh);
 void launch_flux_crp(cudaStream_t s, const Grid &g, const FluxConfig &f, int n_problems,
                      const int *block0_of_problem, const double2 *acc, const double *w, const double *eta_sq,
-                     double *crp);
+                     double *crp, const int *fresh);
 
 // table builders (FP64 on the device)
 void launch_build_theta_table(cudaStream_t s, const Grid &g, const double *pot, const double *d1,

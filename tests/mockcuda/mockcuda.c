@@ -84,6 +84,11 @@ cudaError_t cudaLaunchKernelExC(const void *cfg, const void *f, void **args) {
   return 0;
 }
 cudaError_t cudaEventCreate(void **e) { *e = malloc(8); return 0; }
+cudaError_t cudaEventCreateWithFlags(void **e, unsigned flags) { (void)flags; *e = malloc(8); return 0; }
+cudaError_t cudaStreamWaitEvent(cudaStream_t s, void *e, unsigned flags) { (void)s; (void)e; (void)flags; return 0; }
+cudaError_t cudaMallocHost(void **p, size_t n) { *p = calloc(1, n ? n : 1); return *p ? 0 : 2; }
+cudaError_t cudaFreeHost(void *p) { free(p); return 0; }
+cudaError_t cudaHostAlloc(void **p, size_t n, unsigned flags) { (void)flags; *p = calloc(1, n ? n : 1); return *p ? 0 : 2; }
 cudaError_t cudaEventDestroy(void *e) { free(e); return 0; }
 cudaError_t cudaEventRecord(void *e, cudaStream_t s) { (void)e; (void)s; return 0; }
 cudaError_t cudaEventSynchronize(void *e) { (void)e; return 0; }
