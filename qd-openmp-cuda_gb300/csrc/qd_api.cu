@@ -368,6 +368,12 @@ struct qd_session {
   // energy-record arguments the step graph was captured with
   double *graph_rec = nullptr;
   int graph_rec_base = 0, graph_rec_cap = 0;
+  // graphs of 2^k steps (k = 1..5) without a flux transform, for runs shorter than a chunk;
+  // built together, with the energy-record arguments they were captured with
+  static constexpr int N_POW_GRAPHS = 5;
+  cudaGraphExec_t graph_pow[N_POW_GRAPHS + 1] = {};
+  double *pow_rec = nullptr;
+  int pow_rec_base = 0, pow_rec_cap = 0;
 
   template <typename T> T *alloc(size_t n) { return n ? static_cast<T *>(arena.take(n * sizeof(T))) : nullptr; }
   template <typename T> T *upload(const T *h, size_t n) {
@@ -464,6 +470,8 @@ __global__ void k_flux_reset(int *count, int *fresh, const int *status) {
 
 qd_session::~qd_session() {
   if (graph_chunk) cudaGraphExecDestroy(graph_chunk);
+  for (cudaGraphExec_t &e : graph_pow)
+    if (e) cudaGraphExecDestroy(e);
   fft_plan_free(fft);
   if (stream) {
     cudaStreamSynchronize(stream);
@@ -1329,23 +1337,35 @@ static void flush_flux(qd_session *s) {
   }
 }
 
-static void build_chunk_graph(qd_session *s, int steps) {
-  if (s->graph_chunk) {
-    cudaGraphExecDestroy(s->graph_chunk);
-    s->graph_chunk = nullptr;
+// steps (and, with flux, the transform of a full chunk) captured into one graph
+static void capture_steps(qd_session *s, int steps, bool with_flux, cudaGraphExec_t *exec) {
+  if (*exec) {
+    cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
   }
   cudaGraph_t graph;
   QD_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   try {
     for (int i = 0; i < steps; i++) enqueue_step(s, false);
-    if (s->flux.enabled) enqueue_flux_dft(s);
+    if (with_flux) enqueue_flux_dft(s);
   } catch (...) {
     cudaStreamEndCapture(s->stream, &graph);
     throw;
   }
   QD_CUDA(cudaStreamEndCapture(s->stream, &graph));
-  QD_CUDA(cudaGraphInstantiate(&s->graph_chunk, graph, 0));
+  QD_CUDA(cudaGraphInstantiate(exec, graph, 0));
   cudaGraphDestroy(graph);
+}
+
+static void build_pow_graphs(qd_session *s) {
+  for (int k = 1; k <= qd_session::N_POW_GRAPHS; k++) capture_steps(s, 1 << k, false, &s->graph_pow[k]);
+  s->pow_rec = s->rec;
+  s->pow_rec_base = s->rec_base;
+  s->pow_rec_cap = s->rec_cap;
+}
+
+static void build_chunk_graph(qd_session *s, int steps) {
+  capture_steps(s, steps, s->flux.enabled, &s->graph_chunk);
   s->graph_steps = steps;
   s->graph_rec = s->rec;
   s->graph_rec_base = s->rec_base;
@@ -1372,6 +1392,20 @@ static void run_steps(qd_session *s, int n) {
       QD_CUDA(cudaGraphLaunch(s->graph_chunk, s->stream));
       s->steps += chunk;
       n -= chunk;
+      continue;
+    }
+    // shorter runs (up to the next flux transform): the largest 2^k-step graph that fits
+    const int room = s->flux.enabled ? s->flux.chunk - s->flux_pending : chunk;
+    const int m = std::min(n, room);
+    if (m >= 2) {
+      if (!s->graph_pow[1] || s->pow_rec != s->rec || s->pow_rec_base != s->rec_base || s->pow_rec_cap != s->rec_cap)
+        build_pow_graphs(s);
+      int k = qd_session::N_POW_GRAPHS;
+      while ((1 << k) > m) k--;
+      QD_CUDA(cudaGraphLaunch(s->graph_pow[k], s->stream));
+      s->steps += 1 << k;
+      n -= 1 << k;
+      if (s->flux.enabled && (s->flux_pending += 1 << k) == s->flux.chunk) flush_flux(s);
       continue;
     }
     enqueue_step(s, false);
