@@ -108,3 +108,28 @@ def test_every_fft_candidate_matches_oracle(qd, oracle, lib, tmp_path, grid):
         o.forward_fft(); o.evolution_with_kinetic(cfg.dt); o.backward_fft()
         err = np.linalg.norm(got - o.lpsi[0]) / np.linalg.norm(o.lpsi[0])
         assert err < 3e-6, (c, err)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])
+def test_zero_step_call_on_kept_session(qd, lib, prec):
+    """A call of zero steps on a kept session returns P(E) = 0: the accumulators the earlier
+    call left on the device are not read (the first transform of a call writes them, and
+    P(E) of accumulators no transform has written is zero), and psi comes back as it went
+    in (exactly in the FP64 form, rounded to c64 once in the mixed form)."""
+    cfg = qd.inputs.small_config(J=0, n1=32, n2=16, n_theta=8, l_max=6, steps=20, n_energies=8)
+    qd.release_session_cache()
+    first = _run(qd, cfg, prec)
+    assert np.abs(first["CRP"]["CRP"]).max() > 0
+    d = qd.inputs.build_fh2data(cfg)
+    d["options"]["precision"] = prec
+    d["time"]["total_steps"] = 0
+    psi0 = d["OmegaStates"]["wave_packets"].copy()
+    qd.cudaOpenMPEvolution(d)
+    assert int(d["time"]["steps"]) == 0
+    assert np.array_equal(d["CRP"]["CRP"], np.zeros_like(d["CRP"]["CRP"]))
+    if prec == 0:
+        assert np.array_equal(d["OmegaStates"]["wave_packets"], psi0)
+    else:
+        c64 = psi0.astype(np.complex64).astype(np.complex128)
+        assert np.array_equal(d["OmegaStates"]["wave_packets"], c64)
+    qd.release_session_cache()
