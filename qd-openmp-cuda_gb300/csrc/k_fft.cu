@@ -871,8 +871,9 @@ __global__ void __launch_bounds__(THREADS, PIPE ? 2 : (THREADS <= 256 ? 3 : 1))
 // and a column pass (forward column FFT, kinetic phase along r and its energy,
 // inverse, scale, epilogue phase, rotational energy) finishes it.  Same arithmetic as
 // k_fft_slab_sep; what changes is that no CTA waits for another (no cluster barrier,
-// no distributed-shared-memory gather), and every per-l table a CTA needs is fetched
-// into shared memory right at its start, beside the slab's own loads.
+// no distributed-shared-memory gather), and every table a CTA needs (per-l phases,
+// kinetic phase and energy weights, twiddles) is fetched into shared memory right at its
+// start, beside the slab's own loads.
 //
 // Row transposition buffer: element (a, b), a < A, b < B1, of a row at a B1 + (b ^ (a mod
 // B1)) (an XOR swizzle instead of padding), rows RS apart; the twiddle table W^(a b)
@@ -899,6 +900,8 @@ __global__ void __launch_bounds__(T, W * 32 / T)
   float2 *tw = reinterpret_cast<float2 *>(smem_raw);
   float2 *X = tw + N1;
   float2 *pro = X + RPC * RS;
+  float2 *kin = pro + N1;
+  float *t1s = reinterpret_cast<float *>(kin + N1);
   const int tid = threadIdx.x;
   const int sl = blockIdx.x / CR, c = blockIdx.x % CR;
   const int l = __ldg(&slabs[sl].l);
@@ -912,6 +915,8 @@ __global__ void __launch_bounds__(T, W * 32 / T)
     const int a = p / B1, b = (p % B1) ^ (a % B1);
     tw[p] = __ldg(tw1 + a * b);
     if (lf.proR) pro[p] = __ldg(lf.proR + (int64_t)l * N1 + p);
+    kin[p] = __ldg(lf.kinR + p);
+    t1s[p] = __ldg(lf.T1f + p);
   }
   const float2 pr = lf.proR ? __ldg(lf.pror + (int64_t)l * N2 + r) : make_float2(0.0f, 0.0f);
   __syncthreads();
@@ -943,8 +948,8 @@ __global__ void __launch_bounds__(T, W * 32 / T)
     for (int k2 = 0; k2 < B1; k2++) {   // frequency kR = k1 + A k2
       const int kR = j + B1 * h + A * k2;
       float2 &z = w[h * B1 + k2];
-      ke1 = fmaf(__ldg(lf.T1f + kR), z.x * z.x + z.y * z.y, ke1);
-      lift2(z.x, z.y, __ldg(lf.kinR + kR));
+      ke1 = fmaf(t1s[kR], z.x * z.x + z.y * z.y, ke1);
+      lift2(z.x, z.y, kin[kR]);
     }
     RegDFT<B1, true>::run(w + h * B1);
 #pragma unroll
@@ -992,7 +997,9 @@ __global__ void __launch_bounds__(T, W * 32 / T)
   float2 *t2 = reinterpret_cast<float2 *>(smem_raw);
   float2 *Sc = t2 + N2;
   float2 *epi = Sc + A * B2 * CPC;
-  float *i2 = reinterpret_cast<float *>(epi + N2);
+  float2 *kin = epi + N2;
+  float *i2 = reinterpret_cast<float *>(kin + N2);
+  float *t2s = i2 + N2;
   const int tid = threadIdx.x;
   const int sl = blockIdx.x / CC, c = blockIdx.x % CC;
   const int l = __ldg(&slabs[sl].l);
@@ -1003,6 +1010,8 @@ __global__ void __launch_bounds__(T, W * 32 / T)
     t2[p] = __ldg(tw2 + p);
     if (lf.epiR) epi[p] = __ldg(lf.epir + (int64_t)l * N2 + p);
     if (re_part) i2[p] = __ldg(lf.I2f + p);
+    kin[p] = __ldg(lf.kinr + p);
+    t2s[p] = __ldg(lf.T2f + p);
   }
   const float2 eR = lf.epiR ? __ldg(lf.epiR + (int64_t)l * N1 + R) : make_float2(0.0f, 0.0f);
   const float I1 = re_part ? __ldg(lf.I1f + R) : 0.0f;
@@ -1031,8 +1040,8 @@ __global__ void __launch_bounds__(T, W * 32 / T)
       for (int k2 = 0; k2 < B2; k2++) {   // frequency kr = k1 + A k2
         const int kr = jc + B2 * h + A * k2;
         float2 &z = w[h * B2 + k2];
-        ke2 = fmaf(__ldg(lf.T2f + kr), z.x * z.x + z.y * z.y, ke2);
-        lift2(z.x, z.y, __ldg(lf.kinr + kr));
+        ke2 = fmaf(t2s[kr], z.x * z.x + z.y * z.y, ke2);
+        lift2(z.x, z.y, kin[kr]);
       }
       RegDFT<B2, true>::run(w + h * B2);
 #pragma unroll
@@ -1128,12 +1137,13 @@ int sep_cluster() {
 // two-pass form: shared memory of each pass, CTAs per slab of each pass
 template <int A, int B1, int B2, int T>
 size_t split_rows_smem() {
-  return (size_t)A * B1 * sizeof(float2) + ((size_t)(T / B1) * split_row_stride<A, B1>() + A * B1) * sizeof(float2);
+  return (size_t)A * B1 * sizeof(float2) + ((size_t)(T / B1) * split_row_stride<A, B1>() + 2 * A * B1) * sizeof(float2) +
+         (size_t)A * B1 * sizeof(float);
 }
 template <int A, int B1, int B2, int T>
 size_t split_cols_smem() {
-  return (size_t)A * B2 * sizeof(float2) + ((size_t)A * B2 * (T / B2) + A * B2) * sizeof(float2) +
-         (size_t)A * B2 * sizeof(float);
+  return (size_t)A * B2 * sizeof(float2) + ((size_t)A * B2 * (T / B2) + 2 * A * B2) * sizeof(float2) +
+         2 * (size_t)A * B2 * sizeof(float);
 }
 template <int A, int B1, int B2, int T>
 constexpr int split_row_ctas() {
