@@ -115,7 +115,8 @@ def test_zero_step_call_on_kept_session(qd, lib, prec):
     """A call of zero steps on a kept session returns P(E) = 0: the accumulators the earlier
     call left on the device are not read (the first transform of a call writes them, and
     P(E) of accumulators no transform has written is zero), and psi comes back as it went
-    in (exactly in the FP64 form, rounded to c64 once in the mixed form)."""
+    in (exactly in the FP64 form, rounded to c64 once in the mixed form, where values below
+    the smallest normal FP32 number become zero)."""
     cfg = qd.inputs.small_config(J=0, n1=32, n2=16, n_theta=8, l_max=6, steps=20, n_energies=8)
     qd.release_session_cache()
     first = _run(qd, cfg, prec)
@@ -130,6 +131,8 @@ def test_zero_step_call_on_kept_session(qd, lib, prec):
     if prec == 0:
         assert np.array_equal(d["OmegaStates"]["wave_packets"], psi0)
     else:
-        c64 = psi0.astype(np.complex64).astype(np.complex128)
+        def narrow(x):
+            return np.where(np.abs(x) < 2.0 ** -126, 0.0, x.astype(np.float32).astype(np.float64))
+        c64 = narrow(psi0.real) + 1j * narrow(psi0.imag)
         assert np.array_equal(d["OmegaStates"]["wave_packets"], c64)
     qd.release_session_cache()
