@@ -351,7 +351,8 @@ def e2e(qd, precision: int, steps: int, calls: int = 3):
             "calls": calls, "precision": "mixed" if precision else "fp64",
             "first_call": {"value": steps * nb / secs[0], "seconds": secs[0],
                            "note": "the first qd_evolve call of this shape: device buffers, tables and "
-                                   "(at >= 64 steps) the step graph are created inside it"},
+                                   "the step graphs (64-step chunk, 2^k-step graphs for shorter runs) "
+                                   "are created inside it"},
             "note": f"{calls} consecutive qd_evolve calls of K steps each (a chunked run, time.steps carried "
                     "in the struct), after a first call of the same shape; each call: H2D of psi/pot/Legendre "
                     "matrices from pinned memory, potential compared on the device, K steps with their flux "
