@@ -822,9 +822,12 @@ static void autotune_fft(qd_session *s, const qd_fh2data *d0) {
   lf.T2f = s->T2f;
   lf.I1f = s->I1f;
   lf.I2f = s->I2f;
-  cudaEvent_t e0, e1;
-  QD_CUDA(cudaEventCreate(&e0));
-  QD_CUDA(cudaEventCreate(&e1));
+  // each candidate: two warm-up launches, then seven launches between events; the median
+  // launch time decides (the shapes of one grid differ by a few percent, about the spread of
+  // a three-launch average)
+  constexpr int TUNE_REPS = 7;
+  cudaEvent_t ev[TUNE_REPS + 1];
+  for (cudaEvent_t &e : ev) QD_CUDA(cudaEventCreate(&e));
   int best = -1;
   double best_us = 0.0;
   std::string report;
@@ -832,16 +835,17 @@ static void autotune_fft(qd_session *s, const qd_fh2data *d0) {
     fft_plan_choose(p, p.cand[q]);
     double us = -1.0;
     try {
-      launch_fft_kinetic(st, g, p, s->psi_jf, s->d_slabs, s->n_slabs, ke, s->any_coupled ? nullptr : re, s->status, &lf);
-      QD_CUDA(cudaEventRecord(e0, st));
-      for (int r = 0; r < 3; r++)
+      for (int r = 0; r < 2 + TUNE_REPS; r++) {
+        if (r >= 2) QD_CUDA(cudaEventRecord(ev[r - 2], st));
         launch_fft_kinetic(st, g, p, s->psi_jf, s->d_slabs, s->n_slabs, ke, s->any_coupled ? nullptr : re, s->status,
                            &lf);
-      QD_CUDA(cudaEventRecord(e1, st));
-      QD_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.0f;
-      QD_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      us = 1e3 * ms / 3.0;
+      }
+      QD_CUDA(cudaEventRecord(ev[TUNE_REPS], st));
+      QD_CUDA(cudaEventSynchronize(ev[TUNE_REPS]));
+      float ms[TUNE_REPS];
+      for (int r = 0; r < TUNE_REPS; r++) QD_CUDA(cudaEventElapsedTime(&ms[r], ev[r], ev[r + 1]));
+      std::sort(ms, ms + TUNE_REPS);
+      us = 1e3 * ms[TUNE_REPS / 2];
     } catch (const Error &) {
       cudaGetLastError();   // a candidate that cannot launch here is skipped
       QD_CUDA(cudaStreamSynchronize(st));
@@ -852,8 +856,7 @@ static void autotune_fft(qd_session *s, const qd_fh2data *d0) {
       best_us = us;
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
   if (best < 0) throw Error{QD_ERR_CUDA, "autotuner: no FFT kernel could run on this device"};
   fft_plan_choose(p, best);
   s->tuning = "fft: " + fft_choice_name(best) + " (tuned: " + report + " us)";
