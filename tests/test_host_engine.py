@@ -73,6 +73,7 @@ def test_host_engine_over_stand_in_runtime(lib, tmp_path):
     # first process: every FFT candidate of 256x128 timed, the choice written to the file
     assert out["tuning"].startswith("fft: ") and "tuned:" in out["tuning"]
     assert "threads=512" in out["tuning"] and "three-pass" in out["tuning"]
+    assert "two-pass 24 warps/SM" in out["tuning"] and "two-pass 32 warps/SM" in out["tuning"]
     lines = cache.read_text().splitlines()
     assert all(x.startswith("fft_mixed ") and len(x.split("\t")) == 3 for x in lines)
     assert sum("grid 256x128 slabs 8 coupled 0" in x for x in lines) == 1
