@@ -182,14 +182,24 @@ constexpr int WS_THREADS = 512;      // 8 producer warps + 8 consumer warps
 // the loader's stores (32 consecutive points) and the slicer's loads (8
 // points x re/im x two k-groups 8 apart) fall in 32 distinct banks.
 constexpr int TC_LDM = 162, TC_IM = 72;
+// raw staging of the A-in-TMEM form: row k of a tile's c64 values as 128 interleaved floats
+// (re, im of point 0, ...), rows TC_LDR floats apart (8-byte aligned rows for the copies)
+constexpr int TC_LDR = 130;
+// first TMEM column of the A slices in that form (after the three Np-wide accumulators)
+__host__ __device__ inline uint32_t tc_a_col0(int np_max) { return (uint32_t)((3 * np_max + 31) & ~31); }
 // consumer thread that issues the MMA chain: not thread 0, which forms the
 // backward kernel's per-tile module/potential sums after each epilogue
 constexpr int MMA_ISSUER = 32;
 constexpr int WS_PROD = 256;
 
-template <bool FWD>
+// TA (backward only): the A slices live in TMEM instead of shared memory (tcgen05.mma reads A
+// from tensor memory), which frees the shared memory for two raw staging buffers: the producers
+// copy tile t+1 in with cp.async while they slice tile t, so a tile's load and its slicing
+// overlap instead of following each other.
+template <bool FWD, bool TA = false>
 __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int mtiles, int n_tiles, int kp_max,
                                                                    int np_max) {
+  static_assert(!(FWD && TA), "A in TMEM: backward contraction only");
   if (P.status && *P.status) return;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t mb_ready, mb_done, mb_free;
@@ -198,13 +208,15 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   __shared__ float red_s[16];
   __shared__ float tsc_s[256], w_s[256];   // consumers: column scales and (backward) weights of the block
   __shared__ int abort_p, abort_c, n_issued;
+  __shared__ float rmax_s[TA ? 2 : 1][128];   // A-in-TMEM form: the two k halves' row maxima
   const Grid &g = P.g;
-  const uint32_t a_term_max = 16u * (uint32_t)(kp_max / 8 * 128);
+  const uint32_t a_term_max = TA ? 0u : 16u * (uint32_t)(kp_max / 8 * 128);
   const uint32_t b_term_max = (uint32_t)(np_max / 8) * (uint32_t)(kp_max / 8 * 128);
   unsigned char *sA = smem;
   unsigned char *sB = smem + 3 * a_term_max;
   float *sF = reinterpret_cast<float *>(sB + 3 * b_term_max);
-  float *sWV = sF + kp_max * TC_LDM;   // backward: w V of the tile, [n][64 points]
+  float *sWV = sF + (TA ? 2 * kp_max * TC_LDR : kp_max * TC_LDM);   // backward: w V of the tile, [n][64 points]
+  const uint32_t a_col0 = TA ? tc_a_col0(np_max) : 0u;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t ncols = 512;
   const int t_begin = (int)((int64_t)blockIdx.x * n_tiles / gridDim.x);
@@ -225,7 +237,101 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
 
-  if (tid < WS_PROD) {
+  if (TA && tid < WS_PROD) {
+    // =============================== producers, A in TMEM: 256 threads; thread (w, lane)
+    // slices row m = 32 (w & 3) + lane (its warp's TMEM lanes) over half of the k range
+    // raw copy of tile tt into staging buffer buf: row k holds the 64 points' (re, im)
+    auto issue = [&](int tt, int buf) {
+      const TcTile T = tc_tile<false>(P, tt, mtiles);
+      const BlockDesc bd = P.blocks[T.b];
+      const int64_t p0 = (int64_t)T.mt * TC_POINTS;
+      const float2 *A = P.A + (int64_t)bd.slab0 * g.npt;
+      float *dst = sF + buf * kp_max * TC_LDR;
+      for (int q = tid; q < T.Kp * TC_POINTS; q += WS_PROD) {
+        const int k = q / TC_POINTS, pl = q % TC_POINTS;
+        const int64_t pp = p0 + pl;
+        float *d = dst + k * TC_LDR + 2 * pl;
+        if (k < T.Kv && pp < g.npt)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(d)), "l"(A + (int64_t)k * g.npt + pp)
+                       : "memory");
+        else
+          *reinterpret_cast<float2 *>(d) = make_float2(0.0f, 0.0f);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    if (t_begin < t_end) issue(t_begin, 0);
+    int cur_b = -1;
+    const int qd = warp & 3, kh = warp >> 2;
+    const int m = 32 * qd + lane;
+    for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
+      const TcTile T = tc_tile<false>(P, tt, mtiles);
+      const int buf = it & 1;
+      if (tt + 1 < t_end) {
+        issue(tt + 1, buf ^ 1);
+        asm volatile("cp.async.wait_group 1;" ::: "memory");   // this thread's copies of tile tt
+      } else {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+      }
+      named_bar(1, WS_PROD);   // ... and every producer's
+      // the MMA of the previous tile must be done before A (TMEM) and B are rewritten
+      if (tid == 0 && it > 0 && !mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)((it - 1) & 1))) {
+        if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
+        abort_p = 1;
+      }
+      named_bar(1, WS_PROD);
+      if (abort_p) {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");   // no copy lands after the CTA is gone
+        break;
+      }
+      if (T.b != cur_b) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(P.bimg + P.bimg_off[T.b] / 2);
+        uint4 *dst = reinterpret_cast<uint4 *>(sB);
+        const int n16 = (int)(tc_bimg_bytes(T.Np, T.Kp) / 16);
+        for (int q = tid; q < n16; q += WS_PROD) dst[q] = __ldg(src + q);
+        cur_b = T.b;
+      }
+      const float *row = sF + buf * kp_max * TC_LDR + m;   // element k at row[k * TC_LDR]
+      const int KH = T.Kp / 2, k0 = kh * KH;               // KH: a multiple of 8
+      float mx = 0.0f;
+      for (int k = k0; k < k0 + KH; k++) mx = fmaxf(mx, fabsf(row[k * TC_LDR]));
+      rmax_s[kh][m] = mx;
+      named_bar(1, WS_PROD);
+      mx = fmaxf(rmax_s[0][m], rmax_s[1][m]);
+      // mx = f 2^e, f in [0.5, 1): row scale 2^e, slices of a = 256 x / 2^e
+      const int e = mx >= 1e-30f ? (int)((__float_as_uint(mx) >> 23) & 0xffu) - 126 : 0;
+      const float inv = mx >= 1e-30f ? __uint_as_float((uint32_t)(127 + 8 - e) << 23) : 0.0f;
+      if (kh == 0) srow_s[it & 1][m] = __uint_as_float((uint32_t)(127 + e - 16) << 23);
+      auto rne = [](float x) { return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f); };
+      const uint32_t tl = tmem + ((uint32_t)(32 * qd) << 16) + a_col0;
+      for (int kg = 0; kg < KH / 8; kg++) {
+        uint32_t w[3][4];
+#pragma unroll
+        for (int e2 = 0; e2 < 4; e2++) {
+          uint32_t b[3][2];
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const float a = __fmul_rn(row[(k0 + kg * 8 + 2 * e2 + h) * TC_LDR], inv);
+            const float i0 = rne(a);
+            const float r1 = __fmul_rn(__fsub_rn(a, i0), 256.0f);
+            const float i1 = rne(r1);
+            const float i2 = rne(__fmul_rn(__fsub_rn(r1, i1), 256.0f));
+            b[0][h] = __float_as_uint(i0);
+            b[1][h] = __float_as_uint(i1);
+            b[2][h] = __float_as_uint(i2);
+          }
+#pragma unroll
+          for (int t = 0; t < 3; t++) w[t][e2] = __byte_perm(b[t][0], b[t][1], 0x7632);   // even k low
+        }
+#pragma unroll
+        for (int t = 0; t < 3; t++) tmem_st4(tl + (uint32_t)(t * KH + (k0 + kg * 8) / 2), w[t]);
+      }
+      tmem_wait_st();
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the B image, when rewritten
+      tc_fence_before();
+      mbar_arrive(smem_u32(&mb_ready));
+      named_bar(1, WS_PROD);   // the staging buffer and rmax_s are rewritten only after every producer is done
+    }
+  } else if (tid < WS_PROD) {
     // =============================== producers: 256 threads, two per row
     int cur_b = -1;
     for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
@@ -385,7 +491,33 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
           tc_fence_after();
           const uint32_t idesc = make_idesc(128, T.Np);
           const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-          if (2 * T.Np <= 256) {
+          if (TA) {
+            // A term t of k step s: TMEM columns a_col0 + t Kp/2 + 8 s (16 BF16 values)
+            const uint32_t ta = tmem + a_col0, KH = (uint32_t)(T.Kp / 2);
+            if (2 * T.Np <= 256) {
+              const uint32_t idesc2 = make_idesc(128, 2 * T.Np);
+              for (int s = 0; s < T.Kp / 16; s++) {
+                const uint32_t acc = s > 0 ? 1u : 0u;
+                const uint64_t bd0 = make_desc(b0 + s * 256, 128, T.SBO);
+                mma_bf16_ta(tmem, ta + 8 * s, bd0, idesc2, acc);
+                mma_bf16_ta(tmem + (uint32_t)(2 * T.Np), ta + 8 * s,
+                            make_desc(b0 + 2 * T.B_TERM + s * 256, 128, T.SBO), idesc, acc);
+                mma_bf16_ta(tmem + (uint32_t)T.Np, ta + KH + 8 * s, bd0, idesc2, 1u);
+                mma_bf16_ta(tmem + (uint32_t)(2 * T.Np), ta + 2 * KH + 8 * s, bd0, idesc, 1u);
+              }
+            } else {
+              for (int s = 0; s < T.Kp / 16; s++) {
+#pragma unroll
+                for (int q = 0; q < 6; q++) {
+                  const int d = c_pair_a[q] + c_pair_b[q];
+                  const uint64_t bdsc = make_desc(b0 + c_pair_b[q] * T.B_TERM + s * 256, 128, T.SBO);
+                  const bool first = s == 0 && (q == 0 || q == 1 || q == 3);
+                  mma_bf16_ta(tmem + (uint32_t)(d * T.Np), ta + c_pair_a[q] * KH + 8 * s, bdsc, idesc,
+                              first ? 0u : 1u);
+                }
+              }
+            }
+          } else if (2 * T.Np <= 256) {
             // B0 and B1 are adjacent in shared memory and D0, D1, D2 in TMEM, so
             // A0 [B0 B1] -> [D0 D1] and A1 [B0 B1] -> [D1 D2] are single N = 2 Np
             // MMAs: four per k step instead of six, same sums
@@ -526,6 +658,18 @@ bool tc_shape_ok(bool fwd, int Kp, int Np) {
   return Kp <= 192 && Np <= 160 && tc_ws_smem_bytes(fwd, Kp, Np) <= 220 * 1024;
 }
 
+// The backward contraction with its A slices in TMEM: the B slices, two raw staging buffers and
+// the w V tile in shared memory; usable when the accumulators and the A slices share the 512
+// TMEM columns.
+static size_t tc_ta_smem_bytes(int kp_max, int np_max) {
+  const size_t need = (size_t)tc_bimg_bytes(np_max, kp_max) + (size_t)2 * kp_max * TC_LDR * 4 +
+                      (size_t)np_max * TC_POINTS * 4;
+  return std::max(need, (size_t)120 * 1024);
+}
+static bool tc_ta_ok(int kp_max, int np_max) {
+  return tc_a_col0(np_max) + 3u * (uint32_t)(kp_max / 2) <= 512u && tc_ta_smem_bytes(kp_max, np_max) <= 220 * 1024;
+}
+
 int legendre_tc_part_tiles(const Grid &g) { return (int)((g.npt + TC_POINTS - 1) / TC_POINTS); }
 
 
@@ -536,11 +680,15 @@ void launch_legendre_tc_ws(cudaStream_t s, bool fwd, const TcArgs &a, int n_bloc
   QD_CUDA(cudaGetDevice(&dev));
   QD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int grid = std::min(n_tiles, sms);
-  const size_t smem = tc_ws_smem_bytes(fwd, kp_max, np_max);
   if (fwd)
-    k_legendre_tc_ws<true><<<grid, WS_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
+    k_legendre_tc_ws<true><<<grid, WS_THREADS, tc_ws_smem_bytes(true, kp_max, np_max), s>>>(a, mtiles, n_tiles,
+                                                                                             kp_max, np_max);
+  else if (tc_ta_ok(kp_max, np_max))
+    k_legendre_tc_ws<false, true><<<grid, WS_THREADS, tc_ta_smem_bytes(kp_max, np_max), s>>>(a, mtiles, n_tiles,
+                                                                                              kp_max, np_max);
   else
-    k_legendre_tc_ws<false><<<grid, WS_THREADS, smem, s>>>(a, mtiles, n_tiles, kp_max, np_max);
+    k_legendre_tc_ws<false><<<grid, WS_THREADS, tc_ws_smem_bytes(false, kp_max, np_max), s>>>(a, mtiles, n_tiles,
+                                                                                              kp_max, np_max);
 }
 
 
@@ -590,6 +738,8 @@ void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, 
 void tc_set_smem_limit(size_t bytes) {
   QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  QD_CUDA(cudaFuncSetAttribute(k_legendre_tc_ws<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)bytes));
 }
 
 void launch_build_tc_bimage(cudaStream_t s, const BlockDesc *blocks, int n_blocks, const double *Bsrc, int nth,

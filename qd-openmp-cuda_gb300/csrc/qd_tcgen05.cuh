@@ -1,6 +1,7 @@
 // tcgen05 helpers shared by the tensor-core kernels (sm_103a): shared-memory
 // matrix and instruction descriptors, TMEM allocation, the BF16 MMA with an
-// FP32 accumulator in TMEM, its commit to an mbarrier and TMEM loads.
+// FP32 accumulator in TMEM (A from shared or tensor memory), its commit to an
+// mbarrier, TMEM loads and stores.
 #pragma once
 #include <cstdint>
 
@@ -47,6 +48,16 @@ __device__ inline void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
       : "memory");
 }
+// D (TMEM) = A B^T (+ D when acc != 0), A from tensor memory (row m in lane m, BF16 element k
+// in column k / 2, even k in the low half), B from a shared-memory descriptor
+__device__ inline void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(acc)
+      : "memory");
+}
 // arrive once on the mbarrier when every MMA issued so far by this thread is done
 __device__ inline void mma_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
@@ -63,6 +74,13 @@ __device__ inline void tmem_ld16(uint32_t taddr, uint32_t *r) {
       : "r"(taddr));
 }
 __device__ inline void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// tcgen05.st of 4 columns of this thread's lane; tmem_wait_st waits for every store of the thread
+__device__ inline void tmem_st4(uint32_t taddr, const uint32_t *r) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(r[0]), "r"(r[1]),
+               "r"(r[2]), "r"(r[3])
+               : "memory");
+}
+__device__ inline void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ inline void reg_after_wait(uint32_t &x) { asm volatile("" : "+r"(x)); }
 
 }  // namespace qd
