@@ -203,19 +203,24 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   if (P.status && *P.status) return;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t mb_ready, mb_done, mb_free;
+  __shared__ uint64_t mb_tab;   // A-in-TMEM form: a tile's tables and w V are in shared memory
   __shared__ uint32_t tmem_base_s;
   __shared__ float srow_s[2][128];
   __shared__ float red_s[16];
-  __shared__ float tsc_s[256], w_s[256];   // consumers: column scales and (backward) weights of the block
+  // column scales and (backward) weights of the tile's block; in the A-in-TMEM form one set per
+  // tile parity, since the producers drain tile t - 1 while the consumers set up tile t
+  __shared__ float tsc_s[TA ? 2 : 1][256], w_s[TA ? 2 : 1][256];
   __shared__ int abort_p, abort_c, n_issued;
   __shared__ float rmax_s[TA ? 2 : 1][128];   // A-in-TMEM form: the two k halves' row maxima
+  __shared__ float redp_s[16];                // A-in-TMEM form: the producers' energy partials
   const Grid &g = P.g;
   const uint32_t a_term_max = TA ? 0u : 16u * (uint32_t)(kp_max / 8 * 128);
   const uint32_t b_term_max = (uint32_t)(np_max / 8) * (uint32_t)(kp_max / 8 * 128);
   unsigned char *sA = smem;
   unsigned char *sB = smem + 3 * a_term_max;
   float *sF = reinterpret_cast<float *>(sB + 3 * b_term_max);
-  float *sWV = sF + (TA ? 2 * kp_max * TC_LDR : kp_max * TC_LDM);   // backward: w V of the tile, [n][64 points]
+  // backward: w V of the tile, [n][64 points] (two, by tile parity, in the A-in-TMEM form)
+  float *sWV = sF + (TA ? 2 * kp_max * TC_LDR : kp_max * TC_LDM);
   const uint32_t a_col0 = TA ? tc_a_col0(np_max) : 0u;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t ncols = 512;
@@ -226,7 +231,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   if (tid == 0) {
     mbar_init(smem_u32(&mb_ready), WS_PROD);
     mbar_init(smem_u32(&mb_done), 1);
-    mbar_init(smem_u32(&mb_free), WS_THREADS - WS_PROD);
+    mbar_init(smem_u32(&mb_free), TA ? WS_THREADS : WS_THREADS - WS_PROD);   // A in TMEM: both groups drain
+    mbar_init(smem_u32(&mb_tab), WS_THREADS - WS_PROD);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_p = 0;
     abort_c = 0;
@@ -236,6 +242,95 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
+
+  // Drain of one tile's accumulators by one warp: TMEM lanes of quarter qd (rows m = 32 qd +
+  // lane), 16-column chunks n0 = 16 grp, 16 grp + stride, ...; recombination, c64 store and
+  // (backward) the module and potential partials.
+  auto drain = [&](const TcTile &T, const BlockDesc &bd, int itd, int qd, int grp, int stride, float &mod,
+                   float &pe) {
+    const int m = 32 * qd + lane;
+    const int pl = m >> 1, c = m & 1;
+    const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
+    const int par = TA ? (itd & 1) : 0;
+    const float srow = srow_s[itd & 1][m];
+    const float *tsc = tsc_s[par];
+    const float *wq = w_s[par];
+    const float *wv = sWV + (TA ? par * np_max * TC_POINTS : 0);
+    float *Cf = reinterpret_cast<float *>(P.C);
+    const uint32_t trow = tmem + ((uint32_t)(32 * qd) << 16);
+    for (int n0 = 16 * grp; n0 < T.Np; n0 += stride) {
+      uint32_t r0[16], r1[16], r2[16];
+      tmem_ld16(trow + (uint32_t)n0, r0);
+      tmem_ld16(trow + (uint32_t)(T.Np + n0), r1);
+      tmem_ld16(trow + (uint32_t)(2 * T.Np + n0), r2);
+      tmem_wait_ld();   // one wait for the three loads
+      float d0[16], d1[16], d2[16];
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        reg_after_wait(r0[q]);
+        reg_after_wait(r1[q]);
+        reg_after_wait(r2[q]);
+        d0[q] = __uint_as_float(r0[q]);
+        d1[q] = __uint_as_float(r1[q]);
+        d2[q] = __uint_as_float(r2[q]);
+      }
+      if (p < g.npt) {
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const int n = n0 + q;
+          const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc[n]);
+          if (n < T.Nv) {
+            if (FWD) {
+              Cf[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = v;
+            } else {
+              Cf[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = v;
+              const float v2 = v * v;
+              mod = fmaf(wq[n], v2, mod);
+              pe = fmaf(wv[n * TC_POINTS + pl], v2, pe);
+            }
+          }
+        }
+      }
+    }
+  };
+  // A-in-TMEM form: the producers' share of tile itd's drain (column chunks 2 + kh of four, after
+  // the consumers' two), its module and potential partial (slot 2 mt + 1 of the tile), release
+  auto producer_drain = [&](int ttd, int itd) {
+    const TcTile T = tc_tile<false>(P, ttd, mtiles);
+    const BlockDesc bd = P.blocks[T.b];
+    // the consumers have set up this tile's column scales, weights and w V
+    if (tid == 0 && !mbar_wait_bounded(smem_u32(&mb_tab), (uint32_t)(itd & 1))) {
+      if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
+      abort_p = 1;
+    }
+    named_bar(1, WS_PROD);
+    if (abort_p) return;
+    float mod = 0.0f, pe = 0.0f;
+    drain(T, bd, itd, warp & 3, 2 + (warp >> 2), 64, mod, pe);
+    tc_fence_before();
+    mbar_arrive(smem_u32(&mb_free));
+    if (P.part) {
+      for (int o = 16; o > 0; o >>= 1) {
+        mod += __shfl_down_sync(0xffffffffu, mod, o);
+        pe += __shfl_down_sync(0xffffffffu, pe, o);
+      }
+      if (lane == 0) {
+        redp_s[warp] = mod;
+        redp_s[8 + warp] = pe;
+      }
+      named_bar(1, WS_PROD);
+      if (tid == 0) {
+        float ms = 0.0f, ps = 0.0f;
+        for (int q = 0; q < 8; q++) {
+          ms += redp_s[q];
+          ps += redp_s[8 + q];
+        }
+        P.part[((int64_t)T.b * P.n_part_tiles + 2 * T.mt + 1) * 2 + 0] = (double)ms;
+        P.part[((int64_t)T.b * P.n_part_tiles + 2 * T.mt + 1) * 2 + 1] = (double)ps;
+      }
+      named_bar(1, WS_PROD);   // redp_s is rewritten only after thread 0 has read it
+    }
+  };
 
   if (TA && tid < WS_PROD) {
     // =============================== producers, A in TMEM: 256 threads; thread (w, lane)
@@ -279,6 +374,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         abort_p = 1;
       }
       named_bar(1, WS_PROD);
+      tc_fence_after();
       if (abort_p) {
         asm volatile("cp.async.wait_group 0;" ::: "memory");   // no copy lands after the CTA is gone
         break;
@@ -329,7 +425,22 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the B image, when rewritten
       tc_fence_before();
       mbar_arrive(smem_u32(&mb_ready));
+      // the previous tile's accumulators are complete (its MMA was waited for above): drain a share
+      if (it > 0) producer_drain(tt - 1, it - 1);
       named_bar(1, WS_PROD);   // the staging buffer and rmax_s are rewritten only after every producer is done
+    }
+    // the last tile's share, once its MMA is done
+    if (!abort_p && t_end > t_begin) {
+      const int itl = t_end - 1 - t_begin;
+      if (tid == 0 && !mbar_wait_bounded(smem_u32(&mb_done), (uint32_t)(itl & 1))) {
+        if (P.status_w) atomicCAS(P.status_w, 0, QD_ERR_TIMEOUT);
+        abort_p = 1;
+      }
+      named_bar(1, WS_PROD);
+      if (!abort_p) {
+        tc_fence_after();
+        producer_drain(t_end - 1, itl);
+      }
     }
   } else if (tid < WS_PROD) {
     // =============================== producers: 256 threads, two per row
@@ -456,13 +567,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
     // =============================== consumers: 256 threads (+ the MMA issuer, thread 256)
     const int ctid = tid - WS_PROD, cw = warp - WS_PROD / 32;
     const int quarter = warp & 3, chalf = cw >> 2;
-    const int m = 32 * quarter + lane;
-    const int pl = m >> 1, c = m & 1;
     int cons_b = -1;
     for (int tt = t_begin, it = 0; tt < t_end; tt++, it++) {
       const TcTile T = tc_tile<FWD>(P, tt, mtiles);
       const BlockDesc bd = P.blocks[T.b];
-      const int64_t p = (int64_t)T.mt * TC_POINTS + pl;
       // backward: the tile's w V values [n][64 points], copied asynchronously into
       // shared memory before the MMA wait, 16 bytes (4 points) per copy spread over
       // all consumer threads (a 4-byte copy per point where the tile ends early)
@@ -471,7 +579,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
         for (int q = ctid; q < T.Nv * (TC_POINTS / 4); q += WS_THREADS - WS_PROD) {
           const int n = q / (TC_POINTS / 4), c4 = 4 * (q % (TC_POINTS / 4));
           const float *src = P.wv + (int64_t)n * g.npt + p0 + c4;
-          const uint32_t dst = smem_u32(sWV + n * TC_POINTS + c4);
+          const uint32_t dst = smem_u32(sWV + (TA ? (it & 1) * np_max * TC_POINTS : 0) + n * TC_POINTS + c4);
           if (p0 + c4 + 4 <= g.npt) {
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
           } else {
@@ -558,53 +666,20 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
       if (!FWD) asm volatile("cp.async.wait_all;" ::: "memory");   // this thread's w V copies have landed
       named_bar(2, WS_THREADS - WS_PROD);                          // ... and so have everyone's
       if (abort_c) break;
-      if (T.b != cons_b) {
+      if (TA || T.b != cons_b) {   // the A-in-TMEM form keeps one set per tile parity
+        const int par = TA ? (it & 1) : 0;
         for (int n = ctid; n < 256; n += WS_THREADS - WS_PROD) {
-          tsc_s[n] = n < T.Np ? __ldg(P.bscale + (int64_t)T.b * 256 + n) : 0.0f;
-          if (!FWD) w_s[n] = n < T.Nv ? __ldg(P.w + n) : 0.0f;
+          tsc_s[par][n] = n < T.Np ? __ldg(P.bscale + (int64_t)T.b * 256 + n) : 0.0f;
+          if (!FWD) w_s[par][n] = n < T.Nv ? __ldg(P.w + n) : 0.0f;
         }
         cons_b = T.b;
         named_bar(2, WS_THREADS - WS_PROD);
       }
+      if (TA) mbar_arrive(smem_u32(&mb_tab));   // the producers may drain their share of this tile now
       tc_fence_after();
-      const float srow = srow_s[it & 1][m];
       float mod = 0.0f, pe = 0.0f;
-      float *Cf = reinterpret_cast<float *>(P.C);
-      const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
-      for (int n0 = 16 * chalf; n0 < T.Np; n0 += 32) {
-        uint32_t r0[16], r1[16], r2[16];
-        tmem_ld16(trow + (uint32_t)n0, r0);
-        tmem_ld16(trow + (uint32_t)(T.Np + n0), r1);
-        tmem_ld16(trow + (uint32_t)(2 * T.Np + n0), r2);
-        tmem_wait_ld();   // one wait for the three loads
-        float d0[16], d1[16], d2[16];
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-          reg_after_wait(r0[q]);
-          reg_after_wait(r1[q]);
-          reg_after_wait(r2[q]);
-          d0[q] = __uint_as_float(r0[q]);
-          d1[q] = __uint_as_float(r1[q]);
-          d2[q] = __uint_as_float(r2[q]);
-        }
-        if (p < g.npt) {
-#pragma unroll
-          for (int q = 0; q < 16; q++) {
-            const int n = n0 + q;
-            const float v = fmaf(fmaf(d2[q], 0.00390625f, d1[q]), 0.00390625f, d0[q]) * (srow * tsc_s[n]);
-            if (n < T.Nv) {
-              if (FWD) {
-                Cf[2 * ((int64_t)(bd.slab0 + n) * g.npt + p) + c] = v;
-              } else {
-                Cf[2 * (((int64_t)T.b * g.nth + n) * g.npt + p) + c] = v;
-                const float v2 = v * v;
-                mod = fmaf(w_s[n], v2, mod);
-                pe = fmaf(sWV[n * TC_POINTS + pl], v2, pe);
-              }
-            }
-          }
-        }
-      }
+      // the consumers' share: column chunks chalf of two, or (A in TMEM) of four with the producers
+      drain(T, bd, it, quarter, chalf, TA ? 64 : 32, mod, pe);
       tc_fence_before();
       mbar_arrive(smem_u32(&mb_free));
       __syncwarp();
@@ -625,8 +700,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_legendre_tc_ws(TcArgs P, int 
             ms += red_s[q];
             ps += red_s[8 + q];
           }
-          P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 0] = (double)ms;
-          P.part[((int64_t)T.b * P.n_part_tiles + T.mt) * 2 + 1] = (double)ps;
+          const int64_t slot = (int64_t)T.b * P.n_part_tiles + (TA ? 2 * T.mt : T.mt);
+          P.part[slot * 2 + 0] = (double)ms;
+          P.part[slot * 2 + 1] = (double)ps;
         }
       } else if (!FWD) {
         named_bar(2, WS_THREADS - WS_PROD);   // every consumer is done with the w V tile
@@ -659,11 +735,11 @@ bool tc_shape_ok(bool fwd, int Kp, int Np) {
 }
 
 // The backward contraction with its A slices in TMEM: the B slices, two raw staging buffers and
-// the w V tile in shared memory; usable when the accumulators and the A slices share the 512
+// two w V tiles in shared memory; usable when the accumulators and the A slices share the 512
 // TMEM columns.
 static size_t tc_ta_smem_bytes(int kp_max, int np_max) {
   const size_t need = (size_t)tc_bimg_bytes(np_max, kp_max) + (size_t)2 * kp_max * TC_LDR * 4 +
-                      (size_t)np_max * TC_POINTS * 4;
+                      (size_t)2 * np_max * TC_POINTS * 4;
   return std::max(need, (size_t)120 * 1024);
 }
 static bool tc_ta_ok(int kp_max, int np_max) {
@@ -671,6 +747,11 @@ static bool tc_ta_ok(int kp_max, int np_max) {
 }
 
 int legendre_tc_part_tiles(const Grid &g) { return (int)((g.npt + TC_POINTS - 1) / TC_POINTS); }
+// module/potential partial slots per block of the backward contraction: one per tile, or two in
+// the A-in-TMEM form (the consumers' and the producers' share of each tile's drain)
+int legendre_tc_part_slots(const Grid &g, int max_nl) {
+  return legendre_tc_part_tiles(g) * (tc_ta_ok(round16(max_nl), round16(g.nth)) ? 2 : 1);
+}
 
 
 void launch_legendre_tc_ws(cudaStream_t s, bool fwd, const TcArgs &a, int n_blocks, int kp_max, int np_max) {

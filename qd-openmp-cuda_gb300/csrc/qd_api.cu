@@ -1114,7 +1114,7 @@ static void session_build(qd_session *s, qd_fh2data *const *problems, int n_prob
   autotune_fft(s, d0);
 
   // energies and partials
-  s->t_modpe = s->precision == QD_PRECISION_MIXED ? legendre_tc_part_tiles(g) : legendre_bwd_part_tiles(g);
+  s->t_modpe = s->precision == QD_PRECISION_MIXED ? legendre_tc_part_slots(g, s->max_nl) : legendre_bwd_part_tiles(g);
   s->t_ke = fft_col_tiles(s->fft, s->precision);
   // CTAs per group of the FP32 Coriolis passes: twice the base while the groups are few (one
   // coupled problem has about l_max of them), the base for batched runs with thousands, where

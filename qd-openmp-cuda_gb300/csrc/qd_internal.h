@@ -291,6 +291,7 @@ void launch_legendre_tc_bwd(cudaStream_t s, const Grid &g, const float2 *psi_j, 
                             const float *wf, const float *wvf, double *part, int n_part_tiles, size_t smem,
                             const int *status, int *status_w, const float *bscale, int max_nl);
 int legendre_tc_part_tiles(const Grid &g);
+int legendre_tc_part_slots(const Grid &g, int max_nl);
 
 void launch_build_half_v(cudaStream_t s, const Grid &g, const FluxConfig &f, const double *pot, double dt,
                          double2 *half_v);
