@@ -30,6 +30,14 @@
 // commits to an mbarrier; eight consumer warps read their rows (TMEM lanes)
 // back with tcgen05.ld 32x32b, recombine, and store c64.  The backward
 // epilogue also reduces the module and potential energy per tile.
+//
+// The backward contraction runs in a second form (TA) where the A slices live
+// in TMEM (tcgen05.mma reads A from tensor memory: row m in lane m, BF16 element
+// k in column k / 2, even k in the low half) beside the accumulators.  The
+// shared memory that frees holds two raw staging buffers, filled by cp.async one
+// tile ahead, so each tile's load overlaps the previous tile's slicing; the
+// producer warps also drain a quarter of the previous tile's accumulator columns
+// after slicing, once the consumers have published that tile's tables.
 #include <cuda_bf16.h>
 
 
