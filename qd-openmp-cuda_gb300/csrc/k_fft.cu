@@ -1429,6 +1429,12 @@ int fft_row_tiles(const FFTPlan &p, int precision) {
   if (precision == QD_PRECISION_MIXED && p.sep >= 0) return p.sep_re_tiles;
   return (precision == QD_PRECISION_MIXED && p.use_cluster) ? p.cluster : p.n2 / p.rows_per_cta;
 }
+// kernel launches of the mixed form's FFT stage: one for the single-pass kernels, two for the
+// two-pass form, three for the three-pass kernels
+int fft_mixed_launches(const FFTPlan &p) {
+  if (p.sep >= 0) return kSepShapes[p.sep].mode >= 2 ? 2 : 1;
+  return p.use_cluster ? 1 : 3;
+}
 // partial-sum tiles per slab of any mixed-form candidate (buffers sized for tuning)
 int fft_max_tiles(const FFTPlan &p) {
   int t = std::max(p.n1 / p.cols_per_cta, p.n2 / p.rows_per_cta);

@@ -661,8 +661,8 @@ static void enqueue_tail(qd_session *s) {
 }
 
 static int count_launches_per_step(qd_session *s) {
-  const bool slab = s->precision == QD_PRECISION_MIXED && (s->fft.use_cluster || s->fft.sep >= 0);
-  int n = 1 + (slab ? 1 : 3) + 1 + 1;   // fwd, fft, bwd, finalize (+ step counter)
+  const int fft = s->precision == QD_PRECISION_MIXED ? fft_mixed_launches(s->fft) : 3;
+  int n = 1 + fft + 1 + 1;   // fwd, fft, bwd, end of step (energies, norm guard, step counter)
   if (s->cor_f32) n += 2;              // coriolis x2 (rotational energy fused)
   else if (s->any_coupled) n += 3;     // coriolis x2, rot energy
   if (s->flux.enabled && s->precision != QD_PRECISION_MIXED) n += 1;   // surface extraction (fused in the mixed form)

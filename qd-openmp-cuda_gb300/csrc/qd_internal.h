@@ -140,6 +140,7 @@ struct FFTPlan {
 void fft_plan_choose(FFTPlan &p, int choice);
 std::string fft_choice_name(int choice);
 int fft_max_tiles(const FFTPlan &p);
+int fft_mixed_launches(const FFTPlan &p);
 // FP32 three-shear phase tables of the mixed form (float2 (t, s) per entry,
 // see lift tables below); null entries are skipped.
 struct FFTLift {
