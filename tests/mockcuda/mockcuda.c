@@ -16,8 +16,9 @@ typedef struct {
   unsigned x, y, z;
 } mock_dim3;
 
-static int g_launches = 0;
+static int g_launches = 0, g_graph_launches = 0;
 int mock_launches(void) { return g_launches; }
+int mock_graph_launches(void) { return g_graph_launches; }
 
 cudaError_t cudaGetDeviceCount(int *n) { *n = 1; return 0; }
 cudaError_t cudaGetDevice(int *d) { *d = 0; return 0; }
@@ -109,4 +110,4 @@ cudaError_t cudaGraphInstantiate(void **e, void *g, unsigned long long f) {
 }
 cudaError_t cudaGraphDestroy(void *g) { free(g); return 0; }
 cudaError_t cudaGraphExecDestroy(void *e) { free(e); return 0; }
-cudaError_t cudaGraphLaunch(void *e, cudaStream_t s) { (void)e; (void)s; g_launches++; return 0; }
+cudaError_t cudaGraphLaunch(void *e, cudaStream_t s) { (void)e; (void)s; g_launches++; g_graph_launches++; return 0; }

@@ -4,8 +4,9 @@ A child process preloads the stand-in, so device memory is host memory and kerne
 nothing: the numbers are not checked, the host logic is.  qd_evolve twice with the same
 shape reuses the kept session (and with another potential, reloads it); callbacks fire
 after the steps whose counter is a multiple of steps_to_copy_psi_from_device_to_host;
-time.steps is written back; sessions and the autotuner's cache file round-trip (tuned
-once, then read back as "cached" in a fresh process)."""
+time.steps is written back; runs shorter than a flux chunk replay 2^k-step graphs;
+sessions and the autotuner's cache file round-trip (tuned once, then read back as "cached"
+in a fresh process)."""
 import os
 import shutil
 import subprocess
@@ -38,6 +39,18 @@ for prec in (0, 1):
     qd.cudaOpenMPEvolution(d2)                      # same shape, another potential
     out[f"steps3_{prec}"] = int(d2["time"]["steps"])
 qd.release_session_cache()
+# a 20-step run from step 0: step 0 on its own, then 16 + 2 steps from graphs and one more step
+import ctypes
+mock = ctypes.CDLL(None)
+small = qd.inputs.small_config(J=0, n1=16, n2=8, n_theta=8, l_max=7, steps=1, n_energies=8)
+d = qd.inputs.build_fh2data(small); d["options"]["precision"] = 1
+with qd.Session(d) as s:
+    g0 = mock.mock_graph_launches()
+    s.run(20); s.synchronize()
+    out["graphs_20"] = mock.mock_graph_launches() - g0
+    g0 = mock.mock_graph_launches()
+    s.run(20); s.synchronize()   # steps 20-39: 16 + 4
+    out["graphs_20b"] = mock.mock_graph_launches() - g0
 big = qd.inputs.small_config(J=0, n1=256, n2=128, n_theta=8, l_max=7, steps=1, n_energies=8)
 d = qd.inputs.build_fh2data(big); d["options"]["precision"] = 1
 with qd.Session(d) as s:
@@ -67,6 +80,8 @@ def _run_child(tmp_path, cache):
 def test_host_engine_over_stand_in_runtime(lib, tmp_path):
     cache = tmp_path / "autotune.txt"
     out = _run_child(tmp_path, cache)
+    # runs shorter than a flux chunk replay 2^k-step graphs
+    assert out["graphs_20"] == 2 and out["graphs_20b"] == 2
     for prec in (0, 1):
         assert out[f"callbacks_{prec}"] == [0, 3, 6]
         assert out[f"steps_{prec}"] == 7 and out[f"steps2_{prec}"] == 14 and out[f"steps3_{prec}"] == 7
